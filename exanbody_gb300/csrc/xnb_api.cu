@@ -1,0 +1,824 @@
+// C ABI (include/xnb_gpu.h) and the host runtime of a batch: device pools,
+// system admission, and the launch sequence of the reference's operators.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/xnb_gpu.h"
+#include "xnb_launch.cuh"
+
+using namespace xnb;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define XCK(call)                                                                              \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) return fail(XNB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// First-fit allocator of index ranges inside one device pool.
+struct RangeAlloc {
+  uint64_t cap = 0;
+  std::map<uint64_t, uint64_t> free_;  // offset -> length
+  std::map<uint64_t, uint64_t> used_;  // offset -> length
+  void init(uint64_t c) {
+    cap = c;
+    free_.clear();
+    used_.clear();
+    if (c) free_[0] = c;
+  }
+  int64_t alloc(uint64_t n) {
+    if (n == 0) n = 1;
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= n) {
+        const uint64_t off = it->first, len = it->second;
+        free_.erase(it);
+        if (len > n) free_[off + n] = len - n;
+        used_[off] = n;
+        return static_cast<int64_t>(off);
+      }
+    }
+    return -1;
+  }
+  void release(uint64_t off) {
+    auto u = used_.find(off);
+    if (u == used_.end()) return;
+    uint64_t n = u->second;
+    used_.erase(u);
+    auto nx = free_.lower_bound(off);
+    if (nx != free_.end() && off + n == nx->first) {
+      n += nx->second;
+      nx = free_.erase(nx);
+    }
+    if (nx != free_.begin()) {
+      auto pv = std::prev(nx);
+      if (pv->first + pv->second == off) {
+        pv->second += n;
+        return;
+      }
+    }
+    free_[off] = n;
+  }
+  uint64_t high_water() const {
+    if (used_.empty()) return 0;
+    auto it = std::prev(used_.end());
+    return it->first + it->second;
+  }
+};
+
+struct SysHost {
+  bool active = false;
+  SysDesc d{};
+  double list_factor = 1.3;
+  int64_t list_off = -1;
+  uint64_t list_cap = 0;
+  bool initialised = false;
+};
+
+}  // namespace
+
+struct xnb_batch {
+  unsigned long long launches = 0;  // kernels enqueued by this batch (for benchmark accounting)
+  int device = 0;
+  int sm_count = 1;
+  xnb_batch_config cfg{};
+  int stage_cap = 640;
+  DevArrays a{};
+  SysDesc* d_sys = nullptr;
+  SysState* d_st = nullptr;
+  SysState* h_st = nullptr;  // pinned mirror
+  std::vector<SysHost> sys;
+  RangeAlloc parts, cells, lists;
+  std::vector<void*> allocs;
+
+  Extent extent() const {
+    Extent e;
+    e.n_part = static_cast<uint32_t>(parts.high_water());
+    e.n_cells = static_cast<uint32_t>(cells.high_water());
+    int hw = 0;
+    for (size_t s = 0; s < sys.size(); ++s)
+      if (sys[s].active) hw = static_cast<int>(s) + 1;
+    e.nsys = hw;
+    e.sm_count = sm_count;
+    return e;
+  }
+};
+
+struct xnb_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  xnb_batch* batch = nullptr;
+};
+
+namespace {
+
+template <class T>
+int dalloc(xnb_batch* b, T** p, uint64_t n) {
+  void* q = nullptr;
+  const cudaError_t e = cudaMalloc(&q, std::max<uint64_t>(n, 1) * sizeof(T));
+  if (e != cudaSuccess) return fail(XNB_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  b->allocs.push_back(q);
+  *p = static_cast<T*>(q);
+  return XNB_OK;
+}
+
+// domain_periodic_location (core/include/exanb/core/domain.h:160-191) on the host,
+// same operations as the device rebin.
+void periodic_location(const xnb_lj_params& p, double r[3], int loc[3]) {
+  for (int a = 0; a < 3; ++a) {
+    const double rel = r[a] - p.origin[a];
+    long l = static_cast<long>(std::floor(rel / p.cell_size));
+    if (l < 0 || l >= p.dims[a]) {
+      const long old = l;
+      l = ((l % p.dims[a]) + p.dims[a]) % p.dims[a];
+      r[a] += static_cast<double>(l - old) * p.cell_size;
+    }
+    loc[a] = static_cast<int>(l);
+  }
+}
+
+int validate(const xnb_lj_params* p) {
+  if (!p) return fail(XNB_ERR_ARG, "null params");
+  for (int a = 0; a < 3; ++a)
+    if (p->dims[a] < 2) return fail(XNB_ERR_ARG, "domain needs at least 2 cells per axis");
+  if (!(p->cell_size > 0) || !(p->rcut > 0) || !(p->rcut_inc >= 0)) return fail(XNB_ERR_ARG, "bad cutoffs");
+  const double nbh = p->rcut + p->rcut_inc;
+  if (std::ceil(nbh / p->cell_size) != 1.0)
+    return fail(XNB_ERR_ARG, "cell_size must be >= rcut + rcut_inc (one ghost layer, gap 1)");
+  return XNB_OK;
+}
+
+SysDesc make_desc(const xnb_lj_params& p) {
+  SysDesc d{};
+  for (int a = 0; a < 3; ++a) {
+    d.origin[a] = p.origin[a];
+    d.extent[a] = p.extent[a];
+    d.period[a] = p.extent[a] - p.origin[a];
+    d.dims[a] = p.dims[a];
+  }
+  d.cell_size = p.cell_size;
+  const double ghost_dist = (p.rcut + p.rcut_inc) / 1.0;  // nbh_dist.cpp:63-65
+  for (int a = 0; a < 3; ++a) {
+    // block_to_bounds(partner_block) enlarged by max_neighbor_distance (update_ghosts_comm_scheme.cpp:402-403)
+    const double bmin = 0.0 * p.cell_size + p.origin[a];
+    const double bmax = static_cast<double>(p.dims[a]) * p.cell_size + p.origin[a];
+    d.outer_lo[a] = bmin - ghost_dist;
+    d.outer_hi[a] = bmax + ghost_dist;
+  }
+  d.rcut2 = p.rcut * p.rcut;
+  const double nbh = p.rcut + p.rcut_inc;
+  d.nbh2 = nbh * nbh;
+  const double max_displ = p.rcut_inc / 2.0;
+  d.max_displ2 = max_displ * max_displ;
+  d.epsilon = p.epsilon;
+  d.sigma = p.sigma;
+  {
+    // lj_compute_energy at r = rcut (lennard_jones.cu:46-56)
+    const double inv_r = 1.0 / p.rcut;
+    const double ratio = p.sigma * inv_r;
+    const double ratio2 = ratio * ratio;
+    const double ratio6 = ratio2 * ratio2 * ratio2;
+    const double ratio12 = ratio6 * ratio6;
+    d.e_shift = 4. * p.epsilon * (ratio12 - ratio6);
+  }
+  d.m24eps = -24. * p.epsilon;
+  d.eps4 = 4. * p.epsilon;
+  d.eps24 = 24. * p.epsilon;
+  d.sig2 = p.sigma * p.sigma;
+  d.mass = p.mass;
+  d.divide_by_mass = p.divide_by_mass;
+  d.amr_enabled = p.amr_enabled;
+  d.sub_grid_density = p.sub_grid_density > 0 ? p.sub_grid_density : 6.5;
+  d.dt = p.dt;
+  d.dt_full = p.dt * 1.0;
+  d.dt_sq_half = d.dt_full * d.dt_full * 0.5;
+  d.dt_half = p.dt * 0.5;
+  d.sig2_f = static_cast<float>(d.sig2);
+  d.eps24_f = static_cast<float>(d.eps24);
+  d.eps4_f = static_cast<float>(d.eps4);
+  d.e_shift_f = static_cast<float>(d.e_shift);
+  // Error bounds of the FP32 prefilters (u = 2^-24 unit roundoff).
+  //  neighbour test: coordinates are converted relative to cell a's origin, so
+  //  |coord| <= M = 2*cell + nbh; each axis difference then differs from the
+  //  reference's FP64 difference by at most D = (nbh + 2M) u (1.01), and
+  //  |d2_f32 - d2_f64| <= 3 D (2 nbh + D) + 4 u (nbh^2 + 1); margin = 4x that.
+  const double u = std::ldexp(1.0, -24);
+  const double M = 2.0 * p.cell_size + nbh;
+  const double D = (nbh + 2.0 * M) * u * 1.01;
+  const double err_n = 3.0 * D * (2.0 * nbh + D) + 4.0 * u * (nbh * nbh + 1.0);
+  d.nbh2_f = static_cast<float>(d.nbh2);
+  d.nbh_margin_f = static_cast<float>(4.0 * err_n);
+  //  force cutoff test: d_f32 = fl32(d_f64) per axis, |r2_f32 - d2_f64| <= 5.1 u d2;
+  //  margin = 4x at rc^2 (+1 absolute guard so tiny d2 also go to FP64).
+  d.rc2_f = static_cast<float>(d.rcut2);
+  d.rc_margin_f = static_cast<float>(4.0 * 5.1 * u * (d.rcut2 + 1.0));
+  return d;
+}
+
+int upload_desc(xnb_batch* b, int s, cudaStream_t st) {
+  XCK(cudaMemcpyAsync(b->d_sys + s, &b->sys[s].d, sizeof(SysDesc), cudaMemcpyHostToDevice, st));
+  return XNB_OK;
+}
+
+int check_sys(xnb_batch* b, int32_t s) {
+  if (!b) return fail(XNB_ERR_ARG, "null batch");
+  if (s == -1) return XNB_OK;
+  if (s < 0 || s >= static_cast<int32_t>(b->sys.size()) || !b->sys[s].active) return fail(XNB_ERR_ARG, "bad system id");
+  return XNB_OK;
+}
+
+int pull_states(xnb_batch* b, cudaStream_t st) {
+  const Extent ex = b->extent();
+  if (ex.nsys == 0) return XNB_OK;
+  XCK(cudaMemcpyAsync(b->h_st, b->d_st, sizeof(SysState) * ex.nsys, cudaMemcpyDeviceToHost, st));
+  XCK(cudaStreamSynchronize(st));
+  return XNB_OK;
+}
+
+// Neighbour lists for flagged systems: count pass, segment sizing on the host
+// (synchronising), fill pass.
+int neighbors_sync(xnb_batch* b, cudaStream_t st) {
+  const Extent ex = b->extent();
+  b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, st, 1);
+  int rc = pull_states(b, st);
+  if (rc) return rc;
+  bool changed = false;
+  for (int s = 0; s < ex.nsys; ++s) {
+    SysHost& h = b->sys[s];
+    if (!h.active || !b->h_st[s].rebuild) continue;
+    const uint64_t need = b->h_st[s].list_used;
+    if (need > h.list_cap || h.list_off < 0) {
+      if (h.list_off >= 0) b->lists.release(static_cast<uint64_t>(h.list_off));
+      const uint64_t cap = static_cast<uint64_t>(std::ceil(static_cast<double>(need) * h.list_factor)) + 64;
+      const int64_t off = b->lists.alloc(cap);
+      if (off < 0) {
+        h.list_off = -1;
+        h.list_cap = 0;
+        h.d.list_base = 0;
+        h.d.list_cap = 0;
+        upload_desc(b, s, st);
+        return fail(XNB_ERR_NOMEM, "neighbour list pool exhausted");
+      }
+      h.list_off = off;
+      h.list_cap = cap;
+      h.d.list_base = static_cast<uint64_t>(off);
+      h.d.list_cap = cap;
+      rc = upload_desc(b, s, st);
+      if (rc) return rc;
+      changed = true;
+    }
+  }
+  if (changed) {
+    // clear the overflow bit set by the check against the old capacity
+    for (int s = 0; s < ex.nsys; ++s) {
+      if (!b->sys[s].active || !b->h_st[s].rebuild) continue;
+      const uint32_t err = b->h_st[s].error & ~kErrListOverflow;
+      XCK(cudaMemcpyAsync(&b->d_st[s].error, &err, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    }
+  }
+  b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, st, 2);
+  return XNB_OK;
+}
+
+int clear_rebuild(xnb_batch* b, cudaStream_t st) {
+  const Extent ex = b->extent();
+  b->launches += launch_mark_rebuild(ex, b->d_st, 2, -1, st);
+  return XNB_OK;
+}
+
+int check_launch() {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(XNB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return XNB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* xnb_last_error_string(void) { return g_err.c_str(); }
+int xnb_version(void) { return 10000; }
+
+int64_t xnb_system_bytes(int64_t n, int64_t ncells, double list_per_particle) {
+  const int64_t per_part = 8 * 10 + 8 + 4 + 12 + 24 + 8 * 9 + 8 + 4 * 3 + 4 * 3;
+  const int64_t per_cell = 4 * 7 + 8 * 2 + 4;
+  return n * per_part + ncells * per_cell + static_cast<int64_t>(static_cast<double>(n) * list_per_particle) * 4;
+}
+
+int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
+  if (!cfg || !out) return fail(XNB_ERR_ARG, "null argument");
+  if (cfg->particle_capacity <= 0 || cfg->cell_capacity <= 0 || cfg->list_capacity <= 0 || cfg->max_systems <= 0)
+    return fail(XNB_ERR_ARG, "capacities must be positive");
+  if (cfg->particle_capacity >= (1ll << 31) || cfg->cell_capacity >= (1ll << 31))
+    return fail(XNB_ERR_ARG, "capacity above 2^31");
+  XCK(cudaSetDevice(cfg->device));
+  xnb_batch* b = new xnb_batch();
+  b->device = cfg->device;
+  b->cfg = *cfg;
+  if (cfg->stage_cap > 0) b->stage_cap = (cfg->stage_cap + 31) / 32 * 32;
+  cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, cfg->device);
+  const uint64_t P = static_cast<uint64_t>(cfg->particle_capacity);
+  const uint64_t Cc = static_cast<uint64_t>(cfg->cell_capacity);
+  const uint64_t L = static_cast<uint64_t>(cfg->list_capacity);
+  int rc = 0;
+  DevArrays& a = b->a;
+  double** dbl[] = {&a.rx, &a.ry, &a.rz, &a.vx, &a.vy, &a.vz, &a.fx, &a.fy, &a.fz, &a.pe,
+                    &a.rbx, &a.rby, &a.rbz, &a.t_rx, &a.t_ry, &a.t_rz, &a.t_vx, &a.t_vy, &a.t_vz,
+                    &a.t_fx, &a.t_fy, &a.t_fz};
+  for (double** p : dbl) rc = rc ? rc : dalloc(b, p, P);
+  rc = rc ? rc : dalloc(b, &a.id, P);
+  rc = rc ? rc : dalloc(b, &a.t_id, P);
+  uint32_t** u32p[] = {&a.pcell, &a.bkx, &a.bky, &a.bkz, &a.pdest, &a.plocal, &a.mover_list,
+                       &a.nbr_start, &a.nbr_cnt, &a.nbr_cursor};
+  for (uint32_t** p : u32p) rc = rc ? rc : dalloc(b, p, P);
+  uint32_t** u32c[] = {&a.cell_start, &a.cell_n, &a.cell_sys, &a.cell_cnt, &a.cell_stay, &a.cell_nmov,
+                       &a.cell_nbr_tot};
+  for (uint32_t** p : u32c) rc = rc ? rc : dalloc(b, p, Cc + 1);
+  rc = rc ? rc : dalloc(b, &a.cell_scan, Cc + 1);
+  rc = rc ? rc : dalloc(b, &a.cell_nbr_off, Cc + 1);
+  rc = rc ? rc : dalloc(b, &a.scan_blocks, scan_scratch_elems(static_cast<uint32_t>(Cc + 1)) + 8);
+  rc = rc ? rc : dalloc(b, &a.nbr, L);
+  rc = rc ? rc : dalloc(b, &b->d_sys, static_cast<uint64_t>(cfg->max_systems));
+  rc = rc ? rc : dalloc(b, &b->d_st, static_cast<uint64_t>(cfg->max_systems));
+  if (!rc && cudaMallocHost(&b->h_st, sizeof(SysState) * cfg->max_systems) != cudaSuccess)
+    rc = fail(XNB_ERR_NOMEM, "cudaMallocHost failed");
+  if (rc) {
+    xnb_batch_destroy(b);
+    return rc;
+  }
+  cudaMemset(a.pcell, 0xFF, P * sizeof(uint32_t));
+  cudaMemset(a.cell_sys, 0xFF, (Cc + 1) * sizeof(uint32_t));
+  cudaMemset(a.cell_n, 0, (Cc + 1) * sizeof(uint32_t));
+  cudaMemset(a.cell_start, 0, (Cc + 1) * sizeof(uint32_t));
+  cudaMemset(b->d_st, 0, sizeof(SysState) * cfg->max_systems);
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    xnb_batch_destroy(b);
+    return fail(XNB_ERR_CUDA, "initialisation failed");
+  }
+  b->parts.init(P);
+  b->cells.init(Cc);
+  b->lists.init(L);
+  b->sys.resize(static_cast<size_t>(cfg->max_systems));
+  *out = b;
+  return XNB_OK;
+}
+
+int xnb_batch_destroy(xnb_batch* b) {
+  if (!b) return XNB_OK;
+  cudaSetDevice(b->device);
+  cudaDeviceSynchronize();
+  for (void* p : b->allocs) cudaFree(p);
+  if (b->h_st) cudaFreeHost(b->h_st);
+  delete b;
+  return XNB_OK;
+}
+
+int xnb_system_add(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double* rx, const double* ry,
+                   const double* rz, const double* vx, const double* vy, const double* vz, const uint64_t* id,
+                   const int64_t* cell_counts, double list_factor, void* stream, int32_t* sys_out) {
+  if (!b || !sys_out) return fail(XNB_ERR_ARG, "null argument");
+  int rc = validate(p);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!rx || !ry || !rz || !vx || !vy || !vz || !id))) return fail(XNB_ERR_ARG, "bad particle arrays");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  XCK(cudaSetDevice(b->device));
+  int slot = -1;
+  for (size_t s = 0; s < b->sys.size(); ++s)
+    if (!b->sys[s].active) {
+      slot = static_cast<int>(s);
+      break;
+    }
+  if (slot < 0) return fail(XNB_ERR_NOMEM, "no free system slot");
+  const uint64_t ncells = static_cast<uint64_t>(p->dims[0]) * p->dims[1] * p->dims[2];
+  const int64_t poff = b->parts.alloc(static_cast<uint64_t>(n));
+  if (poff < 0) return fail(XNB_ERR_NOMEM, "particle pool exhausted");
+  const int64_t coff = b->cells.alloc(ncells);
+  if (coff < 0) {
+    b->parts.release(static_cast<uint64_t>(poff));
+    return fail(XNB_ERR_NOMEM, "cell pool exhausted");
+  }
+  // Host staging in storage order.
+  std::vector<double> h[6];
+  for (auto& v : h) v.resize(static_cast<size_t>(n));
+  std::vector<uint64_t> hid(static_cast<size_t>(n));
+  std::vector<uint32_t> hcell(static_cast<size_t>(n));
+  std::vector<uint32_t> cstart(ncells), cn(ncells, 0), csys(ncells, static_cast<uint32_t>(slot));
+  if (cell_counts) {
+    int64_t q = 0;
+    for (uint64_t c = 0; c < ncells; ++c) {
+      if (cell_counts[c] < 0) return fail(XNB_ERR_ARG, "negative cell count");
+      cn[c] = static_cast<uint32_t>(cell_counts[c]);
+      cstart[c] = static_cast<uint32_t>(poff + q);
+      for (int64_t t = 0; t < cell_counts[c]; ++t, ++q) {
+        if (q >= n) return fail(XNB_ERR_ARG, "cell counts exceed n");
+        h[0][q] = rx[q]; h[1][q] = ry[q]; h[2][q] = rz[q];
+        h[3][q] = vx[q]; h[4][q] = vy[q]; h[5][q] = vz[q];
+        hid[q] = id[q];
+        hcell[q] = static_cast<uint32_t>(coff + static_cast<int64_t>(c));
+      }
+    }
+    if (q != n) return fail(XNB_ERR_ARG, "cell counts do not sum to n");
+  } else {
+    std::vector<uint32_t> pc(static_cast<size_t>(n));
+    std::vector<double> wr(static_cast<size_t>(n) * 3);
+    for (int64_t q = 0; q < n; ++q) {
+      double r[3] = {rx[q], ry[q], rz[q]};
+      int loc[3];
+      periodic_location(*p, r, loc);
+      pc[q] = static_cast<uint32_t>((static_cast<uint64_t>(loc[2]) * p->dims[1] + loc[1]) * p->dims[0] + loc[0]);
+      wr[q * 3 + 0] = r[0]; wr[q * 3 + 1] = r[1]; wr[q * 3 + 2] = r[2];
+      cn[pc[q]]++;
+    }
+    uint32_t run = static_cast<uint32_t>(poff);
+    for (uint64_t c = 0; c < ncells; ++c) {
+      cstart[c] = run;
+      run += cn[c];
+    }
+    std::vector<uint32_t> fillc(ncells, 0);
+    for (int64_t q = 0; q < n; ++q) {
+      const uint32_t c = pc[q];
+      const uint64_t dst = cstart[c] - static_cast<uint64_t>(poff) + fillc[c]++;
+      h[0][dst] = wr[q * 3 + 0]; h[1][dst] = wr[q * 3 + 1]; h[2][dst] = wr[q * 3 + 2];
+      h[3][dst] = vx[q]; h[4][dst] = vy[q]; h[5][dst] = vz[q];
+      hid[dst] = id[q];
+      hcell[dst] = static_cast<uint32_t>(coff) + c;
+    }
+  }
+  SysHost& sh = b->sys[slot];
+  sh = SysHost{};
+  sh.d = make_desc(*p);
+  sh.d.cell_base = static_cast<uint32_t>(coff);
+  sh.d.ncells = static_cast<uint32_t>(ncells);
+  sh.d.part_base = static_cast<uint32_t>(poff);
+  sh.d.npart = static_cast<uint32_t>(n);
+  sh.list_factor = list_factor >= 1.0 ? list_factor : 1.3;
+  DevArrays& a = b->a;
+  const size_t nb = static_cast<size_t>(n);
+  double* dsts[6] = {a.rx, a.ry, a.rz, a.vx, a.vy, a.vz};
+  for (int k = 0; k < 6; ++k)
+    if (nb) XCK(cudaMemcpyAsync(dsts[k] + poff, h[k].data(), nb * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (nb) {
+    XCK(cudaMemcpyAsync(a.id + poff, hid.data(), nb * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    XCK(cudaMemcpyAsync(a.pcell + poff, hcell.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    XCK(cudaMemsetAsync(a.fx + poff, 0, nb * sizeof(double), st));
+    XCK(cudaMemsetAsync(a.fy + poff, 0, nb * sizeof(double), st));
+    XCK(cudaMemsetAsync(a.fz + poff, 0, nb * sizeof(double), st));
+    XCK(cudaMemsetAsync(a.pe + poff, 0, nb * sizeof(double), st));
+    XCK(cudaMemsetAsync(a.nbr_cnt + poff, 0, nb * sizeof(uint32_t), st));
+    XCK(cudaMemsetAsync(a.nbr_start + poff, 0, nb * sizeof(uint32_t), st));
+  }
+  XCK(cudaMemcpyAsync(a.cell_start + coff, cstart.data(), ncells * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  XCK(cudaMemcpyAsync(a.cell_n + coff, cn.data(), ncells * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  XCK(cudaMemcpyAsync(a.cell_sys + coff, csys.data(), ncells * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  SysState zero{};
+  XCK(cudaMemcpyAsync(b->d_st + slot, &zero, sizeof(SysState), cudaMemcpyHostToDevice, st));
+  sh.active = true;
+  rc = upload_desc(b, slot, st);
+  if (rc) return rc;
+  // host staging buffers are pageable and local: finish the copies before returning
+  XCK(cudaStreamSynchronize(st));
+  *sys_out = slot;
+  return XNB_OK;
+}
+
+int xnb_system_remove(xnb_batch* b, int32_t s, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0) return fail(XNB_ERR_ARG, "remove needs one system");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  SysHost& h = b->sys[s];
+  XCK(cudaMemsetAsync(b->a.pcell + h.d.part_base, 0xFF, static_cast<size_t>(h.d.npart) * sizeof(uint32_t), st));
+  XCK(cudaMemsetAsync(b->a.cell_sys + h.d.cell_base, 0xFF, static_cast<size_t>(h.d.ncells) * sizeof(uint32_t), st));
+  XCK(cudaMemsetAsync(b->a.cell_n + h.d.cell_base, 0, static_cast<size_t>(h.d.ncells) * sizeof(uint32_t), st));
+  SysState zero{};
+  XCK(cudaMemcpyAsync(b->d_st + s, &zero, sizeof(SysState), cudaMemcpyHostToDevice, st));
+  XCK(cudaStreamSynchronize(st));
+  b->parts.release(h.d.part_base);
+  b->cells.release(h.d.cell_base);
+  if (h.list_off >= 0) b->lists.release(static_cast<uint64_t>(h.list_off));
+  h = SysHost{};
+  return XNB_OK;
+}
+
+int xnb_system_info_get(xnb_batch* b, int32_t s, xnb_system_info* info, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0 || !info) return fail(XNB_ERR_ARG, "info needs one system");
+  rc = pull_states(b, static_cast<cudaStream_t>(stream));
+  if (rc) return rc;
+  const SysHost& h = b->sys[s];
+  info->n_particles = h.d.npart;
+  info->n_cells = h.d.ncells;
+  info->list_used = static_cast<int64_t>(b->h_st[s].list_used);
+  info->list_cap = static_cast<int64_t>(h.list_cap);
+  info->rebuilds = static_cast<int64_t>(b->h_st[s].rebuilds);
+  info->error_bits = b->h_st[s].error;
+  info->max_cell = b->h_st[s].max_cell;
+  info->active = h.active ? 1 : 0;
+  info->reserved = 0;
+  return XNB_OK;
+}
+
+int xnb_system_download(xnb_batch* b, int32_t s, double* rx, double* ry, double* rz, double* vx, double* vy,
+                        double* vz, double* fx, double* fy, double* fz, uint64_t* id, int32_t* cell, double* pe,
+                        void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0) return fail(XNB_ERR_ARG, "download needs one system");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const SysHost& h = b->sys[s];
+  const size_t n = h.d.npart, o = h.d.part_base;
+  double* outs[10] = {rx, ry, rz, vx, vy, vz, fx, fy, fz, pe};
+  const double* ins[10] = {b->a.rx, b->a.ry, b->a.rz, b->a.vx, b->a.vy, b->a.vz, b->a.fx, b->a.fy, b->a.fz, b->a.pe};
+  for (int k = 0; k < 10; ++k)
+    if (outs[k] && n) XCK(cudaMemcpyAsync(outs[k], ins[k] + o, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (id && n) XCK(cudaMemcpyAsync(id, b->a.id + o, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+  std::vector<uint32_t> pc;
+  if (cell && n) {
+    pc.resize(n);
+    XCK(cudaMemcpyAsync(pc.data(), b->a.pcell + o, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  }
+  XCK(cudaStreamSynchronize(st));
+  if (cell)
+    for (size_t q = 0; q < n; ++q) cell[q] = static_cast<int32_t>(pc[q] - h.d.cell_base);
+  return XNB_OK;
+}
+
+int xnb_system_pairs(xnb_batch* b, int32_t s, uint64_t* id_a, uint64_t* id_b, int32_t* nbh_count, int64_t cap,
+                     int64_t* n_out, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0) return fail(XNB_ERR_ARG, "pairs needs one system");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const SysHost& h = b->sys[s];
+  rc = pull_states(b, st);
+  if (rc) return rc;
+  const size_t n = h.d.npart, o = h.d.part_base;
+  std::vector<uint32_t> start(n), cnt(n);
+  std::vector<uint64_t> ids(n);
+  const uint64_t used = b->h_st[s].list_used;
+  std::vector<uint32_t> list(used);
+  if (n) {
+    XCK(cudaMemcpyAsync(start.data(), b->a.nbr_start + o, n * 4, cudaMemcpyDeviceToHost, st));
+    XCK(cudaMemcpyAsync(cnt.data(), b->a.nbr_cnt + o, n * 4, cudaMemcpyDeviceToHost, st));
+    XCK(cudaMemcpyAsync(ids.data(), b->a.id + o, n * 8, cudaMemcpyDeviceToHost, st));
+  }
+  if (used && h.list_off >= 0)
+    XCK(cudaMemcpyAsync(list.data(), b->a.nbr + h.d.list_base, used * 4, cudaMemcpyDeviceToHost, st));
+  XCK(cudaStreamSynchronize(st));
+  int64_t k = 0;
+  for (size_t q = 0; q < n; ++q) {
+    if (nbh_count) nbh_count[q] = static_cast<int32_t>(cnt[q]);
+    for (uint32_t t = 0; t < cnt[q]; ++t, ++k) {
+      if (k < cap) {
+        const uint64_t pos = static_cast<uint64_t>(start[q]) + t;
+        if (pos >= used) return fail(XNB_ERR_DEVICE, "neighbour entry outside the list segment");
+        const uint32_t e = list[pos];
+        if (id_a) id_a[k] = ids[q];
+        if (id_b) id_b[k] = ids[e >> 5];
+      }
+    }
+  }
+  if (n_out) *n_out = k;
+  return XNB_OK;
+}
+
+int xnb_system_energy(xnb_batch* b, int32_t s, double* ke, double* pe, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0) return fail(XNB_ERR_ARG, "energy needs one system");
+  const SysHost& h = b->sys[s];
+  const size_t n = h.d.npart;
+  std::vector<double> v[3], e(n);
+  for (auto& x : v) x.resize(n);
+  rc = xnb_system_download(b, s, nullptr, nullptr, nullptr, v[0].data(), v[1].data(), v[2].data(), nullptr, nullptr,
+                           nullptr, nullptr, nullptr, e.data(), stream);
+  if (rc) return rc;
+  double k = 0.0, p = 0.0;
+  for (size_t q = 0; q < n; ++q) {
+    k += 0.5 * h.d.mass * ((v[0][q] * v[0][q] + v[1][q] * v[1][q]) + v[2][q] * v[2][q]);
+    p += e[q];
+  }
+  if (ke) *ke = k;
+  if (pe) *pe = p;
+  return XNB_OK;
+}
+
+int xnb_init_particles(xnb_batch* b, int32_t s, int32_t precision, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (precision < 0 || precision > 2) return fail(XNB_ERR_ARG, "bad precision");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  XCK(cudaSetDevice(b->device));
+  const Extent ex = b->extent();
+  // init marks every selected system; the counter then starts from zero
+  b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, st);
+  b->launches += launch_rebin(ex, b->d_sys, b->d_st, b->a, st);
+  rc = neighbors_sync(b, st);
+  if (rc) return rc;
+  b->launches += launch_force(ex, b->d_sys, b->d_st, b->a, precision, true, false, s, st);
+  rc = pull_states(b, st);
+  if (rc) return rc;
+  for (int q = 0; q < ex.nsys; ++q) {
+    if (!b->sys[q].active || !b->h_st[q].rebuild) continue;
+    b->h_st[q].rebuilds = 0;
+    b->h_st[q].moved = 0;
+    b->h_st[q].rebuild = 0;
+    XCK(cudaMemcpyAsync(b->d_st + q, b->h_st + q, sizeof(SysState), cudaMemcpyHostToDevice, st));
+    b->sys[q].initialised = true;
+  }
+  XCK(cudaStreamSynchronize(st));
+  rc = check_launch();
+  if (rc) return rc;
+  return xnb_check_errors(b, stream);
+}
+
+int xnb_push_f_v_r(xnb_batch* b, int32_t s, double dt_scale, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  const Extent ex = b->extent();
+  b->launches += launch_first_half(ex, b->d_sys, b->d_st, b->a, true, false, false, dt_scale, 0.0, true, s,
+                    static_cast<cudaStream_t>(stream));
+  return check_launch();
+}
+
+int xnb_push_f_v(xnb_batch* b, int32_t s, double dt_scale, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  const Extent ex = b->extent();
+  b->launches += launch_first_half(ex, b->d_sys, b->d_st, b->a, false, true, false, 1.0, dt_scale, true, s,
+                    static_cast<cudaStream_t>(stream));
+  return check_launch();
+}
+
+int xnb_particle_displ_over(xnb_batch* b, int32_t s, int64_t* count_out, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const Extent ex = b->extent();
+  b->launches += launch_clear_moved(ex, b->d_st, st);
+  b->launches += launch_first_half(ex, b->d_sys, b->d_st, b->a, false, false, true, 1.0, 0.5, true, s, st);
+  rc = pull_states(b, st);
+  if (rc) return rc;
+  if (count_out) {
+    if (s >= 0) {
+      count_out[0] = static_cast<int64_t>(b->h_st[s].moved);
+    } else {
+      for (int q = 0; q < ex.nsys; ++q) count_out[q] = static_cast<int64_t>(b->h_st[q].moved);
+    }
+  }
+  return check_launch();
+}
+
+int xnb_update_particles_full(xnb_batch* b, int32_t s, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const Extent ex = b->extent();
+  b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, st);
+  b->launches += launch_rebin(ex, b->d_sys, b->d_st, b->a, st);
+  rc = neighbors_sync(b, st);
+  if (rc) return rc;
+  clear_rebuild(b, st);
+  return check_launch();
+}
+
+int xnb_chunk_neighbors(xnb_batch* b, int32_t s, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const Extent ex = b->extent();
+  b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, st);
+  rc = neighbors_sync(b, st);
+  if (rc) return rc;
+  clear_rebuild(b, st);
+  return check_launch();
+}
+
+int xnb_backup_r(xnb_batch* b, int32_t s, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const Extent ex = b->extent();
+  b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, st);
+  b->launches += launch_backup(ex, b->d_sys, b->d_st, b->a, st);
+  clear_rebuild(b, st);
+  return check_launch();
+}
+
+int xnb_lennard_jones_force(xnb_batch* b, int32_t s, int32_t precision, int32_t with_energy, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (precision < 0 || precision > 2) return fail(XNB_ERR_ARG, "bad precision");
+  const Extent ex = b->extent();
+  b->launches += launch_force(ex, b->d_sys, b->d_st, b->a, precision, with_energy != 0, false, s, static_cast<cudaStream_t>(stream));
+  return check_launch();
+}
+
+int xnb_ghost_update_r(xnb_batch* b, int32_t s, void*) { return check_sys(b, s); }
+
+int xnb_step(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, void* stream) {
+  if (!b) return fail(XNB_ERR_ARG, "null batch");
+  if (precision < 0 || precision > 2) return fail(XNB_ERR_ARG, "bad precision");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const Extent ex = b->extent();
+  const bool exact = precision == XNB_PREC_FP64_EXACT;
+  const bool energy = (flags & XNB_STEP_ENERGY) != 0;
+  for (int k = 0; k < nsteps; ++k) {
+    // verlet_first_half + trigger_move_particles
+    b->launches += launch_first_half(ex, b->d_sys, b->d_st, b->a, true, true, true, 1.0, 0.5, exact, -1, st);
+    b->launches += launch_mark_rebuild(ex, b->d_st, 1, -1, st);
+    bool rebuild = true;
+    if (flags & XNB_STEP_HOST_SYNC) {
+      int rc = pull_states(b, st);
+      if (rc) return rc;
+      rebuild = false;
+      for (int q = 0; q < ex.nsys; ++q)
+        if (b->sys[q].active && b->h_st[q].moved > 0) rebuild = true;
+    }
+    if (rebuild) {
+      // update_particles_full
+      b->launches += launch_rebin(ex, b->d_sys, b->d_st, b->a, st);
+      if (flags & XNB_STEP_HOST_SYNC) {
+        int rc = neighbors_sync(b, st);
+        if (rc) return rc;
+      } else {
+        b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, st, 3);
+      }
+    }
+    // compute_all_forces_energy + verlet_second_half
+    b->launches += launch_force(ex, b->d_sys, b->d_st, b->a, precision, energy, true, -1, st);
+    b->launches += launch_clear_moved(ex, b->d_st, st);
+  }
+  return check_launch();
+}
+
+int xnb_step_graph_create(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, void* stream,
+                          xnb_graph** out) {
+  if (!b || !out) return fail(XNB_ERR_ARG, "null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (st == nullptr) return fail(XNB_ERR_ARG, "graph capture needs a non-default stream");
+  XCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  const int rc = xnb_step(b, nsteps, precision, flags & ~XNB_STEP_HOST_SYNC, stream);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(st, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(XNB_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+  xnb_graph* G = new xnb_graph();
+  G->graph = g;
+  G->batch = b;
+  const cudaError_t ie = cudaGraphInstantiate(&G->exec, g, 0);
+  if (ie != cudaSuccess) {
+    cudaGraphDestroy(g);
+    delete G;
+    return fail(XNB_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ie));
+  }
+  *out = G;
+  return XNB_OK;
+}
+
+int xnb_graph_launch(xnb_graph* g, void* stream) {
+  if (!g) return fail(XNB_ERR_ARG, "null graph");
+  XCK(cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream)));
+  return XNB_OK;
+}
+
+int xnb_graph_destroy(xnb_graph* g) {
+  if (!g) return XNB_OK;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+  return XNB_OK;
+}
+
+int xnb_check_errors(xnb_batch* b, void* stream) {
+  if (!b) return fail(XNB_ERR_ARG, "null batch");
+  int rc = pull_states(b, static_cast<cudaStream_t>(stream));
+  if (rc) return rc;
+  const Extent ex = b->extent();
+  for (int q = 0; q < ex.nsys; ++q) {
+    if (!b->sys[q].active) continue;
+    const uint32_t e = b->h_st[q].error;
+    if (e & kErrListOverflow) return fail(XNB_ERR_CAPACITY, "neighbour list segment overflow in system " + std::to_string(q));
+    if (e) return fail(XNB_ERR_DEVICE, "device error bits " + std::to_string(e) + " in system " + std::to_string(q));
+  }
+  return XNB_OK;
+}
+
+int64_t xnb_stats_kernel_launches(const xnb_batch* b) { return b ? static_cast<int64_t>(b->launches) : -1; }
+
+}  // extern "C"

@@ -1,0 +1,698 @@
+// Rebuild-path kernels: move/rebin with periodic wrap, AMR in-cell ordering,
+// backup_r, and the cell-grid neighbour build; plus the device scan they use.
+#include "xnb_launch.cuh"
+
+namespace xnb {
+
+namespace {
+
+constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+constexpr uint32_t kMoverBit = 0x80000000u;
+
+__device__ __forceinline__ bool sys_flagged(const SysState* st, uint32_t s) { return st[s].rebuild != 0; }
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// sub_grid_size (amr/include/exanb/amr/amr_grid_algorithm.h:66-78): the largest
+// side s with s^3 <= n/density (1 below side 2, capped at 16), computed from the
+// same double n/density the reference feeds to cbrt.
+__device__ __forceinline__ int sub_grid_side(uint32_t n, double density) {
+  if (n == 0) return 0;
+  const double x = __ddiv_rn(static_cast<double>(n), density);
+  if (x < 8.0) return 1;
+  int s = 2;
+  while (s < 16 && static_cast<double>((s + 1) * (s + 1) * (s + 1)) <= x) ++s;
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// K_r1: destination cell of each particle of a rebuilding system.
+// move_particles_across_cells (grid_cell_particles/include/exanb/grid_cell_particles/
+// move_particles_across_cells.h:115-152): dst = domain_periodic_location(r)
+// (core/include/exanb/core/domain.h:160-191, wrapping r by whole cells), and the
+// particle leaves its cell when dst differs or it lies >= epsilon outside dst's bounds.
+__global__ void __launch_bounds__(256)
+    k_rebin_dest(uint32_t n_part, const SysDesc* __restrict__ sys, SysState* st, DevArrays a) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
+    const uint32_t c = a.pcell[i];
+    if (c == kInvalid) continue;
+    const uint32_t s = a.cell_sys[c];
+    if (!sys_flagged(st, s)) continue;
+    const SysDesc& S = sys[s];
+    int ci, cj, ck;
+    cell_ijk(S, c - S.cell_base, ci, cj, ck);
+    const double ro[3] = {a.rx[i], a.ry[i], a.rz[i]};
+    double r[3] = {ro[0], ro[1], ro[2]};
+    int loc[3];
+    bool bad = false;
+    for (int ax = 0; ax < 3; ++ax) {
+      const double rel = __dsub_rn(r[ax], S.origin[ax]);
+      const double q = floor(__ddiv_rn(rel, S.cell_size));
+      if (!(fabs(q) < 1.0e9)) {
+        bad = true;
+        loc[ax] = 0;
+        continue;
+      }
+      int l = static_cast<int>(q);
+      if (l < 0 || l >= S.dims[ax]) {
+        const int old = l;
+        l = pmod_i(l, S.dims[ax]);
+        r[ax] = __dadd_rn(r[ax], __dmul_rn(static_cast<double>(l - old), S.cell_size));
+      }
+      loc[ax] = l;
+    }
+    if (bad) {
+      atomicOr(&st[s].error, kErrCellIndex);
+      a.pdest[i] = c;
+      continue;
+    }
+    // min_distance2_between(ro, cell_bounds(dst)) >= epsilon_cell_size2 (grid.h:60,89-90; geometry.h:137-153)
+    double d[3];
+    for (int ax = 0; ax < 3; ++ax) {
+      const double lo = cell_lo(S, ax, loc[ax]);
+      const double hi = cell_lo(S, ax, loc[ax] + 1);
+      d[ax] = 0.0;
+      if (ro[ax] < lo) d[ax] = __dsub_rn(lo, ro[ax]);
+      else if (ro[ax] > hi) d[ax] = __dsub_rn(ro[ax], hi);
+    }
+    const double md2 = norm2_rn(d[0], d[1], d[2]);
+    const double eps = __dmul_rn(0x1p-48, S.cell_size);
+    const bool same = (loc[0] == ci && loc[1] == cj && loc[2] == ck);
+    const bool mover = !same || md2 >= __dmul_rn(eps, eps);
+    const uint32_t dst = S.cell_base + static_cast<uint32_t>((loc[2] * S.dims[1] + loc[1]) * S.dims[0] + loc[0]);
+    if (mover) {
+      // arrivals are gathered from the 26 neighbouring cells only
+      const int dd[3] = {pmod_i(loc[0] - ci, S.dims[0]), pmod_i(loc[1] - cj, S.dims[1]), pmod_i(loc[2] - ck, S.dims[2])};
+      for (int ax = 0; ax < 3; ++ax)
+        if (!(dd[ax] == 0 || dd[ax] == 1 || dd[ax] == S.dims[ax] - 1)) atomicOr(&st[s].error, kErrFarMover);
+      a.rx[i] = r[0];
+      a.ry[i] = r[1];
+      a.rz[i] = r[2];
+    }
+    a.pdest[i] = mover ? (dst | kMoverBit) : c;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K_r2: per source cell, compaction of the staying particles and list of movers.
+// The hole left by a mover is filled with the current last particle, scanning
+// from the top (move_particles_across_cells.h:186-207).
+__global__ void __launch_bounds__(128)
+    k_rebin_compact(uint32_t n_cells, const SysDesc* __restrict__ sys, const SysState* __restrict__ st,
+                    DevArrays a) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_cells; c += warps) {
+    const uint32_t s = a.cell_sys[c];
+    if (s == kInvalid || !sys_flagged(st, s)) continue;
+    const uint32_t start = a.cell_start[c];
+    const uint32_t n = a.cell_n[c];
+    // movers, in particle order, via ballots
+    uint32_t nmov = 0;
+    for (uint32_t q0 = 0; q0 < n; q0 += 32) {
+      const uint32_t q = q0 + lane;
+      const bool mv = q < n && (a.pdest[start + q] & kMoverBit);
+      const unsigned m = __ballot_sync(0xffffffffu, mv);
+      if (mv) a.mover_list[start + nmov + __popc(m & lanemask_lt())] = start + q;
+      if (q < n) a.plocal[start + q] = mv ? kInvalid : q;
+      nmov += __popc(m);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      uint32_t ncur = n;
+      for (int q = static_cast<int>(n) - 1; q >= 0; --q) {
+        if (a.plocal[start + q] == kInvalid) {
+          if (static_cast<uint32_t>(q) + 1 < ncur) a.plocal[start + q] = a.plocal[start + ncur - 1];
+          --ncur;
+        }
+      }
+      a.cell_stay[c] = ncur;
+      a.cell_nmov[c] = nmov;
+    }
+  }
+}
+
+// The (up to) 27 source cells around destination cell c, sorted by global cell
+// index, duplicates removed: arrivals are appended in (source cell, source
+// index) order, the order one thread of the reference's OpenMP loop produces.
+struct SrcInfo {
+  uint32_t src;    // source cell (kInvalid if unused / duplicate)
+  uint32_t rank;   // position in sorted order
+  uint32_t count;  // movers from src into c
+  uint32_t offset; // exclusive prefix of counts in sorted order
+};
+
+__device__ __forceinline__ SrcInfo arrivals_of(const SysDesc& S, const DevArrays& a, uint32_t c, uint32_t lane) {
+  int ci, cj, ck;
+  cell_ijk(S, c - S.cell_base, ci, cj, ck);
+  uint32_t src = kInvalid;
+  if (lane < 27) {
+    const int di = static_cast<int>(lane % 3) - 1, dj = static_cast<int>((lane / 3) % 3) - 1,
+              dk = static_cast<int>(lane / 9) - 1;
+    const int ni = pmod_i(ci + di, S.dims[0]), nj = pmod_i(cj + dj, S.dims[1]), nk = pmod_i(ck + dk, S.dims[2]);
+    src = S.cell_base + static_cast<uint32_t>((nk * S.dims[1] + nj) * S.dims[0] + ni);
+  }
+  uint32_t rank = 0;
+  bool dup = false;
+  for (uint32_t m = 0; m < 27; ++m) {
+    const uint32_t o = __shfl_sync(0xffffffffu, src, m);
+    if (lane < 27) {
+      if (o < src) ++rank;
+      if (o == src && m < lane) dup = true;
+    }
+  }
+  uint32_t count = 0;
+  if (lane < 27 && !dup) {
+    const uint32_t st0 = a.cell_start[src];
+    const uint32_t nm = a.cell_nmov[src];
+    for (uint32_t m = 0; m < nm; ++m) {
+      const uint32_t p = a.mover_list[st0 + m];
+      if ((a.pdest[p] & ~kMoverBit) == c) ++count;
+    }
+  }
+  if (dup) src = kInvalid;
+  // offset = sum of counts of lanes with smaller rank
+  uint32_t offset = 0;
+  for (uint32_t m = 0; m < 27; ++m) {
+    const uint32_t rm = __shfl_sync(0xffffffffu, rank, m);
+    const uint32_t cm = __shfl_sync(0xffffffffu, count, m);
+    if (rm < rank) offset += cm;
+  }
+  return SrcInfo{src, rank, count, offset};
+}
+
+// K_r3: new particle count of every cell (flagged systems: stayers + arrivals).
+__global__ void __launch_bounds__(128)
+    k_rebin_count(uint32_t n_cells, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_cells; c += warps) {
+    const uint32_t s = a.cell_sys[c];
+    if (s == kInvalid) {
+      if (lane == 0) a.cell_cnt[c] = 0;
+      continue;
+    }
+    if (!sys_flagged(st, s)) {
+      if (lane == 0) a.cell_cnt[c] = a.cell_n[c];
+      continue;
+    }
+    const SrcInfo si = arrivals_of(sys[s], a, c, lane);
+    uint32_t tot = si.count;
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    if (lane == 0) a.cell_cnt[c] = a.cell_stay[c] + tot;
+  }
+}
+
+// K_r5: gather stayers then arrivals of each destination cell into the scratch arrays.
+__global__ void __launch_bounds__(128)
+    k_rebin_scatter(uint32_t n_cells, const SysDesc* __restrict__ sys, const SysState* __restrict__ st,
+                    DevArrays a) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_cells; c += warps) {
+    const uint32_t s = a.cell_sys[c];
+    if (s == kInvalid || !sys_flagged(st, s)) continue;
+    const SysDesc& S = sys[s];
+    const uint32_t ns = S.part_base + static_cast<uint32_t>(a.cell_scan[c] - a.cell_scan[S.cell_base]);
+    const uint32_t start = a.cell_start[c];
+    const uint32_t stay = a.cell_stay[c];
+    for (uint32_t q = lane; q < stay; q += 32) {
+      const uint32_t src = start + a.plocal[start + q];
+      const uint32_t dst = ns + q;
+      a.t_rx[dst] = a.rx[src]; a.t_ry[dst] = a.ry[src]; a.t_rz[dst] = a.rz[src];
+      a.t_vx[dst] = a.vx[src]; a.t_vy[dst] = a.vy[src]; a.t_vz[dst] = a.vz[src];
+      a.t_fx[dst] = a.fx[src]; a.t_fy[dst] = a.fy[src]; a.t_fz[dst] = a.fz[src];
+      a.t_id[dst] = a.id[src];
+    }
+    const SrcInfo si = arrivals_of(S, a, c, lane);
+    if (si.src != kInvalid && si.count > 0) {
+      const uint32_t st0 = a.cell_start[si.src];
+      const uint32_t nm = a.cell_nmov[si.src];
+      uint32_t k = 0;
+      for (uint32_t m = 0; m < nm; ++m) {
+        const uint32_t p = a.mover_list[st0 + m];
+        if ((a.pdest[p] & ~kMoverBit) != c) continue;
+        const uint32_t dst = ns + stay + si.offset + k++;
+        a.t_rx[dst] = a.rx[p]; a.t_ry[dst] = a.ry[p]; a.t_rz[dst] = a.rz[p];
+        a.t_vx[dst] = a.vx[p]; a.t_vy[dst] = a.vy[p]; a.t_vz[dst] = a.vz[p];
+        a.t_fx[dst] = a.fx[p]; a.t_fy[dst] = a.fy[p]; a.t_fz[dst] = a.fz[p];
+        a.t_id[dst] = a.id[p];
+      }
+    }
+  }
+}
+
+// K_r6: final in-cell order (rebuild_amr's stable sort by sub-cell,
+// amr_grid_algorithm.h:131-374, when the cell is dense enough for a sub-grid),
+// cell table update, and backup_r (io/backup_r.cpp:56-79).
+__global__ void __launch_bounds__(128)
+    k_rebin_finalize(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_cells; c += warps) {
+    const uint32_t s = a.cell_sys[c];
+    if (s == kInvalid || !sys_flagged(st, s)) continue;
+    const SysDesc& S = sys[s];
+    const uint32_t ns = S.part_base + static_cast<uint32_t>(a.cell_scan[c] - a.cell_scan[S.cell_base]);
+    const uint32_t n = a.cell_cnt[c];
+    int ci, cj, ck;
+    cell_ijk(S, c - S.cell_base, ci, cj, ck);
+    const double lo[3] = {cell_lo(S, 0, ci), cell_lo(S, 1, cj), cell_lo(S, 2, ck)};
+    const int side = S.amr_enabled ? sub_grid_side(n, S.sub_grid_density) : 1;
+    if (side > 1) {
+      // sub-cell key of each particle (Grid::particle_pcoord, grid.h:184-190), kept in pdest
+      for (uint32_t q = lane; q < n; q += 32) {
+        const double r[3] = {a.t_rx[ns + q], a.t_ry[ns + q], a.t_rz[ns + q]};
+        int key = 0;
+        int sidx[3];
+        for (int ax = 0; ax < 3; ++ax) {
+          const double pc = __ddiv_rn(__dsub_rn(r[ax], lo[ax]), S.cell_size);
+          long long v = __double2ll_rz(__dmul_rn(pc, static_cast<double>(side)));
+          v = v < 0 ? 0 : (v > side - 1 ? side - 1 : v);
+          sidx[ax] = static_cast<int>(v);
+        }
+        key = (sidx[2] * side + sidx[1]) * side + sidx[0];
+        a.pdest[ns + q] = static_cast<uint32_t>(key);
+      }
+      __syncwarp();
+      for (uint32_t q = lane; q < n; q += 32) {
+        const uint32_t kq = a.pdest[ns + q];
+        uint32_t rank = 0;
+        for (uint32_t p = 0; p < n; ++p) {
+          const uint32_t kp = a.pdest[ns + p];
+          rank += (kp < kq) || (kp == kq && p < q);
+        }
+        a.plocal[ns + q] = rank;
+      }
+      __syncwarp();
+    }
+    for (uint32_t q = lane; q < n; q += 32) {
+      const uint32_t src = ns + q;
+      const uint32_t dst = ns + (side > 1 ? a.plocal[ns + q] : q);
+      const double x = a.t_rx[src], y = a.t_ry[src], z = a.t_rz[src];
+      a.rx[dst] = x; a.ry[dst] = y; a.rz[dst] = z;
+      a.vx[dst] = a.t_vx[src]; a.vy[dst] = a.t_vy[src]; a.vz[dst] = a.t_vz[src];
+      a.fx[dst] = a.t_fx[src]; a.fy[dst] = a.t_fy[src]; a.fz[dst] = a.t_fz[src];
+      a.id[dst] = a.t_id[src];
+      a.pcell[dst] = c;
+      const uint32_t bx = encode_u32(x, lo[0], S.cell_size);
+      const uint32_t by = encode_u32(y, lo[1], S.cell_size);
+      const uint32_t bz = encode_u32(z, lo[2], S.cell_size);
+      a.bkx[dst] = bx; a.bky[dst] = by; a.bkz[dst] = bz;
+      a.rbx[dst] = restore_u32(bx, lo[0], S.cell_size);
+      a.rby[dst] = restore_u32(by, lo[1], S.cell_size);
+      a.rbz[dst] = restore_u32(bz, lo[2], S.cell_size);
+    }
+    if (lane == 0) {
+      a.cell_start[c] = ns;
+      a.cell_n[c] = n;
+      atomicMax(&st[s].max_cell, n);
+    }
+  }
+}
+
+// backup_r alone (io/backup_r.cpp:42-79) for flagged systems.
+__global__ void __launch_bounds__(256)
+    k_backup(uint32_t n_part, const SysDesc* __restrict__ sys, SysState* st, DevArrays a) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
+    const uint32_t c = a.pcell[i];
+    if (c == kInvalid) continue;
+    const uint32_t s = a.cell_sys[c];
+    if (!sys_flagged(st, s)) continue;
+    const SysDesc& S = sys[s];
+    int ci, cj, ck;
+    cell_ijk(S, c - S.cell_base, ci, cj, ck);
+    const double lo[3] = {cell_lo(S, 0, ci), cell_lo(S, 1, cj), cell_lo(S, 2, ck)};
+    const uint32_t bx = encode_u32(a.rx[i], lo[0], S.cell_size);
+    const uint32_t by = encode_u32(a.ry[i], lo[1], S.cell_size);
+    const uint32_t bz = encode_u32(a.rz[i], lo[2], S.cell_size);
+    a.bkx[i] = bx; a.bky[i] = by; a.bkz[i] = bz;
+    a.rbx[i] = restore_u32(bx, lo[0], S.cell_size);
+    a.rby[i] = restore_u32(by, lo[1], S.cell_size);
+    a.rbz[i] = restore_u32(bz, lo[2], S.cell_size);
+  }
+}
+
+__global__ void k_arm(int nsys, SysState* st) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys && st[s].rebuild) st[s].rebuild_armed = 1;
+}
+
+// ---------------------------------------------------------------------------
+// chunk_neighbors_execute (particle_neighbors/include/exanb/particle_neighbors/
+// chunk_neighbors_execute.h:110-244, 286-372): for each particle of cell a, the
+// particles of the 27 cells around a (periodic images included) with
+// (cell_a != cell_b || p_a != p_b) && 0 < d2 <= nbh_dist^2, d2 = norm2(r_a - r_b),
+// in (cell_enc, p_b) order. Candidates are staged per warp in shared memory as
+// FP32 coordinates relative to cell a's origin; the FP32 distance decides
+// whenever it is farther than a proven error bound from the threshold, and the
+// FP64 d2 of the reference decides the rest, so the pair set is bit-exact.
+// Ghost particles outside the partner block enlarged by ghost_dist are not
+// candidates (update_ghosts_comm_scheme.cpp:462-469).
+// One warp per cell, lanes over candidates, ballot compaction keeps the order.
+template <bool FILL>
+__global__ void __launch_bounds__(128)
+    k_neighbors(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap) {
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t wib = threadIdx.x >> 5;
+  float4* srel = reinterpret_cast<float4*>(smem_raw) + static_cast<size_t>(wib) * cap;
+  uint32_t* sent = reinterpret_cast<uint32_t*>(reinterpret_cast<float4*>(smem_raw) + static_cast<size_t>(blockDim.x >> 5) * cap) +
+                   static_cast<size_t>(wib) * cap;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + wib; c < n_cells; c += warps) {
+    const uint32_t s = a.cell_sys[c];
+    if (s == kInvalid) continue;
+    if (!sys_flagged(st, s)) {
+      if (!FILL && lane == 0) a.cell_nbr_tot[c] = 0;
+      continue;
+    }
+    if (FILL && (st[s].error & kErrListOverflow)) continue;
+    const SysDesc& S = sys[s];
+    const uint32_t sa = a.cell_start[c];
+    const uint32_t na = a.cell_n[c];
+    if (na == 0) {
+      if (!FILL && lane == 0) a.cell_nbr_tot[c] = 0;
+      continue;
+    }
+    int ci, cj, ck;
+    cell_ijk(S, c - S.cell_base, ci, cj, ck);
+    const double o[3] = {cell_lo(S, 0, ci), cell_lo(S, 1, cj), cell_lo(S, 2, ck)};
+
+    if (FILL) {
+      // per-particle list starts: cell offset + prefix of the counts
+      uint32_t run = static_cast<uint32_t>(a.cell_nbr_off[c] - a.cell_nbr_off[S.cell_base]);
+      for (uint32_t q0 = 0; q0 < na; q0 += 32) {
+        const uint32_t q = q0 + lane;
+        const uint32_t cnt = q < na ? a.nbr_cnt[sa + q] : 0;
+        uint32_t inc = cnt;
+        for (int off = 1; off < 32; off <<= 1) {
+          const uint32_t v = __shfl_up_sync(0xffffffffu, inc, off);
+          if (lane >= static_cast<uint32_t>(off)) inc += v;
+        }
+        if (q < na) {
+          a.nbr_start[sa + q] = run + inc - cnt;
+          a.nbr_cursor[sa + q] = run + inc - cnt;
+        }
+        run += __shfl_sync(0xffffffffu, inc, 31);
+      }
+      __syncwarp();
+    }
+
+    // group table: lane g < 27 describes neighbour cell g in (dk, dj, di) order
+    uint32_t g_start = 0, g_n = 0, g_code = kImageCenter;
+    if (lane < 27) {
+      const int di = static_cast<int>(lane % 3) - 1, dj = static_cast<int>((lane / 3) % 3) - 1,
+                dk = static_cast<int>(lane / 9) - 1;
+      int n3[3] = {ci + di, cj + dj, ck + dk};
+      int img[3];
+      for (int ax = 0; ax < 3; ++ax) {
+        img[ax] = 1;
+        if (n3[ax] < 0) { n3[ax] += S.dims[ax]; img[ax] = 0; }
+        else if (n3[ax] >= S.dims[ax]) { n3[ax] -= S.dims[ax]; img[ax] = 2; }
+      }
+      const uint32_t src = S.cell_base + static_cast<uint32_t>((n3[2] * S.dims[1] + n3[1]) * S.dims[0] + n3[0]);
+      g_start = a.cell_start[src];
+      g_n = a.cell_n[src];
+      g_code = static_cast<uint32_t>(img[0] + 3 * img[1] + 9 * img[2]);
+    }
+    uint32_t g_off = g_n;  // inclusive scan over lanes
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint32_t v = __shfl_up_sync(0xffffffffu, g_off, off);
+      if (lane >= static_cast<uint32_t>(off)) g_off += v;
+    }
+    const uint32_t ncand = __shfl_sync(0xffffffffu, g_off, 26);
+    g_off -= g_n;
+
+    const float nb_hi = S.nbh2_f + S.nbh_margin_f;
+    const float nb_lo = S.nbh2_f - S.nbh_margin_f;
+    const float nb_zero = S.nbh_margin_f;
+    uint32_t cell_total = 0;
+
+    for (uint32_t c0 = 0; c0 < ncand; c0 += static_cast<uint32_t>(cap)) {
+      const uint32_t c1 = min(ncand, c0 + static_cast<uint32_t>(cap));
+      // stage candidates [c0, c1)
+      for (int g = 0; g < 27; ++g) {
+        const uint32_t gs = __shfl_sync(0xffffffffu, g_start, g);
+        const uint32_t gn = __shfl_sync(0xffffffffu, g_n, g);
+        const uint32_t go = __shfl_sync(0xffffffffu, g_off, g);
+        const uint32_t gc = __shfl_sync(0xffffffffu, g_code, g);
+        if (go + gn <= c0 || go >= c1) continue;
+        for (uint32_t q = lane; q < gn; q += 32) {
+          const uint32_t t = go + q;
+          if (t < c0 || t >= c1) continue;
+          const uint32_t j = gs + q;
+          const double xb = image_coord(a.rx[j], S.period[0], static_cast<int>(gc % 3u));
+          const double yb = image_coord(a.ry[j], S.period[1], static_cast<int>((gc / 3u) % 3u));
+          const double zb = image_coord(a.rz[j], S.period[2], static_cast<int>(gc / 9u));
+          bool keep = true;
+          if (gc != static_cast<uint32_t>(kImageCenter)) {
+            keep = xb >= S.outer_lo[0] && xb <= S.outer_hi[0] && yb >= S.outer_lo[1] && yb <= S.outer_hi[1] &&
+                   zb >= S.outer_lo[2] && zb <= S.outer_hi[2];
+          }
+          srel[t - c0] = make_float4(static_cast<float>(__dsub_rn(xb, o[0])), static_cast<float>(__dsub_rn(yb, o[1])),
+                                     static_cast<float>(__dsub_rn(zb, o[2])), 0.f);
+          sent[t - c0] = keep ? (((j - S.part_base) << 5) | gc) : kInvalid;
+        }
+      }
+      __syncwarp();
+      const uint32_t m = c1 - c0;
+      for (uint32_t pa = 0; pa < na; ++pa) {
+        const uint32_t i = sa + pa;
+        const double xa = a.rx[i], ya = a.ry[i], za = a.rz[i];
+        const float ax = static_cast<float>(__dsub_rn(xa, o[0]));
+        const float ay = static_cast<float>(__dsub_rn(ya, o[1]));
+        const float az = static_cast<float>(__dsub_rn(za, o[2]));
+        const uint32_t self_ent = ((i - S.part_base) << 5) | static_cast<uint32_t>(kImageCenter);
+        uint32_t cnt = 0;
+        uint32_t cursor = 0;
+        if (FILL) cursor = a.nbr_cursor[i];
+        for (uint32_t t0 = 0; t0 < m; t0 += 32) {
+          const uint32_t t = t0 + lane;
+          bool hit = false;
+          uint32_t ent = kInvalid;
+          if (t < m) {
+            ent = sent[t];
+            if (ent != kInvalid && ent != self_ent) {
+              const float4 b = srel[t];
+              const float dx = ax - b.x, dy = ay - b.y, dz = az - b.z;
+              const float d2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+              if (d2f > nb_hi) {
+                hit = false;
+              } else if (d2f < nb_lo && d2f > nb_zero) {
+                hit = true;
+              } else {
+                const uint32_t j = S.part_base + (ent >> 5);
+                const uint32_t gc = ent & 31u;
+                const double xb = image_coord(a.rx[j], S.period[0], static_cast<int>(gc % 3u));
+                const double yb = image_coord(a.ry[j], S.period[1], static_cast<int>((gc / 3u) % 3u));
+                const double zb = image_coord(a.rz[j], S.period[2], static_cast<int>(gc / 9u));
+                const double d2 = norm2_rn(__dsub_rn(xa, xb), __dsub_rn(ya, yb), __dsub_rn(za, zb));
+                hit = d2 > 0.0 && d2 <= S.nbh2;
+              }
+            }
+          }
+          const unsigned mask = __ballot_sync(0xffffffffu, hit);
+          if (FILL) {
+            if (hit) a.nbr[S.list_base + cursor + __popc(mask & lanemask_lt())] = ent;
+            cursor += __popc(mask);
+          } else {
+            cnt += __popc(mask);
+          }
+        }
+        if (lane == 0) {
+          if (FILL) {
+            a.nbr_cursor[i] = cursor;
+          } else {
+            a.nbr_cnt[i] = (c0 == 0 ? 0u : a.nbr_cnt[i]) + cnt;
+          }
+        }
+        cell_total += cnt;
+      }
+      __syncwarp();
+    }
+    if (!FILL && lane == 0) a.cell_nbr_tot[c] = cell_total;
+  }
+}
+
+// Segment capacity check after the per-cell scan.
+__global__ void k_nbr_check(int nsys, const SysDesc* __restrict__ sys, SysState* st, const DevArrays a) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys || !st[s].rebuild) return;
+  const SysDesc& S = sys[s];
+  if (S.ncells == 0) return;
+  const unsigned long long tot = a.cell_nbr_off[S.cell_base + S.ncells] - a.cell_nbr_off[S.cell_base];
+  st[s].list_used = tot;
+  if (tot > S.list_cap) atomicOr(&st[s].error, kErrListOverflow);
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan, u32 -> u64, three phases (tile sums, scan of sums, tiles).
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr uint32_t kScanTile = kScanThreads * kScanItems;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* __restrict__ in, uint32_t n,
+                                                              unsigned long long* sums) {
+  __shared__ unsigned long long red[kScanThreads / 32];
+  const uint32_t base = blockIdx.x * kScanTile;
+  unsigned long long v = 0;
+  for (int k = 0; k < kScanItems; ++k) {
+    const uint32_t idx = base + threadIdx.x + k * kScanThreads;
+    if (idx < n) v += in[idx];
+  }
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int w = 0; w < kScanThreads / 32; ++w) t += red[w];
+    sums[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(unsigned long long* sums, uint32_t nb) {
+  __shared__ unsigned long long carry_s;
+  __shared__ unsigned long long wsum[32];
+  if (threadIdx.x == 0) carry_s = 0;
+  __syncthreads();
+  for (uint32_t b0 = 0; b0 < nb; b0 += 1024) {
+    const uint32_t b = b0 + threadIdx.x;
+    const unsigned long long x = b < nb ? sums[b] : 0ull;
+    unsigned long long inc = x;
+    const uint32_t lane = threadIdx.x & 31;
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, inc, off);
+      if (lane >= static_cast<uint32_t>(off)) inc += y;
+    }
+    if (lane == 31) wsum[threadIdx.x >> 5] = inc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      unsigned long long w = wsum[threadIdx.x];
+      unsigned long long wi = w;
+      for (int off = 1; off < 32; off <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, wi, off);
+        if (threadIdx.x >= static_cast<uint32_t>(off)) wi += y;
+      }
+      wsum[threadIdx.x] = wi - w;
+    }
+    __syncthreads();
+    const unsigned long long carry = carry_s;
+    if (b < nb) sums[b] = carry + wsum[threadIdx.x >> 5] + inc - x;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry_s = carry + wsum[31] + inc;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_final(const uint32_t* __restrict__ in, uint32_t n,
+                                                              const unsigned long long* __restrict__ sums,
+                                                              unsigned long long* out) {
+  __shared__ unsigned long long wsum[kScanThreads / 32];
+  const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  unsigned long long loc[kScanItems];
+  unsigned long long t = 0;
+  for (int k = 0; k < kScanItems; ++k) {
+    const uint32_t idx = base + k;
+    loc[k] = idx < n ? in[idx] : 0ull;
+    t += loc[k];
+  }
+  const uint32_t lane = threadIdx.x & 31;
+  unsigned long long inc = t;
+  for (int off = 1; off < 32; off <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, inc, off);
+    if (lane >= static_cast<uint32_t>(off)) inc += y;
+  }
+  if (lane == 31) wsum[threadIdx.x >> 5] = inc;
+  __syncthreads();
+  unsigned long long wpre = 0;
+  for (uint32_t w = 0; w < (threadIdx.x >> 5); ++w) wpre += wsum[w];
+  unsigned long long run = sums[blockIdx.x] + wpre + inc - t;
+  for (int k = 0; k < kScanItems; ++k) {
+    const uint32_t idx = base + k;
+    if (idx < n) out[idx] = run;
+    run += loc[k];
+    if (idx + 1 == n) out[n] = run;
+  }
+}
+
+inline int warp_grid(uint32_t n_items, int warps_per_block, int sm_count) {
+  long long want = (static_cast<long long>(n_items) + warps_per_block - 1) / warps_per_block;
+  const long long cap = static_cast<long long>(sm_count) * 16;
+  if (want > cap) want = cap;
+  return static_cast<int>(want < 1 ? 1 : want);
+}
+
+inline int thread_grid(uint32_t n, int threads, int sm_count) {
+  long long want = (static_cast<long long>(n) + threads - 1) / threads;
+  const long long cap = static_cast<long long>(sm_count) * 8;
+  if (want > cap) want = cap;
+  return static_cast<int>(want < 1 ? 1 : want);
+}
+
+}  // namespace
+
+size_t scan_scratch_elems(uint32_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
+
+int launch_scan_u32_to_u64(const uint32_t* in, unsigned long long* out, uint32_t n, unsigned long long* scratch,
+                           cudaStream_t stream) {
+  if (n == 0) {
+    cudaMemsetAsync(out, 0, sizeof(unsigned long long), stream);
+    return 0;
+  }
+  const uint32_t nb = (n + kScanTile - 1) / kScanTile;
+  k_scan_tiles<<<nb, kScanThreads, 0, stream>>>(in, n, scratch);
+  k_scan_sums<<<1, 1024, 0, stream>>>(scratch, nb);
+  k_scan_final<<<nb, kScanThreads, 0, stream>>>(in, n, scratch, out);
+  return 3;
+}
+
+int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream) {
+  if (ex.n_part == 0 || ex.n_cells == 0) return 0;
+  k_rebin_dest<<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
+  const int wg = warp_grid(ex.n_cells, 4, ex.sm_count);
+  k_rebin_compact<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
+  k_rebin_count<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
+  const int ns = launch_scan_u32_to_u64(a.cell_cnt, a.cell_scan, ex.n_cells, a.scan_blocks, stream);
+  k_rebin_scatter<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
+  k_rebin_finalize<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
+  k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st);
+  return 6 + ns;
+}
+
+int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream) {
+  if (ex.n_part == 0) return 0;
+  k_backup<<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
+  k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st);
+  return 2;
+}
+
+int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int cap,
+                     cudaStream_t stream, int mode) {
+  if (ex.n_cells == 0) return 0;
+  int count = 0;
+  const size_t smem = static_cast<size_t>(4) * cap * (sizeof(float4) + sizeof(uint32_t));
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_neighbors<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_neighbors<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    attr_set = true;
+  }
+  const int wg = warp_grid(ex.n_cells, 4, ex.sm_count);
+  if (mode & 1) {
+    k_neighbors<false><<<wg, 128, smem, stream>>>(ex.n_cells, sys, st, a, cap);
+    count += 2 + launch_scan_u32_to_u64(a.cell_nbr_tot, a.cell_nbr_off, ex.n_cells, a.scan_blocks, stream);
+    k_nbr_check<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, sys, st, a);
+  }
+  if (mode & 2) {
+    k_neighbors<true><<<wg, 128, smem, stream>>>(ex.n_cells, sys, st, a, cap);
+    ++count;
+  }
+  return count;
+}
+
+}  // namespace xnb

@@ -1,0 +1,152 @@
+// Internal definitions shared by the xnb CUDA translation units.
+//
+// Device data model (one "batch" holds one or many independent periodic systems):
+//   * particles of all systems are packed in one SoA set of arrays, system after
+//     system, and inside a system cell after cell (cells in the reference's linear
+//     order (k*Dj+j)*Di+i, grid_algorithm.h:84-91), inside a cell in the
+//     reference's in-cell order;
+//   * cell_start[c] .. cell_start[c+1] is cell c's particle range (global index);
+//   * there are no ghost cells in memory: a neighbour entry carries a periodic
+//     image code and the image position x + (+-1.0)*(max-min) is recomputed where
+//     it is needed, which is the same rounding as the reference's ghost copy
+//     (ghosts_comm_scheme.h:76-80);
+//   * neighbour lists are per particle, in the reference's stream order
+//     (cell_enc, p_b) (chunk_neighbors_execute.h:308), as u32 entries
+//     (local particle index << 5) | image code, in one list segment per system.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace xnb {
+
+constexpr int kImageCenter = 13;  // image code of the unshifted image: (0+1) + 3*(0+1) + 9*(0+1)
+
+enum ErrorBits : uint32_t {
+  kErrListOverflow = 1u << 0,   // neighbour list segment too small
+  kErrFarMover = 1u << 1,       // a particle moved further than one cell between rebuilds
+  kErrCellIndex = 1u << 2,      // a particle outside the periodic domain grid
+  kErrStage = 1u << 3,          // staging capacity exceeded (programming error)
+};
+
+// Per-system constants, device resident (SysDesc[nsys]).
+struct SysDesc {
+  double origin[3];
+  double extent[3];
+  double period[3];      // extent - origin: the ghost image offset (rmax - rmin)
+  double outer_lo[3];    // ghost particle filter bounds: block bounds -/+ ghost_dist
+  double outer_hi[3];
+  double cell_size;
+  double rcut2;          // rcut*rcut (compute_cell_particle_pairs.h:145)
+  double nbh2;           // (rcut+rcut_inc)^2 (chunk_neighbors_execute.h:75-76)
+  double max_displ2;     // (rcut_inc/2)^2 (nbh_dist.cpp:48, particle_displ_over.cu:111)
+  double epsilon, sigma, e_shift;
+  double mass;
+  double dt;
+  double dt_full, dt_sq_half, dt_half;  // dt*1.0, (dt*dt)*0.5, dt*0.5 (push_vec3_2nd_order.h:87-88)
+  double sub_grid_density;
+  float nbh2_f, nbh_margin_f;  // FP32 prefilter of the neighbour test and its proven error margin
+  float rc2_f, rc_margin_f;    // same for the force cutoff test (mixed path)
+  float sig2_f, eps24_f, eps4_f, e_shift_f;
+  double m24eps, eps4, sig2, eps24;  // -24*eps, 4*eps (lennard_jones.cu:54-55), sigma^2, 24*eps
+  int32_t dims[3];
+  int32_t divide_by_mass;
+  int32_t amr_enabled;
+  uint32_t cell_base, ncells;
+  uint32_t part_base, npart;
+  uint64_t list_base, list_cap;
+};
+
+// Per-system mutable state, device resident (SysState[nsys]).
+struct SysState {
+  unsigned long long moved;     // particles over the displacement threshold (this step)
+  unsigned long long list_used; // entries of the current neighbour lists
+  uint32_t rebuild;             // 1 when the rebuild path must run for this system
+  uint32_t error;               // ErrorBits
+  uint32_t max_cell;            // largest cell occupancy after the last rebin
+  uint32_t rebuild_armed;        // 1 once backup_r has run (the trigger needs a backup)
+  unsigned long long rebuilds;
+};
+
+// All device arrays of a batch (pointers into HBM).
+struct DevArrays {
+  double *rx, *ry, *rz, *vx, *vy, *vz, *fx, *fy, *fz, *pe;
+  uint64_t* id;
+  uint32_t* pcell;                 // global cell of each particle
+  uint32_t *bkx, *bky, *bkz;       // backup_r u32 encoding (backup_r.h:36-51)
+  double *rbx, *rby, *rbz;         // the same backup restored once per rebuild (restore_u32_double)
+  // rebin scratch
+  double *t_rx, *t_ry, *t_rz, *t_vx, *t_vy, *t_vz, *t_fx, *t_fy, *t_fz;
+  uint64_t* t_id;
+  uint32_t* pdest;                 // destination cell (rebin) / scratch
+  uint32_t* plocal;                // new in-cell slot of staying particles
+  uint32_t* mover_list;            // per source cell, its movers (global index), in the cell's own range
+  // cells
+  uint32_t* cell_start;            // first particle of each cell (global index)
+  uint32_t* cell_n;                // particles in each cell
+  uint32_t* cell_sys;              // system of each cell
+  unsigned long long* cell_scan;   // per-cell exclusive scan scratch (ncells + 1)
+  uint32_t* cell_cnt;              // per-cell scratch counts
+  uint32_t* cell_stay;             // staying particles per cell
+  uint32_t* cell_nmov;             // movers leaving each cell
+  unsigned long long* cell_nbr_off;// per-cell neighbour-entry offset (scan scratch)
+  uint32_t* cell_nbr_tot;          // per-cell neighbour-entry totals
+  // neighbour lists
+  uint32_t* nbr_start;             // per particle, relative to its system segment
+  uint32_t* nbr_cnt;               // per particle
+  uint32_t* nbr_cursor;            // per particle fill cursor (scratch)
+  uint32_t* nbr;                   // all segments
+  // scan scratch
+  unsigned long long* scan_blocks;
+};
+
+// ----------------------------------------------------------------------------
+// Exact FP64 helpers: the reference's arithmetic written with explicit rounding
+// so the compiler cannot contract to FMA.
+__device__ __forceinline__ double norm2_rn(double x, double y, double z) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+}
+
+// restore_u32_double (core/include/exanb/core/backup_r.h:31-34)
+__device__ __forceinline__ double restore_u32(uint32_t x, double o, double r) {
+  return __dadd_rn(o, __dmul_rn(__dmul_rn(static_cast<double>(x), r), 0x1p-32));
+}
+
+// encode_double_u32 (core/include/exanb/core/backup_r.h:36-51)
+__device__ __forceinline__ uint32_t encode_u32(double x, double o, double r) {
+  const double xo = __dsub_rn(x, o);
+  long long a = __double2ll_rz(__ddiv_rn(__dmul_rn(xo, 4294967296.0), r));
+  a = a < 0 ? 0 : a;
+  a = a > 4294967295LL ? 4294967295LL : a;
+  const uint32_t xa = static_cast<uint32_t>(a);
+  const uint32_t xb = xa - 1u;
+  const uint32_t xc = xa + 1u;
+  const double ea = fabs(__dsub_rn(restore_u32(xa, o, r), x));
+  const double eb = fabs(__dsub_rn(restore_u32(xb, o, r), x));
+  const double ec = fabs(__dsub_rn(restore_u32(xc, o, r), x));
+  if (eb < ea) return xb;
+  if (ec < ea) return xc;
+  return xa;
+}
+
+// Grid::cell_position for a domain cell index (core/include/exanb/core/grid.h:114-117)
+__device__ __forceinline__ double cell_lo(const SysDesc& s, int axis, int dloc) {
+  return __dadd_rn(s.origin[axis], __dmul_rn(static_cast<double>(dloc), s.cell_size));
+}
+
+__device__ __forceinline__ void cell_ijk(const SysDesc& s, uint32_t local_cell, int& i, int& j, int& k) {
+  i = static_cast<int>(local_cell % static_cast<uint32_t>(s.dims[0]));
+  const uint32_t r = local_cell / static_cast<uint32_t>(s.dims[0]);
+  j = static_cast<int>(r % static_cast<uint32_t>(s.dims[1]));
+  k = static_cast<int>(r / static_cast<uint32_t>(s.dims[1]));
+}
+
+__device__ __forceinline__ int pmod_i(int i, int n) { return ((i % n) + n) % n; }
+
+// Image offset along one axis for image code digit d in {0,1,2} (-1, 0, +1).
+__device__ __forceinline__ double image_coord(double x, double period, int d) {
+  // apply_coord_modifier: x + (SIDE ? 1.0 : -1.0) * (rmax - rmin) when shifted, x otherwise
+  return d == 1 ? x : __dadd_rn(x, __dmul_rn(d == 2 ? 1.0 : -1.0, period));
+}
+
+}  // namespace xnb

@@ -1,0 +1,49 @@
+// Host-side launchers of the xnb kernels (internal; the public C ABI is include/xnb_gpu.h).
+#pragma once
+#include "xnb_internal.cuh"
+
+namespace xnb {
+
+enum Precision : int { kFp64Exact = 0, kFp64 = 1, kMixed = 2 };
+
+// Every launcher returns the number of kernels it enqueued.
+
+// Work extent of a batch: high-water marks of the particle and cell pools.
+struct Extent {
+  uint32_t n_part;   // particles [0, n_part) are scanned; free slots have pcell == ~0u
+  uint32_t n_cells;  // cells [0, n_cells); free cells have cell_sys == ~0u
+  int nsys;
+  int sm_count;
+};
+
+// Fused first half of velocity Verlet plus the displacement trigger:
+// push_f_v_r(dt_scale 1) ; push_f_v(dt_scale 0.5) ; particle_displ_over.
+int launch_first_half(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a,
+                       bool do_push_r, bool do_push_v, bool do_trigger, double dt_scale_r,
+                       double dt_scale_v, bool exact, int sys_only, cudaStream_t stream);
+
+// zero_particle_force + lennard_jones_force (+ divide_force_by_type_scalar when the
+// system asks for it), optionally fused with the second-half kick push_f_v(0.5).
+int launch_force(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int precision,
+                  bool with_pe, bool second_half, int sys_only, cudaStream_t stream);
+
+// Marks systems for rebuild: all of them (init), or those with moved > 0.
+int launch_mark_rebuild(const Extent& ex, SysState* st, int mode, int sys_only, cudaStream_t stream);
+int launch_clear_moved(const Extent& ex, SysState* st, cudaStream_t stream);
+
+// move_particles + migrate + rebuild_amr + backup_r for systems with rebuild != 0.
+int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream);
+// backup_r alone.
+int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream);
+// chunk_neighbors for systems with rebuild != 0. mode bit 1: count pass, scan
+// and segment check; bit 2: fill pass.
+int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int stage_cap,
+                      cudaStream_t stream, int mode);
+
+// Exclusive scan of u32 counts into u64 offsets (n elements; out has n+1 entries).
+int launch_scan_u32_to_u64(const uint32_t* in, unsigned long long* out, uint32_t n,
+                            unsigned long long* block_scratch, cudaStream_t stream);
+size_t scan_scratch_elems(uint32_t n);
+
+
+}  // namespace xnb

@@ -1,0 +1,321 @@
+// Per-step kernels: velocity-Verlet pushes with the displacement trigger, and the
+// Lennard-Jones pair-force traversal over the neighbour lists.
+#include "xnb_launch.cuh"
+
+namespace xnb {
+
+namespace {
+
+constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+
+// ---------------------------------------------------------------------------
+// push_f_v_r + push_f_v + particle_displ_over, one pass over the particles.
+//   push_f_v_r : PushVec3SecondOrderFunctor (defbox/include/exanb/defbox/push_vec3_2nd_order.h:33-38)
+//                x += v*dt + f*dt2, dt = dt*scale, dt2 = dt*dt*0.5 (:87-88)
+//   push_f_v   : PushVec3FirstOrderFunctor (push_vec3_1st_order.h:32-37), v += f*dt*scale
+//   trigger    : ReduceMaxDisplacementFunctor (mpi/particle_displ_over.cu:49-66),
+//                norm2(r - restore(backup)) >= max_displ^2, counted per system.
+// EXACT=true keeps the reference's two roundings per product/sum (bit-identical
+// trajectory); EXACT=false lets the compiler fuse them into FMAs.
+template <bool EXACT>
+__global__ void __launch_bounds__(256)
+    k_first_half(uint32_t n_part, const SysDesc* __restrict__ sys, SysState* __restrict__ st, DevArrays a,
+                 bool push_r, bool push_v, bool trigger, double scale_r, double scale_v, int sys_only) {
+  const bool canonical = (scale_r == 1.0 && scale_v == 0.5);
+  // every lane of a warp runs the same number of iterations, so full-warp
+  // collectives below see all 32 lanes
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n_part; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t c = i < n_part ? a.pcell[i] : kInvalid;
+    bool over = false;
+    uint32_t s = kInvalid;
+    if (c != kInvalid && (sys_only < 0 || a.cell_sys[c] == static_cast<uint32_t>(sys_only))) {
+      s = a.cell_sys[c];
+      const SysDesc& S = sys[s];
+      double dt, dt2, dtv;
+      if (canonical) {
+        dt = S.dt_full;
+        dt2 = S.dt_sq_half;
+        dtv = S.dt_half;
+      } else {
+        dt = __dmul_rn(S.dt, scale_r);
+        dt2 = __dmul_rn(__dmul_rn(dt, dt), 0.5);
+        dtv = __dmul_rn(S.dt, scale_v);
+      }
+      double x = a.rx[i], y = a.ry[i], z = a.rz[i];
+      double vx = a.vx[i], vy = a.vy[i], vz = a.vz[i];
+      const double fx = a.fx[i], fy = a.fy[i], fz = a.fz[i];
+      if (push_r) {
+        if (EXACT) {
+          x = __dadd_rn(x, __dadd_rn(__dmul_rn(vx, dt), __dmul_rn(fx, dt2)));
+          y = __dadd_rn(y, __dadd_rn(__dmul_rn(vy, dt), __dmul_rn(fy, dt2)));
+          z = __dadd_rn(z, __dadd_rn(__dmul_rn(vz, dt), __dmul_rn(fz, dt2)));
+        } else {
+          x += fma(vx, dt, fx * dt2);
+          y += fma(vy, dt, fy * dt2);
+          z += fma(vz, dt, fz * dt2);
+        }
+        a.rx[i] = x;
+        a.ry[i] = y;
+        a.rz[i] = z;
+      }
+      if (push_v) {
+        if (EXACT) {
+          vx = __dadd_rn(vx, __dmul_rn(fx, dtv));
+          vy = __dadd_rn(vy, __dmul_rn(fy, dtv));
+          vz = __dadd_rn(vz, __dmul_rn(fz, dtv));
+        } else {
+          vx = fma(fx, dtv, vx);
+          vy = fma(fy, dtv, vy);
+          vz = fma(fz, dtv, vz);
+        }
+        a.vx[i] = vx;
+        a.vy[i] = vy;
+        a.vz[i] = vz;
+      }
+      if (trigger && st[s].rebuild_armed) {
+        const double dx = __dsub_rn(x, a.rbx[i]);
+        const double dy = __dsub_rn(y, a.rby[i]);
+        const double dz = __dsub_rn(z, a.rbz[i]);
+        const double d2 = EXACT ? norm2_rn(dx, dy, dz) : fma(dz, dz, fma(dy, dy, dx * dx));
+        over = d2 >= S.max_displ2;
+      }
+    }
+    if (trigger) {
+      // warp-aggregated count per system
+      const unsigned same = __match_any_sync(0xffffffffu, s);
+      const unsigned hits = __ballot_sync(0xffffffffu, over) & same;
+      const int leader = __ffs(same) - 1;
+      if (s != kInvalid && static_cast<int>(threadIdx.x & 31) == leader && hits)
+        atomicAdd(&st[s].moved, static_cast<unsigned long long>(__popc(hits)));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fast double-precision reciprocal: FP32 seed refined by two Newton-Raphson
+// steps y <- y + y*(1 - d*y) in FP64 (relative error ~1e-16, not correctly rounded).
+__device__ __forceinline__ double rcp_nr(double d) {
+  double y = static_cast<double>(__frcp_rn(static_cast<float>(d)));
+  double e = fma(-d, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-d, y, 1.0);
+  return fma(y, e, y);
+}
+
+// ---------------------------------------------------------------------------
+// zero_particle_force + lennard_jones_force over the neighbour lists.
+// compute_cell_particle_pairs_cell (compute/include/exanb/compute/
+// compute_cell_particle_pairs_impl_default.h:148-238) walks each particle's
+// stream in (cell_enc, p_b) order with dr = r_b - r_a and keeps 0 < d2 <= rc^2;
+// LennardJonesForceFunctor (contribs/md/lennard_jones/lennard_jones.cu:67-102)
+// sums pair_de*dr sequentially and adds the sum onto the zeroed force.
+// One thread per particle, full lists: no atomics, fixed summation order.
+//   P = kFp64Exact : the functor's own operations and roundings (sqrt, 1/r,
+//                    no contraction): bit-identical to the CPU restatement.
+//   P = kFp64      : same selection of pairs (exact d2 test), force from
+//                    1/d2 by Newton-Raphson, FMA accumulation.
+//   P = kMixed     : FP64 displacement and FP64 accumulation; r^2, r^-6 and the
+//                    force magnitude in FP32; the cutoff decision is made in FP32
+//                    where a proven margin allows and in FP64 otherwise, so the
+//                    pair set is the FP64 one.
+template <int P, bool PE, bool KICK>
+__global__ void __launch_bounds__(256)
+    k_force(uint32_t n_part, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a,
+            int sys_only) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
+    const uint32_t c = a.pcell[i];
+    if (c == kInvalid) continue;
+    const uint32_t s = a.cell_sys[c];
+    if (sys_only >= 0 && s != static_cast<uint32_t>(sys_only)) continue;
+    if (st[s].error) continue;  // lists of a failed system are not trusted
+    const SysDesc& S = sys[s];
+    const double xa = a.rx[i], ya = a.ry[i], za = a.rz[i];
+    const uint32_t* __restrict__ L = a.nbr + S.list_base + a.nbr_start[i];
+    const uint32_t n = a.nbr_cnt[i];
+    const uint32_t pbase = S.part_base;
+    const double px = S.period[0], py = S.period[1], pz = S.period[2];
+    const double rcut2 = S.rcut2;
+    double fx = 0.0, fy = 0.0, fz = 0.0, pe = 0.0;
+    for (uint32_t k = 0; k < n; ++k) {
+      const uint32_t e = __ldg(L + k);
+      const uint32_t j = pbase + (e >> 5);
+      const uint32_t code = e & 31u;
+      double xb = __ldg(a.rx + j), yb = __ldg(a.ry + j), zb = __ldg(a.rz + j);
+      if (code != static_cast<uint32_t>(kImageCenter)) {
+        xb = image_coord(xb, px, static_cast<int>(code % 3u));
+        yb = image_coord(yb, py, static_cast<int>((code / 3u) % 3u));
+        zb = image_coord(zb, pz, static_cast<int>(code / 9u));
+      }
+      const double dx = __dsub_rn(xb, xa);
+      const double dy = __dsub_rn(yb, ya);
+      const double dz = __dsub_rn(zb, za);
+      if (P == kFp64Exact) {
+        const double d2 = norm2_rn(dx, dy, dz);
+        if (d2 > 0.0 && d2 <= rcut2) {
+          // lj_compute_energy (lennard_jones.cu:46-56) then pair_de *= w / r with w = 1
+          const double r = __dsqrt_rn(d2);
+          const double inv_r = __ddiv_rn(1.0, r);
+          const double ratio = __dmul_rn(S.sigma, inv_r);
+          const double ratio2 = __dmul_rn(ratio, ratio);
+          const double ratio6 = __dmul_rn(__dmul_rn(ratio2, ratio2), ratio2);
+          const double ratio12 = __dmul_rn(ratio6, ratio6);
+          double de = __dmul_rn(__dmul_rn(S.m24eps, __dsub_rn(__dmul_rn(2.0, ratio12), ratio6)), inv_r);
+          de = __dmul_rn(de, inv_r);
+          fx = __dadd_rn(fx, __dmul_rn(de, dx));
+          fy = __dadd_rn(fy, __dmul_rn(de, dy));
+          fz = __dadd_rn(fz, __dmul_rn(de, dz));
+          if (PE) {
+            const double en = __dmul_rn(S.eps4, __dsub_rn(ratio12, ratio6));
+            pe = __dadd_rn(pe, __dmul_rn(0.5, __dsub_rn(en, S.e_shift)));
+          }
+        }
+      } else if (P == kFp64) {
+        const double d2 = norm2_rn(dx, dy, dz);
+        if (d2 > 0.0 && d2 <= rcut2) {
+          const double ir2 = rcp_nr(d2);
+          const double s2 = S.sig2 * ir2;
+          const double s6 = s2 * s2 * s2;
+          const double pd = S.eps24 * s6 * fma(-2.0, s6, 1.0) * ir2;
+          fx = fma(pd, dx, fx);
+          fy = fma(pd, dy, fy);
+          fz = fma(pd, dz, fz);
+          if (PE) pe += 0.5 * fma(S.eps4 * s6, s6 - 1.0, -S.e_shift);
+        }
+      } else {
+        const float dxf = static_cast<float>(dx), dyf = static_cast<float>(dy), dzf = static_cast<float>(dz);
+        const float r2 = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
+        bool in;
+        if (r2 > S.rc2_f + S.rc_margin_f) {
+          in = false;
+        } else if (r2 < S.rc2_f - S.rc_margin_f && r2 > S.rc_margin_f) {
+          in = true;
+        } else {
+          const double d2 = norm2_rn(dx, dy, dz);
+          in = (d2 > 0.0 && d2 <= rcut2);
+        }
+        if (in) {
+          const float ir2 = __frcp_rn(r2);
+          const float s2 = S.sig2_f * ir2;
+          const float s6 = s2 * s2 * s2;
+          const float pd = S.eps24_f * s6 * fmaf(-2.0f, s6, 1.0f) * ir2;
+          const double pdd = static_cast<double>(pd);
+          fx = fma(pdd, dx, fx);
+          fy = fma(pdd, dy, fy);
+          fz = fma(pdd, dz, fz);
+          if (PE) pe += static_cast<double>(0.5f * fmaf(S.eps4_f * s6, s6 - 1.0f, -S.e_shift_f));
+        }
+      }
+    }
+    // the force field was zeroed (zero_particle_force.cu:39-46) and receives the sum
+    fx = __dadd_rn(0.0, fx);
+    fy = __dadd_rn(0.0, fy);
+    fz = __dadd_rn(0.0, fz);
+    if (S.divide_by_mass) {
+      // divide_force_by_type_scalar (compute/vec3_typescalar_op.cu:156, math_functors.h:140)
+      fx = __ddiv_rn(fx, S.mass);
+      fy = __ddiv_rn(fy, S.mass);
+      fz = __ddiv_rn(fz, S.mass);
+    }
+    a.fx[i] = fx;
+    a.fy[i] = fy;
+    a.fz[i] = fz;
+    if (PE) a.pe[i] = pe;
+    if (KICK) {
+      // verlet_second_half: push_f_v with dt_scale 0.5 (numerical-scheme.msp:17-18)
+      const double h = S.dt_half;
+      if (P == kFp64Exact) {
+        a.vx[i] = __dadd_rn(a.vx[i], __dmul_rn(fx, h));
+        a.vy[i] = __dadd_rn(a.vy[i], __dmul_rn(fy, h));
+        a.vz[i] = __dadd_rn(a.vz[i], __dmul_rn(fz, h));
+      } else {
+        a.vx[i] = fma(fx, h, a.vx[i]);
+        a.vy[i] = fma(fy, h, a.vy[i]);
+        a.vz[i] = fma(fz, h, a.vz[i]);
+      }
+    }
+  }
+}
+
+__global__ void k_mark_rebuild(int nsys, SysState* st, int mode, int sys_only) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  if (sys_only >= 0 && s != sys_only) {
+    st[s].rebuild = 0;
+    return;
+  }
+  // mode 0: every system (init); mode 1: systems whose trigger fired; mode 2: none
+  const uint32_t r = mode == 0 ? 1u : (mode == 1 ? (st[s].moved > 0 ? 1u : 0u) : 0u);
+  st[s].rebuild = r;
+  if (r) st[s].rebuilds += 1;
+}
+
+__global__ void k_clear_moved(int nsys, SysState* st) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nsys) st[s].moved = 0;
+}
+
+inline int grid_for(uint32_t n, int threads, int sm_count, int per_sm) {
+  const long long want = (static_cast<long long>(n) + threads - 1) / threads;
+  const long long cap = static_cast<long long>(sm_count) * per_sm;
+  long long g = want < cap ? want : cap;
+  return static_cast<int>(g < 1 ? 1 : g);
+}
+
+template <int P, bool PE, bool KICK>
+void force_dispatch(const Extent& ex, const SysDesc* sys, const SysState* st, const DevArrays& a, int sys_only,
+                    cudaStream_t stream) {
+  const int threads = 256;
+  k_force<P, PE, KICK><<<grid_for(ex.n_part, threads, ex.sm_count, 8), threads, 0, stream>>>(ex.n_part, sys, st, a,
+                                                                                           sys_only);
+}
+
+}  // namespace
+
+int launch_first_half(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, bool do_push_r,
+                       bool do_push_v, bool do_trigger, double dt_scale_r, double dt_scale_v, bool exact,
+                       int sys_only, cudaStream_t stream) {
+  if (ex.n_part == 0) return 0;
+  const int threads = 256;
+  const int g = grid_for(ex.n_part, threads, ex.sm_count, 8);
+  if (exact)
+    k_first_half<true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, do_push_r, do_push_v, do_trigger,
+                                                  dt_scale_r, dt_scale_v, sys_only);
+  else
+    k_first_half<false><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, do_push_r, do_push_v, do_trigger,
+                                                   dt_scale_r, dt_scale_v, sys_only);
+  return 1;
+}
+
+int launch_force(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int precision, bool with_pe,
+                  bool second_half, int sys_only, cudaStream_t stream) {
+  if (ex.n_part == 0) return 0;
+#define XNB_FORCE_CASE(PP)                                                           \
+  if (precision == PP) {                                                             \
+    if (with_pe && second_half) force_dispatch<PP, true, true>(ex, sys, st, a, sys_only, stream);   \
+    else if (with_pe) force_dispatch<PP, true, false>(ex, sys, st, a, sys_only, stream);            \
+    else if (second_half) force_dispatch<PP, false, true>(ex, sys, st, a, sys_only, stream);        \
+    else force_dispatch<PP, false, false>(ex, sys, st, a, sys_only, stream);                        \
+    return 1;                                                                        \
+  }
+  XNB_FORCE_CASE(kFp64Exact)
+  XNB_FORCE_CASE(kFp64)
+  XNB_FORCE_CASE(kMixed)
+#undef XNB_FORCE_CASE
+  return 0;
+}
+
+int launch_mark_rebuild(const Extent& ex, SysState* st, int mode, int sys_only, cudaStream_t stream) {
+  if (ex.nsys == 0) return 0;
+  k_mark_rebuild<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, mode, sys_only);
+  return 1;
+}
+
+int launch_clear_moved(const Extent& ex, SysState* st, cudaStream_t stream) {
+  if (ex.nsys == 0) return 0;
+  k_clear_moved<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st);
+  return 1;
+}
+
+}  // namespace xnb

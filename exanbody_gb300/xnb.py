@@ -1,0 +1,300 @@
+"""ctypes binding of libxnb_gpu.so (include/xnb_gpu.h).
+
+This is the Python face of the C ABI: no computation happens here. Every call
+goes to the sm_103a library; if the library or a GPU is missing the calls fail
+loudly (there is no CPU fallback).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+PREC_FP64_EXACT = 0
+PREC_FP64 = 1
+PREC_MIXED = 2
+PRECISIONS = {"fp64_exact": PREC_FP64_EXACT, "fp64": PREC_FP64, "mixed": PREC_MIXED}
+
+STEP_HOST_SYNC = 1
+STEP_ENERGY = 2
+
+ERRBIT_LIST_OVERFLOW = 1
+ERRBIT_FAR_MOVER = 2
+ERRBIT_CELL_INDEX = 4
+
+EXPORTED = [
+    "xnb_last_error_string", "xnb_version", "xnb_batch_create", "xnb_batch_destroy", "xnb_system_bytes",
+    "xnb_system_add", "xnb_system_remove", "xnb_system_info_get", "xnb_system_download", "xnb_system_pairs",
+    "xnb_system_energy", "xnb_init_particles", "xnb_push_f_v_r", "xnb_push_f_v", "xnb_particle_displ_over",
+    "xnb_update_particles_full", "xnb_chunk_neighbors", "xnb_backup_r", "xnb_lennard_jones_force",
+    "xnb_ghost_update_r", "xnb_step", "xnb_step_graph_create", "xnb_graph_launch", "xnb_graph_destroy",
+    "xnb_check_errors", "xnb_stats_kernel_launches",
+]
+
+
+class LJParams(C.Structure):
+    _fields_ = [
+        ("origin", C.c_double * 3),
+        ("extent", C.c_double * 3),
+        ("dims", C.c_int32 * 3),
+        ("cell_size", C.c_double),
+        ("rcut", C.c_double),
+        ("rcut_inc", C.c_double),
+        ("epsilon", C.c_double),
+        ("sigma", C.c_double),
+        ("dt", C.c_double),
+        ("mass", C.c_double),
+        ("divide_by_mass", C.c_int32),
+        ("amr_enabled", C.c_int32),
+        ("sub_grid_density", C.c_double),
+    ]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32),
+        ("max_systems", C.c_int32),
+        ("particle_capacity", C.c_int64),
+        ("cell_capacity", C.c_int64),
+        ("list_capacity", C.c_int64),
+        ("stage_cap", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class SystemInfo(C.Structure):
+    _fields_ = [
+        ("n_particles", C.c_int64),
+        ("n_cells", C.c_int64),
+        ("list_used", C.c_int64),
+        ("list_cap", C.c_int64),
+        ("rebuilds", C.c_int64),
+        ("error_bits", C.c_uint32),
+        ("max_cell", C.c_uint32),
+        ("active", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class XnbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("xnb error %d: %s" % (code, msg))
+        self.code = code
+
+
+_LIB = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libxnb_gpu.so (building it when missing) and declare the ABI."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise OSError("libxnb_gpu.so not built: run exanbody_gb300/build.py")
+        _build.build()
+    lib = C.CDLL(path)
+    P = C.POINTER
+    d, i32, i64, u64, vp = C.c_double, C.c_int32, C.c_int64, C.c_uint64, C.c_void_p
+    lib.xnb_last_error_string.restype = C.c_char_p
+    lib.xnb_batch_create.argtypes = [P(BatchConfig), P(vp)]
+    lib.xnb_batch_destroy.argtypes = [vp]
+    lib.xnb_system_bytes.restype = i64
+    lib.xnb_system_bytes.argtypes = [i64, i64, d]
+    lib.xnb_system_add.argtypes = [vp, P(LJParams), i64] + [P(d)] * 6 + [P(u64), P(i64), d, vp, P(i32)]
+    lib.xnb_system_remove.argtypes = [vp, i32, vp]
+    lib.xnb_system_info_get.argtypes = [vp, i32, P(SystemInfo), vp]
+    lib.xnb_system_download.argtypes = [vp, i32] + [P(d)] * 9 + [P(u64), P(i32), P(d), vp]
+    lib.xnb_system_pairs.argtypes = [vp, i32, P(u64), P(u64), P(i32), i64, P(i64), vp]
+    lib.xnb_system_energy.argtypes = [vp, i32, P(d), P(d), vp]
+    lib.xnb_init_particles.argtypes = [vp, i32, i32, vp]
+    lib.xnb_push_f_v_r.argtypes = [vp, i32, d, vp]
+    lib.xnb_push_f_v.argtypes = [vp, i32, d, vp]
+    lib.xnb_particle_displ_over.argtypes = [vp, i32, P(i64), vp]
+    lib.xnb_update_particles_full.argtypes = [vp, i32, vp]
+    lib.xnb_chunk_neighbors.argtypes = [vp, i32, vp]
+    lib.xnb_backup_r.argtypes = [vp, i32, vp]
+    lib.xnb_lennard_jones_force.argtypes = [vp, i32, i32, i32, vp]
+    lib.xnb_ghost_update_r.argtypes = [vp, i32, vp]
+    lib.xnb_step.argtypes = [vp, i32, i32, i32, vp]
+    lib.xnb_step_graph_create.argtypes = [vp, i32, i32, i32, vp, P(vp)]
+    lib.xnb_graph_launch.argtypes = [vp, vp]
+    lib.xnb_graph_destroy.argtypes = [vp]
+    lib.xnb_check_errors.argtypes = [vp, vp]
+    lib.xnb_stats_kernel_launches.restype = i64
+    lib.xnb_stats_kernel_launches.argtypes = [vp]
+    _LIB = lib
+    return lib
+
+
+def _ck(rc):
+    if rc != 0:
+        raise XnbError(rc, _LIB.xnb_last_error_string().decode())
+    return rc
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def lj_params(geom, epsilon=1.0, sigma=1.0, rcut=2.5, rcut_inc=0.3, dt=0.005, mass=1.0, divide_by_mass=False,
+              amr=True, sub_grid_density=6.5):
+    """LJParams from a geometry dict (origin, extent, dims, cell_size)."""
+    p = LJParams()
+    for a in range(3):
+        p.origin[a] = geom["origin"][a]
+        p.extent[a] = geom["extent"][a]
+        p.dims[a] = int(geom["dims"][a])
+    p.cell_size = geom["cell_size"]
+    p.rcut, p.rcut_inc = rcut, rcut_inc
+    p.epsilon, p.sigma, p.dt = epsilon, sigma, dt
+    p.mass, p.divide_by_mass = mass, int(bool(divide_by_mass))
+    p.amr_enabled, p.sub_grid_density = int(bool(amr)), sub_grid_density
+    return p
+
+
+class Batch:
+    """Device pools holding any number of resident systems (xnb_batch)."""
+
+    def __init__(self, particle_capacity, cell_capacity, list_capacity, max_systems=1, device=0, stage_cap=0,
+                 stream=None):
+        self.lib = load()
+        cfg = BatchConfig(int(device), int(max_systems), int(particle_capacity), int(cell_capacity),
+                          int(list_capacity), int(stage_cap), 0)
+        h = C.c_void_p()
+        _ck(self.lib.xnb_batch_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self.stream = C.c_void_p(stream) if stream else None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.xnb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- systems ----
+    def add_system(self, params, r, v, ids, cell_counts=None, list_factor=1.3):
+        r = np.ascontiguousarray(r, np.float64)
+        v = np.ascontiguousarray(v, np.float64)
+        ids = np.ascontiguousarray(ids, np.uint64)
+        cols = [np.ascontiguousarray(r[:, a]) for a in range(3)] + [np.ascontiguousarray(v[:, a]) for a in range(3)]
+        cc = None
+        if cell_counts is not None:
+            cell_counts = np.ascontiguousarray(cell_counts, np.int64)
+            cc = cell_counts.ctypes.data_as(C.POINTER(C.c_int64))
+        sid = C.c_int32()
+        _ck(self.lib.xnb_system_add(self.h, C.byref(params), len(ids), *[_dp(c) for c in cols],
+                                    ids.ctypes.data_as(C.POINTER(C.c_uint64)), cc, float(list_factor),
+                                    self.stream, C.byref(sid)))
+        return sid.value
+
+    def remove_system(self, s):
+        _ck(self.lib.xnb_system_remove(self.h, s, self.stream))
+
+    def info(self, s):
+        inf = SystemInfo()
+        _ck(self.lib.xnb_system_info_get(self.h, s, C.byref(inf), self.stream))
+        return inf
+
+    def download(self, s):
+        n = self.info(s).n_particles
+        out = {k: np.empty(n, np.float64) for k in ("rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz", "pe")}
+        ids = np.empty(n, np.uint64)
+        cell = np.empty(n, np.int32)
+        _ck(self.lib.xnb_system_download(self.h, s, *[_dp(out[k]) for k in ("rx", "ry", "rz", "vx", "vy", "vz",
+                                                                            "fx", "fy", "fz")],
+                                         ids.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                         cell.ctypes.data_as(C.POINTER(C.c_int32)), _dp(out["pe"]), self.stream))
+        out["id"] = ids
+        out["cell"] = cell
+        return out
+
+    def pairs(self, s):
+        inf = self.info(s)
+        m = inf.list_used
+        a = np.empty(m, np.uint64)
+        b = np.empty(m, np.uint64)
+        cnt = np.empty(inf.n_particles, np.int32)
+        nout = C.c_int64()
+        _ck(self.lib.xnb_system_pairs(self.h, s, a.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                      b.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                      cnt.ctypes.data_as(C.POINTER(C.c_int32)), m, C.byref(nout), self.stream))
+        return a[: nout.value], b[: nout.value], cnt
+
+    def energy(self, s):
+        ke, pe = C.c_double(), C.c_double()
+        _ck(self.lib.xnb_system_energy(self.h, s, C.byref(ke), C.byref(pe), self.stream))
+        return ke.value, pe.value
+
+    # ---- operators ----
+    def init_particles(self, s=-1, precision=PREC_FP64_EXACT):
+        _ck(self.lib.xnb_init_particles(self.h, s, precision, self.stream))
+
+    def push_f_v_r(self, dt_scale=1.0, s=-1):
+        _ck(self.lib.xnb_push_f_v_r(self.h, s, dt_scale, self.stream))
+
+    def push_f_v(self, dt_scale=0.5, s=-1):
+        _ck(self.lib.xnb_push_f_v(self.h, s, dt_scale, self.stream))
+
+    def particle_displ_over(self, s):
+        out = np.zeros(max(1, 1 if s >= 0 else 4096), np.int64)
+        _ck(self.lib.xnb_particle_displ_over(self.h, s, out.ctypes.data_as(C.POINTER(C.c_int64)), self.stream))
+        return int(out[0]) if s >= 0 else out
+
+    def update_particles_full(self, s=-1):
+        _ck(self.lib.xnb_update_particles_full(self.h, s, self.stream))
+
+    def chunk_neighbors(self, s=-1):
+        _ck(self.lib.xnb_chunk_neighbors(self.h, s, self.stream))
+
+    def backup_r(self, s=-1):
+        _ck(self.lib.xnb_backup_r(self.h, s, self.stream))
+
+    def lennard_jones_force(self, s=-1, precision=PREC_FP64_EXACT, energy=True):
+        _ck(self.lib.xnb_lennard_jones_force(self.h, s, precision, int(bool(energy)), self.stream))
+
+    def step(self, nsteps=1, precision=PREC_FP64_EXACT, flags=STEP_HOST_SYNC):
+        _ck(self.lib.xnb_step(self.h, int(nsteps), int(precision), int(flags), self.stream))
+
+    def graph(self, nsteps, precision=PREC_MIXED, flags=0):
+        g = C.c_void_p()
+        _ck(self.lib.xnb_step_graph_create(self.h, int(nsteps), int(precision), int(flags), self.stream,
+                                           C.byref(g)))
+        return Graph(self, g)
+
+    def check_errors(self):
+        _ck(self.lib.xnb_check_errors(self.h, self.stream))
+
+    def kernel_launches(self):
+        return int(self.lib.xnb_stats_kernel_launches(self.h))
+
+
+class Graph:
+    def __init__(self, batch, g):
+        self.batch, self.g = batch, g
+
+    def launch(self):
+        _ck(self.batch.lib.xnb_graph_launch(self.g, self.batch.stream))
+
+    def close(self):
+        if self.g:
+            self.batch.lib.xnb_graph_destroy(self.g)
+            self.g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

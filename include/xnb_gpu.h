@@ -1,0 +1,179 @@
+/*
+ * xnb_gpu.h -- C ABI of the GB300 (sm_103a) particle hot path.
+ *
+ * The library advances periodic Lennard-Jones systems with the reference's
+ * per-step operator sequence (exaNBody data/config/numerical-scheme.msp:13-25):
+ *   push_f_v_r ; push_f_v ; particle_displ_over ;
+ *   [ move_particles ; rebuild_amr ; backup_r ; ghost_comm_scheme ;
+ *     ghost_update_all ; chunk_neighbors ]  or  ghost_update_r ;
+ *   zero_particle_force ; lennard_jones_force ; push_f_v
+ * One "batch" holds any number of independent systems resident in HBM; every
+ * entry point below that takes `sys` accepts -1 for "all systems of the batch".
+ *
+ * Conventions: all functions return 0 (XNB_OK) or a negative XNB_ERR_* code
+ * and never throw; xnb_last_error_string() describes the last failure of the
+ * calling thread. Host arrays are plain C arrays; `stream` is a cudaStream_t
+ * (NULL = legacy default stream). The reference reports errors with
+ * fatal_error()/abort (e.g. move_particles_across_cells.h:68-75); this ABI
+ * returns codes instead so that a host runtime can recover per system.
+ *
+ * The reference has no C ABI: each entry point names the OperatorNode it
+ * replaces (file:line inside the exaNBody tree).
+ */
+#ifndef XNB_GPU_H
+#define XNB_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XNB_OK 0
+#define XNB_ERR_ARG (-1)      /* invalid argument or unsupported geometry */
+#define XNB_ERR_CUDA (-2)     /* a CUDA runtime call failed */
+#define XNB_ERR_NOMEM (-3)    /* pool or device memory exhausted */
+#define XNB_ERR_CAPACITY (-4) /* neighbour list segment overflow (see xnb_system_info.error_bits) */
+#define XNB_ERR_DEVICE (-5)   /* a kernel reported an error bit for a system */
+
+/* Precision of the force traversal. */
+#define XNB_PREC_FP64_EXACT 0 /* the reference functor's operations, bit-identical to its CPU path */
+#define XNB_PREC_FP64 1       /* FP64, same pair set, reciprocal by Newton-Raphson, FMA */
+#define XNB_PREC_MIXED 2      /* FP64 positions/displacements/accumulation/integration; FP32 r^2, r^-6, |F| */
+
+/* xnb_step flags */
+#define XNB_STEP_HOST_SYNC 1 /* read the trigger on the host and skip the rebuild launches when idle */
+#define XNB_STEP_ENERGY 2    /* also write per-particle potential energy */
+
+/* Error bits of xnb_system_info.error_bits */
+#define XNB_ERRBIT_LIST_OVERFLOW 1u
+#define XNB_ERRBIT_FAR_MOVER 2u
+#define XNB_ERRBIT_CELL_INDEX 4u
+
+typedef struct xnb_batch xnb_batch;
+typedef struct xnb_graph xnb_graph;
+
+/* One periodic LJ system: domain (Domain, core/include/exanb/core/domain.h:36-129),
+ * potential (LennardJonesParms, contribs/md/lennard_jones/lennard_jones.cu:40-44),
+ * neighbour distances (nbh_dist, particle_neighbors/nbh_dist.cpp:45-66) and the
+ * integrator step (global.dt). */
+typedef struct xnb_lj_params {
+  double origin[3];
+  double extent[3];
+  int32_t dims[3];        /* domain grid dims; >= 2 per axis */
+  double cell_size;       /* >= rcut + rcut_inc (one ghost layer) */
+  double rcut;            /* lennard_jones_force.rcut */
+  double rcut_inc;        /* Verlet skin: nbh_dist = rcut + rcut_inc, max_displ = rcut_inc / 2 */
+  double epsilon;
+  double sigma;
+  double dt;
+  double mass;            /* used when divide_by_mass != 0 */
+  int32_t divide_by_mass; /* force chain ends with divide_force_by_type_scalar: mass */
+  int32_t amr_enabled;    /* rebuild_amr in-cell ordering (amr/rebuild_amr.cpp:42-61) */
+  double sub_grid_density;
+} xnb_lj_params;
+
+typedef struct xnb_batch_config {
+  int32_t device;
+  int32_t max_systems;
+  int64_t particle_capacity; /* particles over all resident systems */
+  int64_t cell_capacity;     /* cells over all resident systems */
+  int64_t list_capacity;     /* neighbour entries over all resident systems */
+  int32_t stage_cap;         /* neighbour-build staging candidates per warp; 0 = default */
+  int32_t reserved;
+} xnb_batch_config;
+
+typedef struct xnb_system_info {
+  int64_t n_particles;
+  int64_t n_cells;
+  int64_t list_used;
+  int64_t list_cap;
+  int64_t rebuilds;   /* neighbour-list rebuilds since xnb_init_particles */
+  uint32_t error_bits;
+  uint32_t max_cell;  /* largest cell occupancy after the last rebin */
+  int32_t active;
+  int32_t reserved;
+} xnb_system_info;
+
+const char* xnb_last_error_string(void);
+int xnb_version(void);
+
+/* Device pools for one batch. */
+int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out);
+int xnb_batch_destroy(xnb_batch* b);
+/* Bytes of device memory a system of n particles and ncells cells needs, with
+ * list_per_particle neighbour entries per particle (admission control). */
+int64_t xnb_system_bytes(int64_t n, int64_t ncells, double list_per_particle);
+
+/* Upload one system. cell_counts == NULL: particles are placed in the cell of
+ * their periodic location, in input order (stable). Otherwise the arrays are
+ * given per interior cell (linear order (k*Dj+j)*Di+i) as the reference grid
+ * holds them, and positions may lie outside their cell (the reference's
+ * lattice generator then relies on init's move_particles). list_factor scales
+ * the neighbour segment reserved at init (>= 1; 0 = 1.3). */
+int xnb_system_add(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double* rx, const double* ry,
+                   const double* rz, const double* vx, const double* vy, const double* vz, const uint64_t* id,
+                   const int64_t* cell_counts, double list_factor, void* stream, int32_t* sys_out);
+int xnb_system_remove(xnb_batch* b, int32_t sys, void* stream);
+int xnb_system_info_get(xnb_batch* b, int32_t sys, xnb_system_info* info, void* stream);
+/* Particles in storage order (cells in linear order, then in-cell order).
+ * Any output pointer may be NULL. */
+int xnb_system_download(xnb_batch* b, int32_t sys, double* rx, double* ry, double* rz, double* vx, double* vy,
+                        double* vz, double* fx, double* fy, double* fz, uint64_t* id, int32_t* cell, double* pe,
+                        void* stream);
+/* Neighbour pairs as particle ids in list order; nbh_count gets one length per
+ * particle (storage order). cap is the size of id_a/id_b; n_out the pair count. */
+int xnb_system_pairs(xnb_batch* b, int32_t sys, uint64_t* id_a, uint64_t* id_b, int32_t* nbh_count, int64_t cap,
+                     int64_t* n_out, void* stream);
+/* Kinetic 0.5*m*v^2 and truncated-and-shifted LJ energy of the last force call
+ * made with energies. */
+int xnb_system_energy(xnb_batch* b, int32_t sys, double* ke, double* pe, void* stream);
+
+/* ---- reference operators (sys = -1: all systems) ---- */
+
+/* init_particles (data/config/update-particles.msp:31-36) then
+ * compute_all_forces_energy (numerical-scheme.msp:8-11). */
+int xnb_init_particles(xnb_batch* b, int32_t sys, int32_t precision, void* stream);
+/* push_f_v_r: PushVec3SecondOrderXForm (defbox/include/exanb/defbox/push_vec3_2nd_order.h:85-117). */
+int xnb_push_f_v_r(xnb_batch* b, int32_t sys, double dt_scale, void* stream);
+/* push_f_v: PushVec3FirstOrder (defbox/include/exanb/defbox/push_vec3_1st_order.h:79-106). */
+int xnb_push_f_v(xnb_batch* b, int32_t sys, double dt_scale, void* stream);
+/* particle_displ_over: ParticleDisplacementOver (mpi/particle_displ_over.cu:93-177).
+ * Synchronises the stream; count_out[sys or 0] = particles over the threshold. */
+int xnb_particle_displ_over(xnb_batch* b, int32_t sys, int64_t* count_out, void* stream);
+/* update_particles_full (update-particles.msp:62-68): move_particles
+ * (grid_cell_particles/move_particles.cpp:39-48), migrate_cell_particles,
+ * rebuild_amr, backup_r, ghost_comm_scheme, ghost_update_all, chunk_neighbors. */
+int xnb_update_particles_full(xnb_batch* b, int32_t sys, void* stream);
+/* chunk_neighbors: BuildChunkNeighbors (particle_neighbors/chunk_neighbors.cpp:47-72). */
+int xnb_chunk_neighbors(xnb_batch* b, int32_t sys, void* stream);
+/* backup_r: PositionBackupNode (io/backup_r.cpp:35-107). */
+int xnb_backup_r(xnb_batch* b, int32_t sys, void* stream);
+/* zero_particle_force (compute/zero_particle_force.cu:17-53) + lennard_jones_force
+ * (contribs/md/lennard_jones/lennard_jones.cu:171-213) [+ divide_force_by_type_scalar]. */
+int xnb_lennard_jones_force(xnb_batch* b, int32_t sys, int32_t precision, int32_t with_energy, void* stream);
+/* ghost_update_r (mpi/update_ghosts.cu:58): ghost images are evaluated on the
+ * fly from their owners, so there is nothing to copy; kept for the operator set. */
+int xnb_ghost_update_r(xnb_batch* b, int32_t sys, void* stream);
+
+/* ---- fused numerical scheme ---- */
+
+/* nsteps of numerical_scheme (numerical-scheme.msp:21-25) for every system of
+ * the batch, fused into three kernels per step plus the rebuild path. */
+int xnb_step(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, void* stream);
+/* Captures nsteps of the fused step (device-side trigger, no host sync) as a CUDA graph. */
+int xnb_step_graph_create(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, void* stream,
+                          xnb_graph** out);
+int xnb_graph_launch(xnb_graph* g, void* stream);
+int xnb_graph_destroy(xnb_graph* g);
+/* Any device error bit set on any system -> XNB_ERR_DEVICE / XNB_ERR_CAPACITY (synchronises). */
+int xnb_check_errors(xnb_batch* b, void* stream);
+/* Kernels this batch has enqueued so far (host-side count, for launch accounting;
+ * the reference's equivalent bookkeeping lives in onika's profiling layer). */
+int64_t xnb_stats_kernel_launches(const xnb_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XNB_GPU_H */

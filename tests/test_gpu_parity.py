@@ -1,0 +1,217 @@
+"""Parity of the sm_103a library (through its C ABI) with the CPU oracle.
+
+FP64_EXACT must be bit-identical to the oracle: neighbour pair lists (as
+particle ids, in the reference's stream order), positions, velocities and
+forces after every step. FP64 must agree within 1e-12 relative force error and
+MIXED within 1e-5 (|dF_i| / max(|F_i|, F_rms), max over particles).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from exanbody_gb300 import workloads, xnb
+from helpers import (assert_bitwise_equal, force_error, forces, ncells, new_batch, ni_deck_oracle,
+                     ni_deck_params, oracle_from)
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_TOL = 1e-5
+
+
+def gpu_system(w, batch=None, list_factor=1.3):
+    b = batch or new_batch([w["n_atoms"]], [ncells(w["geom"])])
+    s = b.add_system(xnb.lj_params(w["geom"]), w["r"], w["v"], w["id"], list_factor=list_factor)
+    return b, s
+
+
+def compare_pairs(b, s, o):
+    ga, gb, gc = b.pairs(s)
+    oa, ob, oc = o.pairs()
+    assert np.array_equal(gc, oc), "per-particle neighbour counts differ"
+    assert np.array_equal(ga, oa) and np.array_equal(gb, ob), "neighbour lists differ"
+    return len(ga)
+
+
+def test_init_bit_exact_config0():
+    w = workloads.lj_fcc_system(20, 0.8442, 1.44, 12345)  # 32,000 atoms
+    b, s = gpu_system(w)
+    b.init_particles(s, xnb.PREC_FP64_EXACT)
+    o = oracle_from(w)
+    o.init()
+    G, O = b.download(s), o.particles()
+    assert_bitwise_equal(G, O, fields=("rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz", "pe"))
+    npairs = compare_pairs(b, s, o)
+    assert 75 * w["n_atoms"] < npairs < 80 * w["n_atoms"]
+
+
+def test_trajectory_bit_exact_config0_100_steps():
+    """Same rebuild steps, same pair lists at every rebuild, same bits after 100 steps."""
+    w = workloads.lj_fcc_system(20, 0.8442, 1.44, 12345)
+    b, s = gpu_system(w)
+    b.init_particles(s, xnb.PREC_FP64_EXACT)
+    o = oracle_from(w)
+    o.init()
+    rebuild_steps = 0
+    for step in range(100):
+        r0 = b.info(s).rebuilds
+        b.step(1, xnb.PREC_FP64_EXACT, xnb.STEP_HOST_SYNC | xnb.STEP_ENERGY)
+        rebuilt = o.step()
+        assert (b.info(s).rebuilds - r0) == rebuilt, "rebuild decision differs at step %d" % step
+        if rebuilt:
+            rebuild_steps += 1
+            compare_pairs(b, s, o)
+    assert rebuild_steps >= 1
+    assert_bitwise_equal(b.download(s), o.particles(), fields=("rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz", "pe"))
+    ke_g, pe_g = b.energy(s)
+    ke_o, pe_o = o.energy()
+    assert ke_g == ke_o and pe_g == pe_o
+
+
+def test_fp64_and_mixed_forces_on_same_state():
+    w = workloads.lj_fcc_system(20, 0.8442, 1.44, 12345)
+    b, s = gpu_system(w)
+    b.init_particles(s, xnb.PREC_FP64_EXACT)
+    b.step(30, xnb.PREC_FP64_EXACT, xnb.STEP_HOST_SYNC)  # a liquid-like state with rebuilds behind it
+    ref = forces(b.download(s))
+    b.lennard_jones_force(s, xnb.PREC_FP64, True)
+    f64 = forces(b.download(s))
+    b.lennard_jones_force(s, xnb.PREC_MIXED, True)
+    fmx = forces(b.download(s))
+    e64, _ = force_error(f64, ref)
+    emx, rms = force_error(fmx, ref)
+    assert e64 <= FP64_TOL, e64
+    assert emx <= MIXED_TOL, emx
+    assert rms < emx or rms == emx
+
+
+def test_graph_equals_host_sync_exact():
+    w = workloads.lj_fcc_system(12, 0.8442, 1.44, 99)
+    b1, s1 = gpu_system(w)
+    b1.init_particles(s1, xnb.PREC_FP64_EXACT)
+    b1.step(60, xnb.PREC_FP64_EXACT, xnb.STEP_HOST_SYNC)
+    import torch
+    stream = torch.cuda.Stream()
+    b2 = new_batch([w["n_atoms"]], [ncells(w["geom"])])
+    b2.stream = __import__("ctypes").c_void_p(stream.cuda_stream)
+    s2 = b2.add_system(xnb.lj_params(w["geom"]), w["r"], w["v"], w["id"])
+    b2.init_particles(s2, xnb.PREC_FP64_EXACT)
+    g = b2.graph(20, xnb.PREC_FP64_EXACT, 0)
+    for _ in range(3):
+        g.launch()
+    stream.synchronize()
+    b2.check_errors()
+    assert_bitwise_equal(b2.download(s2), b1.download(s1))
+    assert b1.info(s1).rebuilds == b2.info(s2).rebuilds
+
+
+@pytest.mark.parametrize("n,rho,T", [(5, 1.0, 1.2), (4, 1.0, 0.9), (7, 0.7, 1.5)])
+def test_small_and_dense_systems_bit_exact(n, rho, T):
+    """D = 2 cells per axis, cells dense enough for AMR sub-grids (62 atoms/cell)."""
+    w = workloads.lj_fcc_system(n, rho, T, 3 + n)
+    b, s = gpu_system(w)
+    b.init_particles(s, xnb.PREC_FP64_EXACT)
+    o = oracle_from(w)
+    o.init()
+    compare_pairs(b, s, o)
+    for _ in range(50):
+        b.step(1, xnb.PREC_FP64_EXACT, xnb.STEP_HOST_SYNC)
+        if o.step():
+            compare_pairs(b, s, o)
+    assert_bitwise_equal(b.download(s), o.particles())
+
+
+def test_slab_with_empty_cells_bit_exact():
+    w = workloads.lj_slab_system(8, 0.8442, 0.8, 5)
+    b, s = gpu_system(w)
+    b.init_particles(s, xnb.PREC_FP64_EXACT)
+    o = oracle_from(w)
+    o.init()
+    assert (o.cell_counts() == 0).sum() > 0
+    compare_pairs(b, s, o)
+    for _ in range(50):
+        b.step(1, xnb.PREC_FP64_EXACT, xnb.STEP_HOST_SYNC)
+        if o.step():
+            compare_pairs(b, s, o)
+    assert_bitwise_equal(b.download(s), o.particles())
+
+
+def test_ni_golden_deck_on_gpu():
+    """input_lj_Ni.msp through the library: cells as the lattice generator leaves
+    them, 100 steps, check_values golden data within 1e-5 and bitwise = oracle."""
+    o = ni_deck_oracle()
+    P0 = o.particles()
+    counts = o.cell_counts()
+    r = np.stack([P0["rx"], P0["ry"], P0["rz"]], 1)
+    v = np.stack([P0["vx"], P0["vy"], P0["vz"]], 1)
+    b = new_batch([len(r)], [64], list_per_atom=130.0)
+    s = b.add_system(ni_deck_params(), r, v, P0["id"], cell_counts=counts)
+    b.init_particles(s, xnb.PREC_FP64_EXACT)
+    o.init()
+    for _ in range(100):
+        b.step(1, xnb.PREC_FP64_EXACT, xnb.STEP_HOST_SYNC)
+        o.step()
+    G = b.download(s)
+    assert_bitwise_equal(G, o.particles())
+    here = os.path.dirname(__file__)
+    with open(os.path.join(here, "golden", "check_values_lj_Ni.json")) as f:
+        gold = json.load(f)
+    idx = {int(i): k for k, i in enumerate(G["id"])}
+    er = ea = ev = 0.0
+    for row in gold["rows"]:
+        ref = np.array([float.fromhex(h) for h in row["hex"]])
+        k = idx[row["id"]]
+        d = np.array([G["rx"][k], G["ry"][k], G["rz"][k]]) - ref[0:3]
+        d -= 55.68 * np.round(d / 55.68)
+        er += float((d ** 2).sum())
+        ea += float(((np.array([G["fx"][k], G["fy"][k], G["fz"][k]]) - ref[3:6]) ** 2).sum())
+        ev += float(((np.array([G["vx"][k], G["vy"][k], G["vz"][k]]) - ref[6:9]) ** 2).sum())
+    assert er ** 0.5 <= 1e-5 and ea ** 0.5 <= 1e-5 and ev ** 0.5 <= 1e-5
+
+
+def test_operator_sequence_equals_fused_step():
+    """The unfused reference operators called one by one give the fused step's bits."""
+    w = workloads.lj_fcc_system(10, 0.8442, 1.44, 21)
+    b1, s1 = gpu_system(w)
+    b1.init_particles(s1, xnb.PREC_FP64_EXACT)
+    b2, s2 = gpu_system(w)
+    b2.init_particles(s2, xnb.PREC_FP64_EXACT)
+    for _ in range(40):
+        b1.step(1, xnb.PREC_FP64_EXACT, xnb.STEP_HOST_SYNC)
+        b2.push_f_v_r(1.0, s2)
+        b2.push_f_v(0.5, s2)
+        if b2.particle_displ_over(s2) > 0:
+            b2.update_particles_full(s2)
+        b2.lennard_jones_force(s2, xnb.PREC_FP64_EXACT, False)
+        b2.push_f_v(0.5, s2)
+    assert_bitwise_equal(b1.download(s1), b2.download(s2))
+
+
+def test_batched_systems_equal_alone():
+    """Uneven systems advanced together in one batch give each system's solo result."""
+    specs = workloads.ensemble_specs(5, seed=77, nmin=4, nmax=9)
+    ws = [workloads.lj_fcc_system(sp["n"], sp["rho"], sp["T"], sp["seed"]) for sp in specs]
+    big = new_batch([w["n_atoms"] for w in ws], [ncells(w["geom"]) for w in ws])
+    ids = [big.add_system(xnb.lj_params(w["geom"]), w["r"], w["v"], w["id"]) for w in ws]
+    big.init_particles(-1, xnb.PREC_MIXED)
+    big.step(80, xnb.PREC_MIXED, 0)
+    big.check_errors()
+    for w, s in zip(ws, ids):
+        b, so = gpu_system(w)
+        b.init_particles(so, xnb.PREC_MIXED)
+        b.step(80, xnb.PREC_MIXED, 0)
+        assert_bitwise_equal(big.download(s), b.download(so))
+        assert big.info(s).rebuilds == b.info(so).rebuilds
+
+
+def test_list_overflow_is_reported_and_recovered():
+    """A too-small list segment in graph mode is flagged, not written past."""
+    w = workloads.lj_fcc_system(8, 0.8442, 1.44, 4)
+    b, s = gpu_system(w, list_factor=1.0)
+    b.init_particles(s, xnb.PREC_MIXED)
+    # host-sync steps regrow the segment when a rebuild needs more room
+    b.step(200, xnb.PREC_MIXED, xnb.STEP_HOST_SYNC)
+    b.check_errors()
+    assert b.info(s).rebuilds >= 1
