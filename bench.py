@@ -1,0 +1,379 @@
+"""Benchmark of the LJ molecular-dynamics hot path on one GB300 (atom-steps/s).
+
+Workload (default): periodic FCC 100^3 = 4,000,000 atoms, rho* = 0.8442,
+T* = 1.44, truncated-and-shifted LJ rc = 2.5, skin 0.3, dt = 0.005; one bench
+"step" is one velocity-Verlet MD step (push, trigger, conditional rebin +
+neighbour rebuild, forces, push) of the whole system, in the mixed precision
+path. The state (~2.4 GB) is larger than L2 (129 MB), so no flush is needed.
+
+Reported on one JSON line: mixed-path atom-steps/s with inputs resident in
+HBM (`value`), the plain FP64 path beside it, the force error of the mixed
+path against FP64, an end-to-end run through the C ABI with host buffers
+(`e2e`), the roofline of the dominant (force) kernel, and the CPU oracle
+(restated reference OpenMP path) on the same workload.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun (N > 1) each rank advances its own replica (the systems are
+independent; no collective on the data path): scaling is weak.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Algorithmic work per atom-step of the LJ force kernel at rho* = 0.8442, rc = 2.5,
+# skin 0.3 (77.63 list / 55.25 in-cutoff neighbours per atom, each pair counted
+# once): FP64 path 0.5*(8*77.63 + 13*55.25) = 669.6 flop; mixed path
+# 0.5*(3*77.63 + 6*55.25) = 282.2 FP64 flop + 0.5*(5*77.63 + 7*55.25) = 387.4 FP32 flop.
+FLOP64_PER_ATOM_FP64_PATH = 669.6
+FLOP64_PER_ATOM_MIXED = 282.2
+FLOP32_PER_ATOM_MIXED = 387.4
+
+WORKLOAD = dict(n=100, rho=0.8442, T=1.44, seed=12345, rcut=2.5, skin=0.3, dt=0.005)
+METRIC = "atom-steps/s, 4M-atom LJ MD step (mixed precision; FP64 path and force error reported beside it)"
+
+
+def config_of(n, atoms, **extra):
+    c = {"workload": "lj_fcc_%d^3_rho0.8442_T1.44" % n, "atoms": atoms, "rcut": 2.5, "skin": 0.3, "dt": 0.005,
+         "flush": "state %.1f GB > L2 (129 MB)" % (atoms * 600 / 1e9)}
+    c.update(extra)
+    return c
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=WORKLOAD["n"], help="FCC unit cells per side")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": smax, "reasons": sorted(reasons)}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(n):
+    from exanbody_gb300 import workloads
+
+    return workloads.lj_fcc_system(n, WORKLOAD["rho"], WORKLOAD["T"], WORKLOAD["seed"], WORKLOAD["rcut"],
+                                   WORKLOAD["skin"])
+
+
+def cpu_oracle_run(w, steps, threads):
+    """The oracle (CPU restatement of the reference's OpenMP path) on workload w."""
+    from oracle.oracle import OracleSystem
+
+    g = w["geom"]
+    s = OracleSystem(g["origin"], g["extent"], g["dims"], g["cell_size"], WORKLOAD["rcut"], WORKLOAD["skin"], 1.0,
+                     1.0, WORKLOAD["dt"], kind="omp")
+    used = s.set_threads(threads)
+    s.load_flat(w["r"], w["v"], w["id"])
+    s.init()
+    return s, used
+
+
+def run_reference(args):
+    """--impl reference: the restated reference CPU path on the same workload."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    w = make_workload(args.n)
+    threads = os.cpu_count() or 1
+    s, used = cpu_oracle_run(w, args.steps, threads)
+    for _ in range(args.warmup):
+        s.step()
+    r0 = s.rebuilds
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.step()
+    dt = time.perf_counter() - t0
+    v = w["n_atoms"] * args.steps / dt
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": v,
+        "unit": "atom-steps/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": config_of(args.n, w["n_atoms"], parallelism="single"),
+        "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": used, "kind": "port",
+                         "sample": "%d MD steps of the %d-atom system (%d rebuilds), oracle/xnb_oracle.cpp OpenMP"
+                                   % (args.steps, w["n_atoms"], s.rebuilds - r0)},
+        "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def fp64_peak_tflops(torch, dev):
+    """FP64 FMA throughput measured live with cuBLAS DGEMM (2*N^3 flop)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    best = 0.0
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = max(best, 2.0 * n ** 3 / (ms * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def run_ours(args):
+    import ctypes
+
+    import torch
+
+    from exanbody_gb300 import xnb
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    w = make_workload(args.n)
+    N = w["n_atoms"]
+    g = w["geom"]
+    ncell = g["dims"][0] * g["dims"][1] * g["dims"][2]
+    params = xnb.lj_params(g, rcut=WORKLOAD["rcut"], rcut_inc=WORKLOAD["skin"], dt=WORKLOAD["dt"])
+
+    def new_batch():
+        b = xnb.Batch(N + 64, ncell + 64, int(N * 120) + 4096, max_systems=1, device=local)
+        b.stream = sp
+        return b
+
+    def timed(fn, reps=1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    # ---- mixed path, resident state ----
+    b = new_batch()
+    s = b.add_system(params, w["r"], w["v"], w["id"], list_factor=1.2)
+    b.init_particles(s, xnb.PREC_MIXED)
+    b.step(max(3, args.warmup), xnb.PREC_MIXED, 0)
+    b.check_errors()
+    reb0 = b.info(s).rebuilds
+    l0 = b.kernel_launches()
+    with Clocks(local) as ck:
+        ms = timed(lambda: b.step(args.steps, xnb.PREC_MIXED, 0))
+    clocks = ck.summary()
+    launches = b.kernel_launches() - l0
+    b.check_errors()
+    rebuilds = b.info(s).rebuilds - reb0
+    value = world * N * args.steps / (ms * 1e-3)
+
+    # ---- plain FP64 path from the same state ----
+    k64 = max(5, min(args.steps, 40))
+    b.step(2, xnb.PREC_FP64, 0)
+    ms64 = timed(lambda: b.step(k64, xnb.PREC_FP64, 0))
+    b.check_errors()
+    value64 = N * k64 / (ms64 * 1e-3)
+
+    # ---- force error of the mixed path against FP64 on one state ----
+    b.lennard_jones_force(s, xnb.PREC_FP64, False)
+    P = b.download(s)
+    f64 = np.stack([P["fx"], P["fy"], P["fz"]], 1)
+    b.lennard_jones_force(s, xnb.PREC_MIXED, False)
+    P = b.download(s)
+    fmx = np.stack([P["fx"], P["fy"], P["fz"]], 1)
+    d = np.linalg.norm(fmx - f64, axis=1)
+    mag = np.linalg.norm(f64, axis=1)
+    frms = float(np.sqrt((mag ** 2).mean()))
+    rel = d / np.maximum(mag, frms)
+    err_max, err_rms = float(rel.max()), float(np.sqrt((rel ** 2).mean()))
+
+    # ---- dominant kernel timing (force traversal alone, same launch as in the step) ----
+    reps = 10
+    ms_force = timed(lambda: b.lennard_jones_force(s, xnb.PREC_MIXED, False), reps) / reps
+    ms_force64 = timed(lambda: b.lennard_jones_force(s, xnb.PREC_FP64, False), 3) / 3
+    peak64 = fp64_peak_tflops(torch, dev)
+    achieved = FLOP64_PER_ATOM_MIXED * N / (ms_force * 1e-3) / 1e12
+    b.close()
+
+    # ---- end to end through the C ABI: host arrays in, K steps, host arrays out ----
+    e2e = None
+    if not args.no_e2e:
+        out = {k: np.empty(N) for k in ("rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz")}
+
+        def e2e_run():
+            bb = new_batch()
+            ss = bb.add_system(params, w["r"], w["v"], w["id"], list_factor=1.2)
+            bb.init_particles(ss, xnb.PREC_MIXED)
+            bb.step(args.steps, xnb.PREC_MIXED, 0)
+            got = bb.download(ss)
+            bb.check_errors()
+            bb.close()
+            return got
+
+        e2e_run()  # warm the allocator and the module
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_run()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        h2d = N * (6 * 8 + 8)
+        d2h = N * (10 * 8 + 8 + 4)
+        e2e = {"value": world * N * args.steps / dt, "unit": "atom-steps/s",
+               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+               "run": "host arrays -> xnb_system_add -> xnb_init_particles -> %d x xnb_step -> xnb_system_download"
+                      % args.steps}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        so, used = cpu_oracle_run(w, 0, threads)
+        sample = 10
+        r0 = so.rebuilds
+        t0 = time.perf_counter()
+        for _ in range(sample):
+            so.step()
+        dt = time.perf_counter() - t0
+        cpu = {"value": N * sample / dt, "unit": "atom-steps/s", "cores": used, "kind": "port",
+               "sample": "%d MD steps of the same %d-atom system after init (%d rebuilds), oracle OpenMP build"
+                         % (sample, N, so.rebuilds - r0)}
+        del so
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "atom-steps/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64+f32",
+            "data": "synthetic",
+            "config": config_of(args.n, N, parallelism="replicas" if world > 1 else "single",
+                                precision="mixed", rebuilds_in_timed_steps=rebuilds),
+            "fp64": {"value": value64, "unit": "atom-steps/s", "steps": k64,
+                     "speedup_mixed_vs_fp64": value / world / value64},
+            "force_error_mixed_vs_fp64": {"max": err_max, "rms": err_rms, "tolerance": 1e-5},
+            "clocks": clocks,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "kernel": "k_force<mixed>", "achieved": achieved, "peak": peak64,
+                         "unit": "TFLOP/s", "frac": achieved / peak64,
+                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                         "ms_per_launch": ms_force, "ms_per_launch_fp64_kernel": ms_force64,
+                         "traffic": None},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())
