@@ -821,4 +821,34 @@ int xnb_check_errors(xnb_batch* b, void* stream) {
 
 int64_t xnb_stats_kernel_launches(const xnb_batch* b) { return b ? static_cast<int64_t>(b->launches) : -1; }
 
+// chunk_neighbors for callers that cannot allocate device memory: only the
+// caller's buffers and the library's static scratch array are touched.
+int xnb_chunk_neighbors_noalloc(const xnb_lj_params* p, int64_t n, const double* rx, const double* ry,
+                                const double* rz, const uint32_t* cell_start, const uint32_t* cell_count,
+                                uint32_t* nbr, int64_t nbr_capacity, uint32_t* nbr_start, uint32_t* nbr_count,
+                                int64_t* total_out, void* stream) {
+  int rc = validate(p);
+  if (rc) return rc;
+  if (n < 0 || !rx || !ry || !rz || !cell_start || !cell_count || !nbr || !nbr_start || !nbr_count || !total_out ||
+      nbr_capacity < 0)
+    return fail(XNB_ERR_ARG, "chunk_neighbors without allocation: null buffer or negative size");
+  SysDesc d = make_desc(*p);
+  d.cell_base = 0;
+  d.ncells = static_cast<uint32_t>(static_cast<uint64_t>(p->dims[0]) * p->dims[1] * p->dims[2]);
+  d.part_base = 0;
+  d.npart = static_cast<uint32_t>(n);
+  unsigned long long total = 0;
+  std::string err;
+  const int lr = launch_neighbors_static(d, static_cast<uint32_t>(n), rx, ry, rz, cell_start, cell_count, nbr,
+                                         static_cast<uint64_t>(nbr_capacity), nbr_start, nbr_count, &total,
+                                         static_cast<cudaStream_t>(stream), &err);
+  if (lr == -1) return fail(XNB_ERR_ARG, err);
+  if (lr != 0) return fail(XNB_ERR_CUDA, err);
+  *total_out = static_cast<int64_t>(total);
+  if (total > static_cast<unsigned long long>(nbr_capacity))
+    return fail(XNB_ERR_CAPACITY, "chunk_neighbors without allocation: " + std::to_string(total) +
+                                      " entries needed, capacity " + std::to_string(nbr_capacity));
+  return XNB_OK;
+}
+
 }  // extern "C"

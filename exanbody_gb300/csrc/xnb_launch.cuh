@@ -1,5 +1,7 @@
 // Host-side launchers of the xnb kernels (internal; the public C ABI is include/xnb_gpu.h).
 #pragma once
+#include <string>
+
 #include "xnb_internal.cuh"
 
 namespace xnb {
@@ -45,5 +47,13 @@ int launch_scan_u32_to_u64(const uint32_t* in, unsigned long long* out, uint32_t
                             unsigned long long* block_scratch, cudaStream_t stream);
 size_t scan_scratch_elems(uint32_t n);
 
+
+// Allocation-free neighbour build of one system (xnb_static_scratch.cu): scratch
+// in a file-scope device array; returns 0, -1 (size above the array's limit,
+// *err says which) or -2 (CUDA error).
+int launch_neighbors_static(const SysDesc& S, uint32_t n, const double* rx, const double* ry, const double* rz,
+                            const uint32_t* cell_start, const uint32_t* cell_n, uint32_t* nbr, uint64_t cap,
+                            uint32_t* nbr_start, uint32_t* nbr_cnt, unsigned long long* total_out,
+                            cudaStream_t stream, std::string* err);
 
 }  // namespace xnb

@@ -29,7 +29,7 @@ EXPORTED = [
     "xnb_system_energy", "xnb_init_particles", "xnb_push_f_v_r", "xnb_push_f_v", "xnb_particle_displ_over",
     "xnb_update_particles_full", "xnb_chunk_neighbors", "xnb_backup_r", "xnb_lennard_jones_force",
     "xnb_ghost_update_r", "xnb_step", "xnb_step_graph_create", "xnb_graph_launch", "xnb_graph_destroy",
-    "xnb_check_errors", "xnb_stats_kernel_launches",
+    "xnb_check_errors", "xnb_stats_kernel_launches", "xnb_chunk_neighbors_noalloc",
 ]
 
 
@@ -130,6 +130,8 @@ def load(build_if_missing=True):
     lib.xnb_check_errors.argtypes = [vp, vp]
     lib.xnb_stats_kernel_launches.restype = i64
     lib.xnb_stats_kernel_launches.argtypes = [vp]
+    u32p = P(C.c_uint32)
+    lib.xnb_chunk_neighbors_noalloc.argtypes = [P(LJParams), i64, vp, vp, vp, vp, vp, vp, i64, vp, vp, P(i64), vp]
     _LIB = lib
     return lib
 
@@ -279,6 +281,18 @@ class Batch:
 
     def kernel_launches(self):
         return int(self.lib.xnb_stats_kernel_launches(self.h))
+
+
+def chunk_neighbors_noalloc(params, n, rx, ry, rz, cell_start, cell_count, nbr, nbr_capacity, nbr_start, nbr_count,
+                            stream=None):
+    """xnb_chunk_neighbors_noalloc on caller-owned device buffers (device pointers as ints).
+    Returns the number of entries written."""
+    lib = load()
+    total = C.c_int64()
+    _ck(lib.xnb_chunk_neighbors_noalloc(C.byref(params), int(n), rx, ry, rz, cell_start, cell_count, nbr,
+                                        int(nbr_capacity), nbr_start, nbr_count, C.byref(total),
+                                        C.c_void_p(stream) if stream else None))
+    return total.value
 
 
 class Graph:

@@ -172,6 +172,34 @@ int xnb_check_errors(xnb_batch* b, void* stream);
  * the reference's equivalent bookkeeping lives in onika's profiling layer). */
 int64_t xnb_stats_kernel_launches(const xnb_batch* b);
 
+/* ---- allocation-free entry point ---- */
+
+/* No counterpart in the reference. chunk_neighbors for one system, for callers
+ * that cannot allocate device memory where they need the lists: a host
+ * framework that owns all device memory through its own pools and forbids
+ * cudaMalloc inside a step, or code running while a stream is being captured
+ * into a CUDA graph (allocation is not permitted there). It allocates nothing:
+ * inputs and outputs are the caller's device buffers, and scratch is one
+ * file-scope device array of the library (about 5.3 MB, held by every GPU that
+ * loads the library until exit).
+ *   rx, ry, rz       n positions in cell order (cells in linear order (k*Dj+j)*Di+i)
+ *   cell_start/count per cell: first particle index (0-based) and particle count
+ *   nbr              output entries (local index << 5 | periodic image code), in
+ *                    the reference's (cell_enc, p_b) order; capacity nbr_capacity
+ *   nbr_start/count  output per particle: first entry and number of entries
+ *   total_out        entries needed (set also when the capacity is too small)
+ * Limits: n <= 1,048,576 particles and <= 131,072 cells; larger inputs return
+ * XNB_ERR_ARG with the limit in xnb_last_error_string(). Returns XNB_ERR_CAPACITY
+ * when total_out > nbr_capacity (nbr is then left unwritten).
+ * The first call on a device looks up the scratch array's address (set-up);
+ * make it before any stream capture that includes this call. All calls share the
+ * array: calls that overlap on the GPU race and must be serialised by the
+ * caller. The call synchronises `stream` to return total_out. */
+int xnb_chunk_neighbors_noalloc(const xnb_lj_params* p, int64_t n, const double* rx, const double* ry,
+                                const double* rz, const uint32_t* cell_start, const uint32_t* cell_count,
+                                uint32_t* nbr, int64_t nbr_capacity, uint32_t* nbr_start, uint32_t* nbr_count,
+                                int64_t* total_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
