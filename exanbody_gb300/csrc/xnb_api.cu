@@ -208,19 +208,32 @@ SysDesc make_desc(const xnb_lj_params& p) {
   d.eps24_f = static_cast<float>(d.eps24);
   d.eps4_f = static_cast<float>(d.eps4);
   d.e_shift_f = static_cast<float>(d.e_shift);
-  // Error bounds of the FP32 prefilters (u = 2^-24 unit roundoff).
-  //  neighbour test: coordinates are converted relative to cell a's origin, so
-  //  |coord| <= M = 2*cell + nbh; each axis difference then differs from the
-  //  reference's FP64 difference by at most D = (nbh + 2M) u (1.01), and
-  //  |d2_f32 - d2_f64| <= 3 D (2 nbh + D) + 4 u (nbh^2 + 1); margin = 4x that.
+  // Error bounds of the FP32 prefilters (u = 2^-24 unit roundoff). Positions
+  // are mirrored as pf = fl32(x - origin) with |x - origin| <= X = max period
+  // + nbh (drift allowance); an image coordinate adds fl32(period) (P); so one
+  // axis of an FP32 difference is within D = (3X + 2P + R) u (1.01) of the FP64
+  // one for pairs within distance R, and |d2_f32 - d2_f64| <=
+  // err(R) = 2 sqrt(3) R D + 3 D^2 + 4 u (R^2 + 1). Each margin is 4 err.
   const double u = std::ldexp(1.0, -24);
-  const double M = 2.0 * p.cell_size + nbh;
-  const double D = (nbh + 2.0 * M) * u * 1.01;
-  const double err_n = 3.0 * D * (2.0 * nbh + D) + 4.0 * u * (nbh * nbh + 1.0);
+  double P = 0.0;
+  for (int a = 0; a < 3; ++a) P = std::max(P, std::fabs(d.period[a]));
+  const double X = P + nbh;
+  auto err_at = [&](double R) {
+    const double D = (3.0 * X + 2.0 * P + R) * u * 1.01;
+    return 2.0 * std::sqrt(3.0) * R * D + 3.0 * D * D + 4.0 * u * (R * R + 1.0);
+  };
   d.nbh2_f = static_cast<float>(d.nbh2);
-  d.nbh_margin_f = static_cast<float>(4.0 * err_n);
-  //  force cutoff test: d_f32 = fl32(d_f64) per axis, |r2_f32 - d2_f64| <= 5.1 u d2;
-  //  margin = 4x at rc^2 (+1 absolute guard so tiny d2 also go to FP64).
+  d.nbh_margin_f = static_cast<float>(4.0 * err_at(nbh));
+  d.pre_margin_f = static_cast<float>(4.0 * err_at(p.rcut));
+  for (int a = 0; a < 3; ++a) {
+    d.period_f[a] = static_cast<float>(d.period[a]);
+    d.outer_lo_f[a] = static_cast<float>(d.outer_lo[a] - d.origin[a]);
+    d.outer_hi_f[a] = static_cast<float>(d.outer_hi[a] - d.origin[a]);
+  }
+  // ghost filter compare: coordinate error 2 (X + P) u, bound conversion (X + nbh) u
+  d.filter_margin_f = static_cast<float>(4.0 * (2.0 * (X + P) + X + nbh) * u * 1.01);
+  //  force cutoff test of the mixed path: d_f32 = fl32(d_f64) per axis,
+  //  |r2_f32 - d2_f64| <= 5.1 u d2; margin = 4x at rc^2 (+1 absolute guard so tiny d2 also go to FP64).
   d.rc2_f = static_cast<float>(d.rcut2);
   d.rc_margin_f = static_cast<float>(4.0 * 5.1 * u * (d.rcut2 + 1.0));
   return d;
@@ -293,7 +306,7 @@ int neighbors_sync(xnb_batch* b, cudaStream_t st) {
 
 int clear_rebuild(xnb_batch* b, cudaStream_t st) {
   const Extent ex = b->extent();
-  b->launches += launch_mark_rebuild(ex, b->d_st, 2, -1, st);
+  b->launches += launch_mark_rebuild(ex, b->d_st, 2, -1, b->a.any_rebuild, st);
   return XNB_OK;
 }
 
@@ -311,7 +324,7 @@ const char* xnb_last_error_string(void) { return g_err.c_str(); }
 int xnb_version(void) { return 10000; }
 
 int64_t xnb_system_bytes(int64_t n, int64_t ncells, double list_per_particle) {
-  const int64_t per_part = 8 * 10 + 8 + 4 + 12 + 24 + 8 * 9 + 8 + 4 * 3 + 4 * 3;
+  const int64_t per_part = 8 * 10 + 8 + 4 + 12 + 24 + 8 * 9 + 8 + 4 * 3 + 4 * 3 + 16 + 4 * kMaskWords;
   const int64_t per_cell = 4 * 7 + 8 * 2 + 4;
   return n * per_part + ncells * per_cell + static_cast<int64_t>(static_cast<double>(n) * list_per_particle) * 4;
 }
@@ -338,6 +351,9 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
                     &a.t_fx, &a.t_fy, &a.t_fz};
   for (double** p : dbl) rc = rc ? rc : dalloc(b, p, P);
   rc = rc ? rc : dalloc(b, &a.id, P);
+  rc = rc ? rc : dalloc(b, &a.pf, P);
+  rc = rc ? rc : dalloc(b, &a.nbr_masks, P * kMaskWords);
+  rc = rc ? rc : dalloc(b, &a.any_rebuild, 4);
   rc = rc ? rc : dalloc(b, &a.t_id, P);
   uint32_t** u32p[] = {&a.pcell, &a.bkx, &a.bky, &a.bkz, &a.pdest, &a.plocal, &a.mover_list,
                        &a.nbr_start, &a.nbr_cnt, &a.nbr_cursor};
@@ -362,6 +378,7 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   cudaMemset(a.cell_n, 0, (Cc + 1) * sizeof(uint32_t));
   cudaMemset(a.cell_start, 0, (Cc + 1) * sizeof(uint32_t));
   cudaMemset(b->d_st, 0, sizeof(SysState) * cfg->max_systems);
+  cudaMemset(a.any_rebuild, 0, sizeof(unsigned int));
   if (cudaDeviceSynchronize() != cudaSuccess) {
     xnb_batch_destroy(b);
     return fail(XNB_ERR_CUDA, "initialisation failed");
@@ -391,6 +408,7 @@ int xnb_system_add(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double
   int rc = validate(p);
   if (rc) return rc;
   if (n < 0 || (n > 0 && (!rx || !ry || !rz || !vx || !vy || !vz || !id))) return fail(XNB_ERR_ARG, "bad particle arrays");
+  if (n >= (1ll << 26)) return fail(XNB_ERR_ARG, "a system holds at most 2^26 - 1 particles");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   XCK(cudaSetDevice(b->device));
   int slot = -1;
@@ -471,6 +489,11 @@ int xnb_system_add(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double
   if (nb) {
     XCK(cudaMemcpyAsync(a.id + poff, hid.data(), nb * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     XCK(cudaMemcpyAsync(a.pcell + poff, hcell.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    std::vector<float4> hpf(nb);
+    for (size_t q = 0; q < nb; ++q)
+      hpf[q] = make_float4(static_cast<float>(h[0][q] - p->origin[0]), static_cast<float>(h[1][q] - p->origin[1]),
+                           static_cast<float>(h[2][q] - p->origin[2]), 0.f);
+    XCK(cudaMemcpyAsync(a.pf + poff, hpf.data(), nb * sizeof(float4), cudaMemcpyHostToDevice, st));
     XCK(cudaMemsetAsync(a.fx + poff, 0, nb * sizeof(double), st));
     XCK(cudaMemsetAsync(a.fy + poff, 0, nb * sizeof(double), st));
     XCK(cudaMemsetAsync(a.fz + poff, 0, nb * sizeof(double), st));
@@ -623,7 +646,7 @@ int xnb_init_particles(xnb_batch* b, int32_t s, int32_t precision, void* stream)
   XCK(cudaSetDevice(b->device));
   const Extent ex = b->extent();
   // init marks every selected system; the counter then starts from zero
-  b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, st);
+  b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, b->a.any_rebuild, st);
   b->launches += launch_rebin(ex, b->d_sys, b->d_st, b->a, st);
   rc = neighbors_sync(b, st);
   if (rc) return rc;
@@ -686,7 +709,7 @@ int xnb_update_particles_full(xnb_batch* b, int32_t s, void* stream) {
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const Extent ex = b->extent();
-  b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, st);
+  b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, b->a.any_rebuild, st);
   b->launches += launch_rebin(ex, b->d_sys, b->d_st, b->a, st);
   rc = neighbors_sync(b, st);
   if (rc) return rc;
@@ -699,7 +722,7 @@ int xnb_chunk_neighbors(xnb_batch* b, int32_t s, void* stream) {
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const Extent ex = b->extent();
-  b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, st);
+  b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, b->a.any_rebuild, st);
   rc = neighbors_sync(b, st);
   if (rc) return rc;
   clear_rebuild(b, st);
@@ -711,7 +734,7 @@ int xnb_backup_r(xnb_batch* b, int32_t s, void* stream) {
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const Extent ex = b->extent();
-  b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, st);
+  b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, b->a.any_rebuild, st);
   b->launches += launch_backup(ex, b->d_sys, b->d_st, b->a, st);
   clear_rebuild(b, st);
   return check_launch();
@@ -738,7 +761,7 @@ int xnb_step(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, voi
   for (int k = 0; k < nsteps; ++k) {
     // verlet_first_half + trigger_move_particles
     b->launches += launch_first_half(ex, b->d_sys, b->d_st, b->a, true, true, true, 1.0, 0.5, exact, -1, st);
-    b->launches += launch_mark_rebuild(ex, b->d_st, 1, -1, st);
+    b->launches += launch_mark_rebuild(ex, b->d_st, 1, -1, b->a.any_rebuild, st);
     bool rebuild = true;
     if (flags & XNB_STEP_HOST_SYNC) {
       int rc = pull_states(b, st);

@@ -37,6 +37,7 @@ __device__ __forceinline__ int sub_grid_side(uint32_t n, double density) {
 // particle leaves its cell when dst differs or it lies >= epsilon outside dst's bounds.
 __global__ void __launch_bounds__(256)
     k_rebin_dest(uint32_t n_part, const SysDesc* __restrict__ sys, SysState* st, DevArrays a) {
+  if (*a.any_rebuild == 0) return;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
     const uint32_t c = a.pcell[i];
     if (c == kInvalid) continue;
@@ -104,6 +105,7 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(128)
     k_rebin_compact(uint32_t n_cells, const SysDesc* __restrict__ sys, const SysState* __restrict__ st,
                     DevArrays a) {
+  if (*a.any_rebuild == 0) return;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_cells; c += warps) {
@@ -188,6 +190,7 @@ __device__ __forceinline__ SrcInfo arrivals_of(const SysDesc& S, const DevArrays
 // K_r3: new particle count of every cell (flagged systems: stayers + arrivals).
 __global__ void __launch_bounds__(128)
     k_rebin_count(uint32_t n_cells, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a) {
+  if (*a.any_rebuild == 0) return;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_cells; c += warps) {
@@ -211,6 +214,7 @@ __global__ void __launch_bounds__(128)
 __global__ void __launch_bounds__(128)
     k_rebin_scatter(uint32_t n_cells, const SysDesc* __restrict__ sys, const SysState* __restrict__ st,
                     DevArrays a) {
+  if (*a.any_rebuild == 0) return;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_cells; c += warps) {
@@ -251,6 +255,7 @@ __global__ void __launch_bounds__(128)
 // cell table update, and backup_r (io/backup_r.cpp:56-79).
 __global__ void __launch_bounds__(128)
     k_rebin_finalize(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a) {
+  if (*a.any_rebuild == 0) return;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_cells; c += warps) {
@@ -298,6 +303,7 @@ __global__ void __launch_bounds__(128)
       a.vx[dst] = a.t_vx[src]; a.vy[dst] = a.t_vy[src]; a.vz[dst] = a.t_vz[src];
       a.fx[dst] = a.t_fx[src]; a.fy[dst] = a.t_fy[src]; a.fz[dst] = a.t_fz[src];
       a.id[dst] = a.t_id[src];
+      a.pf[dst] = make_pf(S, x, y, z);
       a.pcell[dst] = c;
       const uint32_t bx = encode_u32(x, lo[0], S.cell_size);
       const uint32_t by = encode_u32(y, lo[1], S.cell_size);
@@ -318,6 +324,7 @@ __global__ void __launch_bounds__(128)
 // backup_r alone (io/backup_r.cpp:42-79) for flagged systems.
 __global__ void __launch_bounds__(256)
     k_backup(uint32_t n_part, const SysDesc* __restrict__ sys, SysState* st, DevArrays a) {
+  if (*a.any_rebuild == 0) return;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
     const uint32_t c = a.pcell[i];
     if (c == kInvalid) continue;
@@ -337,7 +344,8 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-__global__ void k_arm(int nsys, SysState* st) {
+__global__ void k_arm(int nsys, SysState* st, const unsigned int* any) {
+  if (*any == 0) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s < nsys && st[s].rebuild) st[s].rebuild_armed = 1;
 }
@@ -347,22 +355,68 @@ __global__ void k_arm(int nsys, SysState* st) {
 // chunk_neighbors_execute.h:110-244, 286-372): for each particle of cell a, the
 // particles of the 27 cells around a (periodic images included) with
 // (cell_a != cell_b || p_a != p_b) && 0 < d2 <= nbh_dist^2, d2 = norm2(r_a - r_b),
-// in (cell_enc, p_b) order. Candidates are staged per warp in shared memory as
-// FP32 coordinates relative to cell a's origin; the FP32 distance decides
-// whenever it is farther than a proven error bound from the threshold, and the
-// FP64 d2 of the reference decides the rest, so the pair set is bit-exact.
-// Ghost particles outside the partner block enlarged by ghost_dist are not
-// candidates (update_ghosts_comm_scheme.cpp:462-469).
-// One warp per cell, lanes over candidates, ballot compaction keeps the order.
+// in (cell_enc, p_b) order. Ghost particles outside the partner block enlarged
+// by ghost_dist are not candidates (update_ghosts_comm_scheme.cpp:462-469).
+//
+// One warp per cell. Candidates are staged in shared memory as float4 (FP32
+// position relative to the system origin, entry bits in .w); lanes test 32
+// candidates at a time against one particle of the cell and a ballot keeps the
+// hits in order. The FP32 distance decides whenever it lies farther than a
+// proven error bound from the threshold; otherwise the reference's FP64 d2 (and
+// the FP64 ghost filter) decide, so the pair set is bit-exact.
+// The count pass stores every 32-candidate ballot of a particle (kMaskWords
+// words); the fill pass then writes entries from the masks without testing
+// again. Cells with more than kMaskWords*32 candidates are tested again.
+constexpr uint32_t kAmbiguousBit = 0x80000000u;  // entry flag: ghost filter undecided in FP32
+
+__device__ __forceinline__ float4 stage_candidate(const SysDesc& S, const DevArrays& a, uint32_t j, uint32_t gc) {
+  const float4 pb = a.pf[j];
+  float4 rb;
+  rb.x = image_coord_f(pb.x, S.period_f[0], static_cast<int>(gc % 3u));
+  rb.y = image_coord_f(pb.y, S.period_f[1], static_cast<int>((gc / 3u) % 3u));
+  rb.z = image_coord_f(pb.z, S.period_f[2], static_cast<int>(gc / 9u));
+  uint32_t ent = ((j - S.part_base) << 5) | gc;
+  if (gc != static_cast<uint32_t>(kImageCenter)) {
+    const float fm = S.filter_margin_f;
+    const float v[3] = {rb.x, rb.y, rb.z};
+    bool out = false, amb = false;
+    for (int ax = 0; ax < 3; ++ax) {
+      if (v[ax] < S.outer_lo_f[ax] - fm || v[ax] > S.outer_hi_f[ax] + fm) out = true;
+      else if (v[ax] < S.outer_lo_f[ax] + fm || v[ax] > S.outer_hi_f[ax] - fm) amb = true;
+    }
+    if (out) ent = kInvalid;
+    else if (amb) ent |= kAmbiguousBit;
+  }
+  rb.w = __uint_as_float(ent);
+  return rb;
+}
+
+// The reference's FP64 decision for one (particle i, candidate entry) pair.
+__device__ __noinline__ bool exact_neighbor_test(const SysDesc& S, const DevArrays& a, uint32_t i, uint32_t ent) {
+  const uint32_t e = ent & ~kAmbiguousBit;
+  const uint32_t j = S.part_base + (e >> 5);
+  const uint32_t gc = e & 31u;
+  const double xb = image_coord(a.rx[j], S.period[0], static_cast<int>(gc % 3u));
+  const double yb = image_coord(a.ry[j], S.period[1], static_cast<int>((gc / 3u) % 3u));
+  const double zb = image_coord(a.rz[j], S.period[2], static_cast<int>(gc / 9u));
+  bool keep = true;
+  if (gc != static_cast<uint32_t>(kImageCenter))
+    keep = xb >= S.outer_lo[0] && xb <= S.outer_hi[0] && yb >= S.outer_lo[1] && yb <= S.outer_hi[1] &&
+           zb >= S.outer_lo[2] && zb <= S.outer_hi[2];
+  const double d2 = norm2_rn(__dsub_rn(a.rx[i], xb), __dsub_rn(a.ry[i], yb), __dsub_rn(a.rz[i], zb));
+  return keep && d2 > 0.0 && d2 <= S.nbh2;
+}
+
 template <bool FILL>
 __global__ void __launch_bounds__(128)
     k_neighbors(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap) {
+  if (*a.any_rebuild == 0) return;
   extern __shared__ unsigned char smem_raw[];
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t wib = threadIdx.x >> 5;
   float4* srel = reinterpret_cast<float4*>(smem_raw) + static_cast<size_t>(wib) * cap;
-  uint32_t* sent = reinterpret_cast<uint32_t*>(reinterpret_cast<float4*>(smem_raw) + static_cast<size_t>(blockDim.x >> 5) * cap) +
-                   static_cast<size_t>(wib) * cap;
+  uint32_t* sent = reinterpret_cast<uint32_t*>(srel);  // fill pass from masks: entries only, same per-warp region
+  const unsigned lt = lanemask_lt();
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + wib; c < n_cells; c += warps) {
     const uint32_t s = a.cell_sys[c];
@@ -381,7 +435,6 @@ __global__ void __launch_bounds__(128)
     }
     int ci, cj, ck;
     cell_ijk(S, c - S.cell_base, ci, cj, ck);
-    const double o[3] = {cell_lo(S, 0, ci), cell_lo(S, 1, cj), cell_lo(S, 2, ck)};
 
     if (FILL) {
       // per-particle list starts: cell offset + prefix of the counts
@@ -427,6 +480,7 @@ __global__ void __launch_bounds__(128)
     }
     const uint32_t ncand = __shfl_sync(0xffffffffu, g_off, 26);
     g_off -= g_n;
+    const bool use_masks = ncand <= kMaskWords * 32u;
 
     const float nb_hi = S.nbh2_f + S.nbh_margin_f;
     const float nb_lo = S.nbh2_f - S.nbh_margin_f;
@@ -435,6 +489,7 @@ __global__ void __launch_bounds__(128)
 
     for (uint32_t c0 = 0; c0 < ncand; c0 += static_cast<uint32_t>(cap)) {
       const uint32_t c1 = min(ncand, c0 + static_cast<uint32_t>(cap));
+      const bool test = !FILL || !use_masks;
       // stage candidates [c0, c1)
       for (int g = 0; g < 27; ++g) {
         const uint32_t gs = __shfl_sync(0xffffffffu, g_start, g);
@@ -446,72 +501,59 @@ __global__ void __launch_bounds__(128)
           const uint32_t t = go + q;
           if (t < c0 || t >= c1) continue;
           const uint32_t j = gs + q;
-          const double xb = image_coord(a.rx[j], S.period[0], static_cast<int>(gc % 3u));
-          const double yb = image_coord(a.ry[j], S.period[1], static_cast<int>((gc / 3u) % 3u));
-          const double zb = image_coord(a.rz[j], S.period[2], static_cast<int>(gc / 9u));
-          bool keep = true;
-          if (gc != static_cast<uint32_t>(kImageCenter)) {
-            keep = xb >= S.outer_lo[0] && xb <= S.outer_hi[0] && yb >= S.outer_lo[1] && yb <= S.outer_hi[1] &&
-                   zb >= S.outer_lo[2] && zb <= S.outer_hi[2];
+          if (test) {
+            srel[t - c0] = stage_candidate(S, a, j, gc);
+          } else {
+            sent[t - c0] = ((j - S.part_base) << 5) | gc;
           }
-          srel[t - c0] = make_float4(static_cast<float>(__dsub_rn(xb, o[0])), static_cast<float>(__dsub_rn(yb, o[1])),
-                                     static_cast<float>(__dsub_rn(zb, o[2])), 0.f);
-          sent[t - c0] = keep ? (((j - S.part_base) << 5) | gc) : kInvalid;
         }
       }
       __syncwarp();
       const uint32_t m = c1 - c0;
       for (uint32_t pa = 0; pa < na; ++pa) {
         const uint32_t i = sa + pa;
-        const double xa = a.rx[i], ya = a.ry[i], za = a.rz[i];
-        const float ax = static_cast<float>(__dsub_rn(xa, o[0]));
-        const float ay = static_cast<float>(__dsub_rn(ya, o[1]));
-        const float az = static_cast<float>(__dsub_rn(za, o[2]));
-        const uint32_t self_ent = ((i - S.part_base) << 5) | static_cast<uint32_t>(kImageCenter);
-        uint32_t cnt = 0;
+        uint32_t* maskp = a.nbr_masks + static_cast<size_t>(i) * kMaskWords + c0 / 32;
         uint32_t cursor = 0;
         if (FILL) cursor = a.nbr_cursor[i];
-        for (uint32_t t0 = 0; t0 < m; t0 += 32) {
-          const uint32_t t = t0 + lane;
-          bool hit = false;
-          uint32_t ent = kInvalid;
-          if (t < m) {
-            ent = sent[t];
-            if (ent != kInvalid && ent != self_ent) {
-              const float4 b = srel[t];
-              const float dx = ax - b.x, dy = ay - b.y, dz = az - b.z;
-              const float d2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-              if (d2f > nb_hi) {
-                hit = false;
-              } else if (d2f < nb_lo && d2f > nb_zero) {
-                hit = true;
-              } else {
-                const uint32_t j = S.part_base + (ent >> 5);
-                const uint32_t gc = ent & 31u;
-                const double xb = image_coord(a.rx[j], S.period[0], static_cast<int>(gc % 3u));
-                const double yb = image_coord(a.ry[j], S.period[1], static_cast<int>((gc / 3u) % 3u));
-                const double zb = image_coord(a.rz[j], S.period[2], static_cast<int>(gc / 9u));
-                const double d2 = norm2_rn(__dsub_rn(xa, xb), __dsub_rn(ya, yb), __dsub_rn(za, zb));
-                hit = d2 > 0.0 && d2 <= S.nbh2;
-              }
+        if (!test) {
+          // fill from the count pass's ballots
+          for (uint32_t t0 = 0; t0 < m; t0 += 32) {
+            const uint32_t mask = maskp[t0 / 32];
+            if (mask) {
+              if ((mask >> lane) & 1u) a.nbr[S.list_base + cursor + __popc(mask & lt)] = sent[t0 + lane];
+              cursor += __popc(mask);
             }
           }
-          const unsigned mask = __ballot_sync(0xffffffffu, hit);
-          if (FILL) {
-            if (hit) a.nbr[S.list_base + cursor + __popc(mask & lanemask_lt())] = ent;
-            cursor += __popc(mask);
-          } else {
-            cnt += __popc(mask);
+        } else {
+          const float4 paf = a.pf[i];
+          const uint32_t self_ent = ((i - S.part_base) << 5) | static_cast<uint32_t>(kImageCenter);
+          uint32_t cnt = 0;
+          for (uint32_t t0 = 0; t0 < m; t0 += 32) {
+            const uint32_t t = t0 + lane;
+            float4 b = make_float4(0.f, 0.f, 0.f, __uint_as_float(kInvalid));
+            if (t < m) b = srel[t];
+            const uint32_t ent = __float_as_uint(b.w);
+            const bool cand = ent != kInvalid && ent != self_ent;
+            const float dx = paf.x - b.x, dy = paf.y - b.y, dz = paf.z - b.z;
+            const float d2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            bool hit = cand && d2f < nb_lo && d2f > nb_zero && !(ent & kAmbiguousBit);
+            const bool maybe = cand && !hit && d2f <= nb_hi;
+            if (__any_sync(0xffffffffu, maybe)) {
+              if (maybe) hit = exact_neighbor_test(S, a, i, ent);
+            }
+            const unsigned mask = __ballot_sync(0xffffffffu, hit);
+            if (FILL) {
+              if (hit) a.nbr[S.list_base + cursor + __popc(mask & lt)] = ent & ~kAmbiguousBit;
+              cursor += __popc(mask);
+            } else {
+              cnt += __popc(mask);
+              if (use_masks && lane == 0) maskp[t0 / 32] = mask;
+            }
           }
+          if (!FILL && lane == 0) a.nbr_cnt[i] = (c0 == 0 ? 0u : a.nbr_cnt[i]) + cnt;
+          cell_total += cnt;
         }
-        if (lane == 0) {
-          if (FILL) {
-            a.nbr_cursor[i] = cursor;
-          } else {
-            a.nbr_cnt[i] = (c0 == 0 ? 0u : a.nbr_cnt[i]) + cnt;
-          }
-        }
-        cell_total += cnt;
+        if (FILL && lane == 0) a.nbr_cursor[i] = cursor;
       }
       __syncwarp();
     }
@@ -521,6 +563,7 @@ __global__ void __launch_bounds__(128)
 
 // Segment capacity check after the per-cell scan.
 __global__ void k_nbr_check(int nsys, const SysDesc* __restrict__ sys, SysState* st, const DevArrays a) {
+  if (*a.any_rebuild == 0) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsys || !st[s].rebuild) return;
   const SysDesc& S = sys[s];
@@ -537,7 +580,8 @@ constexpr int kScanItems = 8;
 constexpr uint32_t kScanTile = kScanThreads * kScanItems;
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* __restrict__ in, uint32_t n,
-                                                              unsigned long long* sums) {
+                                                              unsigned long long* sums, const unsigned int* gate) {
+  if (gate && *gate == 0) return;
   __shared__ unsigned long long red[kScanThreads / 32];
   const uint32_t base = blockIdx.x * kScanTile;
   unsigned long long v = 0;
@@ -555,7 +599,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* __r
   }
 }
 
-__global__ void __launch_bounds__(1024) k_scan_sums(unsigned long long* sums, uint32_t nb) {
+__global__ void __launch_bounds__(1024) k_scan_sums(unsigned long long* sums, uint32_t nb, const unsigned int* gate) {
+  if (gate && *gate == 0) return;
   __shared__ unsigned long long carry_s;
   __shared__ unsigned long long wsum[32];
   if (threadIdx.x == 0) carry_s = 0;
@@ -591,7 +636,8 @@ __global__ void __launch_bounds__(1024) k_scan_sums(unsigned long long* sums, ui
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_final(const uint32_t* __restrict__ in, uint32_t n,
                                                               const unsigned long long* __restrict__ sums,
-                                                              unsigned long long* out) {
+                                                              unsigned long long* out, const unsigned int* gate) {
+  if (gate && *gate == 0) return;
   __shared__ unsigned long long wsum[kScanThreads / 32];
   const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
   unsigned long long loc[kScanItems];
@@ -639,15 +685,15 @@ inline int thread_grid(uint32_t n, int threads, int sm_count) {
 size_t scan_scratch_elems(uint32_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
 
 int launch_scan_u32_to_u64(const uint32_t* in, unsigned long long* out, uint32_t n, unsigned long long* scratch,
-                           cudaStream_t stream) {
+                           cudaStream_t stream, const unsigned int* gate) {
   if (n == 0) {
     cudaMemsetAsync(out, 0, sizeof(unsigned long long), stream);
     return 0;
   }
   const uint32_t nb = (n + kScanTile - 1) / kScanTile;
-  k_scan_tiles<<<nb, kScanThreads, 0, stream>>>(in, n, scratch);
-  k_scan_sums<<<1, 1024, 0, stream>>>(scratch, nb);
-  k_scan_final<<<nb, kScanThreads, 0, stream>>>(in, n, scratch, out);
+  k_scan_tiles<<<nb, kScanThreads, 0, stream>>>(in, n, scratch, gate);
+  k_scan_sums<<<1, 1024, 0, stream>>>(scratch, nb, gate);
+  k_scan_final<<<nb, kScanThreads, 0, stream>>>(in, n, scratch, out, gate);
   return 3;
 }
 
@@ -657,17 +703,17 @@ int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevAr
   const int wg = warp_grid(ex.n_cells, 4, ex.sm_count);
   k_rebin_compact<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
   k_rebin_count<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
-  const int ns = launch_scan_u32_to_u64(a.cell_cnt, a.cell_scan, ex.n_cells, a.scan_blocks, stream);
+  const int ns = launch_scan_u32_to_u64(a.cell_cnt, a.cell_scan, ex.n_cells, a.scan_blocks, stream, a.any_rebuild);
   k_rebin_scatter<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
   k_rebin_finalize<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
-  k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st);
+  k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild);
   return 6 + ns;
 }
 
 int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream) {
   if (ex.n_part == 0) return 0;
   k_backup<<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
-  k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st);
+  k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild);
   return 2;
 }
 
@@ -675,7 +721,7 @@ int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const D
                      cudaStream_t stream, int mode) {
   if (ex.n_cells == 0) return 0;
   int count = 0;
-  const size_t smem = static_cast<size_t>(4) * cap * (sizeof(float4) + sizeof(uint32_t));
+  const size_t smem = static_cast<size_t>(4) * cap * sizeof(float4);
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_neighbors<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
@@ -685,7 +731,8 @@ int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const D
   const int wg = warp_grid(ex.n_cells, 4, ex.sm_count);
   if (mode & 1) {
     k_neighbors<false><<<wg, 128, smem, stream>>>(ex.n_cells, sys, st, a, cap);
-    count += 2 + launch_scan_u32_to_u64(a.cell_nbr_tot, a.cell_nbr_off, ex.n_cells, a.scan_blocks, stream);
+    count += 2 + launch_scan_u32_to_u64(a.cell_nbr_tot, a.cell_nbr_off, ex.n_cells, a.scan_blocks, stream,
+                                        a.any_rebuild);
     k_nbr_check<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, sys, st, a);
   }
   if (mode & 2) {

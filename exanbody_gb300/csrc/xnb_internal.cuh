@@ -21,6 +21,7 @@
 namespace xnb {
 
 constexpr int kImageCenter = 13;  // image code of the unshifted image: (0+1) + 3*(0+1) + 9*(0+1)
+constexpr uint32_t kMaskWords = 24;  // neighbour-build ballots kept per particle (768 candidates)
 
 enum ErrorBits : uint32_t {
   kErrListOverflow = 1u << 0,   // neighbour list segment too small
@@ -48,6 +49,12 @@ struct SysDesc {
   float nbh2_f, nbh_margin_f;  // FP32 prefilter of the neighbour test and its proven error margin
   float rc2_f, rc_margin_f;    // same for the force cutoff test (mixed path)
   float sig2_f, eps24_f, eps4_f, e_shift_f;
+  // FP32 copies used by the prefilters: positions are kept as float offsets
+  // from the origin (DevArrays::pf); image offsets and ghost-filter bounds in the
+  // same frame; pre_margin_f bounds |d2_f32 - d2_f64| for the force prefilter.
+  float period_f[3];
+  float outer_lo_f[3], outer_hi_f[3];
+  float pre_margin_f, filter_margin_f;
   double m24eps, eps4, sig2, eps24;  // -24*eps, 4*eps (lennard_jones.cu:54-55), sigma^2, 24*eps
   int32_t dims[3];
   int32_t divide_by_mass;
@@ -71,6 +78,8 @@ struct SysState {
 // All device arrays of a batch (pointers into HBM).
 struct DevArrays {
   double *rx, *ry, *rz, *vx, *vy, *vz, *fx, *fy, *fz, *pe;
+  float4* pf;                      // FP32 (x - origin, y - origin, z - origin, 0), refreshed with r
+  unsigned int* any_rebuild;       // number of systems flagged for the rebuild path this step
   uint64_t* id;
   uint32_t* pcell;                 // global cell of each particle
   uint32_t *bkx, *bky, *bkz;       // backup_r u32 encoding (backup_r.h:36-51)
@@ -95,6 +104,7 @@ struct DevArrays {
   uint32_t* nbr_start;             // per particle, relative to its system segment
   uint32_t* nbr_cnt;               // per particle
   uint32_t* nbr_cursor;            // per particle fill cursor (scratch)
+  uint32_t* nbr_masks;             // per particle kMaskWords candidate ballots (scratch)
   uint32_t* nbr;                   // all segments
   // scan scratch
   unsigned long long* scan_blocks;
@@ -142,6 +152,16 @@ __device__ __forceinline__ void cell_ijk(const SysDesc& s, uint32_t local_cell, 
 }
 
 __device__ __forceinline__ int pmod_i(int i, int n) { return ((i % n) + n) % n; }
+
+// FP32 position relative to the system origin, as stored in DevArrays::pf.
+__device__ __forceinline__ float4 make_pf(const SysDesc& s, double x, double y, double z) {
+  return make_float4(static_cast<float>(x - s.origin[0]), static_cast<float>(y - s.origin[1]),
+                     static_cast<float>(z - s.origin[2]), 0.f);
+}
+
+__device__ __forceinline__ float image_coord_f(float x, float period, int d) {
+  return d == 1 ? x : (d == 2 ? x + period : x - period);
+}
 
 // Image offset along one axis for image code digit d in {0,1,2} (-1, 0, +1).
 __device__ __forceinline__ double image_coord(double x, double period, int d) {

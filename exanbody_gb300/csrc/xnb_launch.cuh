@@ -30,7 +30,8 @@ int launch_force(const Extent& ex, const SysDesc* sys, SysState* st, const DevAr
                   bool with_pe, bool second_half, int sys_only, cudaStream_t stream);
 
 // Marks systems for rebuild: all of them (init), or those with moved > 0.
-int launch_mark_rebuild(const Extent& ex, SysState* st, int mode, int sys_only, cudaStream_t stream);
+int launch_mark_rebuild(const Extent& ex, SysState* st, int mode, int sys_only, unsigned int* any,
+                        cudaStream_t stream);
 int launch_clear_moved(const Extent& ex, SysState* st, cudaStream_t stream);
 
 // move_particles + migrate + rebuild_amr + backup_r for systems with rebuild != 0.
@@ -43,8 +44,10 @@ int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const D
                       cudaStream_t stream, int mode);
 
 // Exclusive scan of u32 counts into u64 offsets (n elements; out has n+1 entries).
+// With gate != nullptr the kernels return at once while *gate == 0.
 int launch_scan_u32_to_u64(const uint32_t* in, unsigned long long* out, uint32_t n,
-                            unsigned long long* block_scratch, cudaStream_t stream);
+                           unsigned long long* block_scratch, cudaStream_t stream,
+                           const unsigned int* gate = nullptr);
 size_t scan_scratch_elems(uint32_t n);
 
 

@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(256)
         a.rx[i] = x;
         a.ry[i] = y;
         a.rz[i] = z;
+        a.pf[i] = make_pf(S, x, y, z);
       }
       if (push_v) {
         if (EXACT) {
@@ -94,8 +95,9 @@ __global__ void __launch_bounds__(256)
 }
 
 // ---------------------------------------------------------------------------
-// Fast double-precision reciprocal: FP32 seed refined by two Newton-Raphson
-// steps y <- y + y*(1 - d*y) in FP64 (relative error ~1e-16, not correctly rounded).
+// Double-precision reciprocal from an FP32 seed (relative error <= 2^-23)
+// refined by two Newton-Raphson steps y <- y + y*(1 - d*y) in FP64: the error
+// squares twice (2^-46, then below the FP64 rounding), not correctly rounded.
 __device__ __forceinline__ double rcp_nr(double d) {
   double y = static_cast<double>(__frcp_rn(static_cast<float>(d)));
   double e = fma(-d, y, 1.0);
@@ -137,11 +139,36 @@ __global__ void __launch_bounds__(256)
     const uint32_t pbase = S.part_base;
     const double px = S.period[0], py = S.period[1], pz = S.period[2];
     const double rcut2 = S.rcut2;
+    const float4 paf = a.pf[i];
+    const float pre_hi = S.rc2_f + S.pre_margin_f;
+    const float pfx = S.period_f[0], pfy = S.period_f[1], pfz = S.period_f[2];
     double fx = 0.0, fy = 0.0, fz = 0.0, pe = 0.0;
-    for (uint32_t k = 0; k < n; ++k) {
-      const uint32_t e = __ldg(L + k);
-      const uint32_t j = pbase + (e >> 5);
-      const uint32_t code = e & 31u;
+    uint32_t k = 0;
+    for (;;) {
+      // FP32 prefilter: each lane skips, on its own, the entries provably beyond
+      // rc, so the warp runs the FP64 block below once per in-range entry of
+      // its busiest lane rather than once per list entry.
+      uint32_t j = 0, code = 0;
+      bool found = false;
+      while (k < n) {
+        const uint32_t e = __ldg(L + k);
+        ++k;
+        j = pbase + (e >> 5);
+        code = e & 31u;
+        const float4 pbf = __ldg(a.pf + j);
+        float bx = pbf.x, by = pbf.y, bz = pbf.z;
+        if (code != static_cast<uint32_t>(kImageCenter)) {
+          bx = image_coord_f(bx, pfx, static_cast<int>(code % 3u));
+          by = image_coord_f(by, pfy, static_cast<int>((code / 3u) % 3u));
+          bz = image_coord_f(bz, pfz, static_cast<int>(code / 9u));
+        }
+        const float ex = bx - paf.x, ey = by - paf.y, ez = bz - paf.z;
+        if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= pre_hi) {
+          found = true;
+          break;
+        }
+      }
+      if (!found) break;
       double xb = __ldg(a.rx + j), yb = __ldg(a.ry + j), zb = __ldg(a.rz + j);
       if (code != static_cast<uint32_t>(kImageCenter)) {
         xb = image_coord(xb, px, static_cast<int>(code % 3u));
@@ -238,7 +265,7 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-__global__ void k_mark_rebuild(int nsys, SysState* st, int mode, int sys_only) {
+__global__ void k_mark_rebuild(int nsys, SysState* st, int mode, int sys_only, unsigned int* any) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsys) return;
   if (sys_only >= 0 && s != sys_only) {
@@ -248,7 +275,10 @@ __global__ void k_mark_rebuild(int nsys, SysState* st, int mode, int sys_only) {
   // mode 0: every system (init); mode 1: systems whose trigger fired; mode 2: none
   const uint32_t r = mode == 0 ? 1u : (mode == 1 ? (st[s].moved > 0 ? 1u : 0u) : 0u);
   st[s].rebuild = r;
-  if (r) st[s].rebuilds += 1;
+  if (r) {
+    st[s].rebuilds += 1;
+    atomicAdd(any, 1u);
+  }
 }
 
 __global__ void k_clear_moved(int nsys, SysState* st) {
@@ -306,9 +336,11 @@ int launch_force(const Extent& ex, const SysDesc* sys, SysState* st, const DevAr
   return 0;
 }
 
-int launch_mark_rebuild(const Extent& ex, SysState* st, int mode, int sys_only, cudaStream_t stream) {
+int launch_mark_rebuild(const Extent& ex, SysState* st, int mode, int sys_only, unsigned int* any,
+                        cudaStream_t stream) {
+  cudaMemsetAsync(any, 0, sizeof(unsigned int), stream);
   if (ex.nsys == 0) return 0;
-  k_mark_rebuild<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, mode, sys_only);
+  k_mark_rebuild<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, mode, sys_only, any);
   return 1;
 }
 
