@@ -232,10 +232,11 @@ SysDesc make_desc(const xnb_lj_params& p) {
   }
   // ghost filter compare: coordinate error 2 (X + P) u, bound conversion (X + nbh) u
   d.filter_margin_f = static_cast<float>(4.0 * (2.0 * (X + P) + X + nbh) * u * 1.01);
-  //  force cutoff test of the mixed path: d_f32 = fl32(d_f64) per axis,
-  //  |r2_f32 - d2_f64| <= 5.1 u d2; margin = 4x at rc^2 (+1 absolute guard so tiny d2 also go to FP64).
+  //  force cutoff test of the mixed path: each FP32 axis difference is within
+  //  2u|d| of the FP64 one (converted, or compensated hi/lo), so
+  //  |r2_f32 - d2_f64| <= 6 u d2; margin = 4x at rc^2 (+1 absolute guard so tiny d2 also go to FP64).
   d.rc2_f = static_cast<float>(d.rcut2);
-  d.rc_margin_f = static_cast<float>(4.0 * 5.1 * u * (d.rcut2 + 1.0));
+  d.rc_margin_f = static_cast<float>(4.0 * 6.0 * u * (d.rcut2 + 1.0));
   return d;
 }
 
@@ -324,7 +325,7 @@ const char* xnb_last_error_string(void) { return g_err.c_str(); }
 int xnb_version(void) { return 10000; }
 
 int64_t xnb_system_bytes(int64_t n, int64_t ncells, double list_per_particle) {
-  const int64_t per_part = 8 * 10 + 8 + 4 + 12 + 24 + 8 * 9 + 8 + 4 * 3 + 4 * 3 + 16 + 4 * kMaskWords;
+  const int64_t per_part = 8 * 10 + 8 + 4 + 12 + 24 + 8 * 9 + 8 + 4 * 3 + 4 * 3 + 32 + 4 * kMaskWords;
   const int64_t per_cell = 4 * 7 + 8 * 2 + 4;
   return n * per_part + ncells * per_cell + static_cast<int64_t>(static_cast<double>(n) * list_per_particle) * 4;
 }
@@ -352,6 +353,7 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   for (double** p : dbl) rc = rc ? rc : dalloc(b, p, P);
   rc = rc ? rc : dalloc(b, &a.id, P);
   rc = rc ? rc : dalloc(b, &a.pf, P);
+  rc = rc ? rc : dalloc(b, &a.pflo, P);
   rc = rc ? rc : dalloc(b, &a.nbr_masks, P * kMaskWords);
   rc = rc ? rc : dalloc(b, &a.any_rebuild, 4);
   rc = rc ? rc : dalloc(b, &a.t_id, P);
@@ -489,11 +491,16 @@ int xnb_system_add(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double
   if (nb) {
     XCK(cudaMemcpyAsync(a.id + poff, hid.data(), nb * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     XCK(cudaMemcpyAsync(a.pcell + poff, hcell.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    std::vector<float4> hpf(nb);
-    for (size_t q = 0; q < nb; ++q)
-      hpf[q] = make_float4(static_cast<float>(h[0][q] - p->origin[0]), static_cast<float>(h[1][q] - p->origin[1]),
-                           static_cast<float>(h[2][q] - p->origin[2]), 0.f);
+    std::vector<float4> hpf(nb), hlo(nb);
+    for (size_t q = 0; q < nb; ++q) {
+      const double r0 = h[0][q] - p->origin[0], r1 = h[1][q] - p->origin[1], r2 = h[2][q] - p->origin[2];
+      hpf[q] = make_float4(static_cast<float>(r0), static_cast<float>(r1), static_cast<float>(r2), 0.f);
+      hlo[q] = make_float4(static_cast<float>(r0 - static_cast<double>(hpf[q].x)),
+                           static_cast<float>(r1 - static_cast<double>(hpf[q].y)),
+                           static_cast<float>(r2 - static_cast<double>(hpf[q].z)), 0.f);
+    }
     XCK(cudaMemcpyAsync(a.pf + poff, hpf.data(), nb * sizeof(float4), cudaMemcpyHostToDevice, st));
+    XCK(cudaMemcpyAsync(a.pflo + poff, hlo.data(), nb * sizeof(float4), cudaMemcpyHostToDevice, st));
     XCK(cudaMemsetAsync(a.fx + poff, 0, nb * sizeof(double), st));
     XCK(cudaMemsetAsync(a.fy + poff, 0, nb * sizeof(double), st));
     XCK(cudaMemsetAsync(a.fz + poff, 0, nb * sizeof(double), st));

@@ -268,6 +268,7 @@ __global__ void __launch_bounds__(128)
     cell_ijk(S, c - S.cell_base, ci, cj, ck);
     const double lo[3] = {cell_lo(S, 0, ci), cell_lo(S, 1, cj), cell_lo(S, 2, ck)};
     const int side = S.amr_enabled ? sub_grid_side(n, S.sub_grid_density) : 1;
+    // backup_r runs afterwards in k_backup, one thread per particle
     if (side > 1) {
       // sub-cell key of each particle (Grid::particle_pcoord, grid.h:184-190), kept in pdest
       for (uint32_t q = lane; q < n; q += 32) {
@@ -303,15 +304,11 @@ __global__ void __launch_bounds__(128)
       a.vx[dst] = a.t_vx[src]; a.vy[dst] = a.t_vy[src]; a.vz[dst] = a.t_vz[src];
       a.fx[dst] = a.t_fx[src]; a.fy[dst] = a.t_fy[src]; a.fz[dst] = a.t_fz[src];
       a.id[dst] = a.t_id[src];
-      a.pf[dst] = make_pf(S, x, y, z);
+      float4 mhi, mlo;
+      make_pf2(S, x, y, z, mhi, mlo);
+      a.pf[dst] = mhi;
+      a.pflo[dst] = mlo;
       a.pcell[dst] = c;
-      const uint32_t bx = encode_u32(x, lo[0], S.cell_size);
-      const uint32_t by = encode_u32(y, lo[1], S.cell_size);
-      const uint32_t bz = encode_u32(z, lo[2], S.cell_size);
-      a.bkx[dst] = bx; a.bky[dst] = by; a.bkz[dst] = bz;
-      a.rbx[dst] = restore_u32(bx, lo[0], S.cell_size);
-      a.rby[dst] = restore_u32(by, lo[1], S.cell_size);
-      a.rbz[dst] = restore_u32(bz, lo[2], S.cell_size);
     }
     if (lane == 0) {
       a.cell_start[c] = ns;
@@ -516,9 +513,12 @@ __global__ void __launch_bounds__(128)
         uint32_t cursor = 0;
         if (FILL) cursor = a.nbr_cursor[i];
         if (!test) {
-          // fill from the count pass's ballots
+          // fill from the count pass's ballots: the particle's mask words arrive in one
+          // coalesced load (lane w holds word w) and are broadcast by shuffles
+          const uint32_t nsub = (m + 31) / 32;
+          const uint32_t mine = lane < nsub ? __ldg(maskp + lane) : 0u;
           for (uint32_t t0 = 0; t0 < m; t0 += 32) {
-            const uint32_t mask = maskp[t0 / 32];
+            const uint32_t mask = __shfl_sync(0xffffffffu, mine, t0 / 32);
             if (mask) {
               if ((mask >> lane) & 1u) a.nbr[S.list_base + cursor + __popc(mask & lt)] = sent[t0 + lane];
               cursor += __popc(mask);
@@ -706,8 +706,9 @@ int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevAr
   const int ns = launch_scan_u32_to_u64(a.cell_cnt, a.cell_scan, ex.n_cells, a.scan_blocks, stream, a.any_rebuild);
   k_rebin_scatter<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
   k_rebin_finalize<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
+  k_backup<<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
   k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild);
-  return 6 + ns;
+  return 7 + ns;
 }
 
 int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream) {

@@ -78,7 +78,8 @@ struct SysState {
 // All device arrays of a batch (pointers into HBM).
 struct DevArrays {
   double *rx, *ry, *rz, *vx, *vy, *vz, *fx, *fy, *fz, *pe;
-  float4* pf;                      // FP32 (x - origin, y - origin, z - origin, 0), refreshed with r
+  float4* pf;                      // FP32 hi part of (x - origin, y - origin, z - origin), refreshed with r
+  float4* pflo;                    // FP32 residual (x - origin) - hi, so hi + lo carries ~48 bits
   unsigned int* any_rebuild;       // number of systems flagged for the rebuild path this step
   uint64_t* id;
   uint32_t* pcell;                 // global cell of each particle
@@ -153,10 +154,17 @@ __device__ __forceinline__ void cell_ijk(const SysDesc& s, uint32_t local_cell, 
 
 __device__ __forceinline__ int pmod_i(int i, int n) { return ((i % n) + n) % n; }
 
-// FP32 position relative to the system origin, as stored in DevArrays::pf.
+// FP32 position relative to the system origin, as stored in DevArrays::pf, and
+// its residual (DevArrays::pflo): hi = fl32(x - o), lo = fl32((x - o) - hi).
 __device__ __forceinline__ float4 make_pf(const SysDesc& s, double x, double y, double z) {
   return make_float4(static_cast<float>(x - s.origin[0]), static_cast<float>(y - s.origin[1]),
                      static_cast<float>(z - s.origin[2]), 0.f);
+}
+__device__ __forceinline__ void make_pf2(const SysDesc& s, double x, double y, double z, float4& hi, float4& lo) {
+  const double rx = x - s.origin[0], ry = y - s.origin[1], rz = z - s.origin[2];
+  hi = make_float4(static_cast<float>(rx), static_cast<float>(ry), static_cast<float>(rz), 0.f);
+  lo = make_float4(static_cast<float>(rx - static_cast<double>(hi.x)), static_cast<float>(ry - static_cast<double>(hi.y)),
+                   static_cast<float>(rz - static_cast<double>(hi.z)), 0.f);
 }
 
 __device__ __forceinline__ float image_coord_f(float x, float period, int d) {

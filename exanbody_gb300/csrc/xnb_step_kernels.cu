@@ -59,7 +59,10 @@ __global__ void __launch_bounds__(256)
         a.rx[i] = x;
         a.ry[i] = y;
         a.rz[i] = z;
-        a.pf[i] = make_pf(S, x, y, z);
+        float4 hi, lo;
+        make_pf2(S, x, y, z, hi, lo);
+        a.pf[i] = hi;
+        a.pflo[i] = lo;
       }
       if (push_v) {
         if (EXACT) {
@@ -140,6 +143,7 @@ __global__ void __launch_bounds__(256)
     const double px = S.period[0], py = S.period[1], pz = S.period[2];
     const double rcut2 = S.rcut2;
     const float4 paf = a.pf[i];
+    const float4 pal = (P == kMixed) ? a.pflo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float pre_hi = S.rc2_f + S.pre_margin_f;
     const float pfx = S.period_f[0], pfy = S.period_f[1], pfz = S.period_f[2];
     double fx = 0.0, fy = 0.0, fz = 0.0, pe = 0.0;
@@ -175,10 +179,10 @@ __global__ void __launch_bounds__(256)
         yb = image_coord(yb, py, static_cast<int>((code / 3u) % 3u));
         zb = image_coord(zb, pz, static_cast<int>(code / 9u));
       }
-      const double dx = __dsub_rn(xb, xa);
-      const double dy = __dsub_rn(yb, ya);
-      const double dz = __dsub_rn(zb, za);
       if (P == kFp64Exact) {
+        const double dx = __dsub_rn(xb, xa);
+        const double dy = __dsub_rn(yb, ya);
+        const double dz = __dsub_rn(zb, za);
         const double d2 = norm2_rn(dx, dy, dz);
         if (d2 > 0.0 && d2 <= rcut2) {
           // lj_compute_energy (lennard_jones.cu:46-56) then pair_de *= w / r with w = 1
@@ -199,6 +203,9 @@ __global__ void __launch_bounds__(256)
           }
         }
       } else if (P == kFp64) {
+        const double dx = __dsub_rn(xb, xa);
+        const double dy = __dsub_rn(yb, ya);
+        const double dz = __dsub_rn(zb, za);
         const double d2 = norm2_rn(dx, dy, dz);
         if (d2 > 0.0 && d2 <= rcut2) {
           const double ir2 = rcp_nr(d2);
@@ -211,7 +218,21 @@ __global__ void __launch_bounds__(256)
           if (PE) pe += 0.5 * fma(S.eps4 * s6, s6 - 1.0, -S.e_shift);
         }
       } else {
-        const float dxf = static_cast<float>(dx), dyf = static_cast<float>(dy), dzf = static_cast<float>(dz);
+        // r^2 in FP32. For an entry in the same periodic image, the compensated
+        // difference (hi_b - hi_a) + (lo_b - lo_a) of the FP32 hi/lo mirrors is
+        // within 2u|d| of the FP64 displacement (u = 2^-24), as close as
+        // converting it, without FP64 work; image entries convert the FP64 one.
+        float dxf, dyf, dzf;
+        if (code == static_cast<uint32_t>(kImageCenter)) {
+          const float4 hb = __ldg(a.pf + j), lb = __ldg(a.pflo + j);
+          dxf = (hb.x - paf.x) + (lb.x - pal.x);
+          dyf = (hb.y - paf.y) + (lb.y - pal.y);
+          dzf = (hb.z - paf.z) + (lb.z - pal.z);
+        } else {
+          dxf = static_cast<float>(__dsub_rn(xb, xa));
+          dyf = static_cast<float>(__dsub_rn(yb, ya));
+          dzf = static_cast<float>(__dsub_rn(zb, za));
+        }
         const float r2 = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
         bool in;
         if (r2 > S.rc2_f + S.rc_margin_f) {
@@ -219,10 +240,14 @@ __global__ void __launch_bounds__(256)
         } else if (r2 < S.rc2_f - S.rc_margin_f && r2 > S.rc_margin_f) {
           in = true;
         } else {
-          const double d2 = norm2_rn(dx, dy, dz);
+          const double d2 = norm2_rn(__dsub_rn(xb, xa), __dsub_rn(yb, ya), __dsub_rn(zb, za));
           in = (d2 > 0.0 && d2 <= rcut2);
         }
         if (in) {
+          // the force vector uses the FP64 displacement
+          const double dx = __dsub_rn(xb, xa);
+          const double dy = __dsub_rn(yb, ya);
+          const double dz = __dsub_rn(zb, za);
           const float ir2 = __frcp_rn(r2);
           const float s2 = S.sig2_f * ir2;
           const float s6 = s2 * s2 * s2;
