@@ -4,7 +4,9 @@ Workload (default): periodic FCC 100^3 = 4,000,000 atoms, rho* = 0.8442,
 T* = 1.44, truncated-and-shifted LJ rc = 2.5, skin 0.3, dt = 0.005; one bench
 "step" is one velocity-Verlet MD step (push, trigger, conditional rebin +
 neighbour rebuild, forces, push) of the whole system, in the mixed precision
-path. The state (~2.4 GB) is larger than L2 (129 MB), so no flush is needed.
+path with Newton half lists (each pair evaluated once, reactions by FP64
+reductions); the plain FP64 path is timed with the same traversal, and both
+full-list (bitwise reproducible) traversals are reported beside them. The state (~2.4 GB) is larger than L2 (129 MB), so no flush is needed.
 
 Reported on one JSON line: mixed-path atom-steps/s with inputs resident in
 HBM (`value`), the plain FP64 path beside it, the force error of the mixed
@@ -246,34 +248,45 @@ def run_ours(args):
             ms = float(t.item())
         return ms
 
-    # ---- mixed path, resident state ----
+    MIXED = xnb.PREC_MIXED | xnb.PREC_NEWTON
+    FP64 = xnb.PREC_FP64 | xnb.PREC_NEWTON
+
+    # ---- mixed path (Newton half lists), resident state ----
     b = new_batch()
     s = b.add_system(params, w["r"], w["v"], w["id"], list_factor=1.2)
-    b.init_particles(s, xnb.PREC_MIXED)
-    b.step(max(3, args.warmup), xnb.PREC_MIXED, 0)
+    b.init_particles(s, MIXED)
+    b.step(max(3, args.warmup), MIXED, 0)
     b.check_errors()
     reb0 = b.info(s).rebuilds
     l0 = b.kernel_launches()
     with Clocks(local) as ck:
-        ms = timed(lambda: b.step(args.steps, xnb.PREC_MIXED, 0))
+        ms = timed(lambda: b.step(args.steps, MIXED, 0))
     clocks = ck.summary()
     launches = b.kernel_launches() - l0
     b.check_errors()
     rebuilds = b.info(s).rebuilds - reb0
     value = world * N * args.steps / (ms * 1e-3)
 
-    # ---- plain FP64 path from the same state ----
+    # ---- plain FP64 path (same traversal) from the same state ----
     k64 = max(5, min(args.steps, 40))
-    b.step(2, xnb.PREC_FP64, 0)
-    ms64 = timed(lambda: b.step(k64, xnb.PREC_FP64, 0))
+    b.step(2, FP64, 0)
+    ms64 = timed(lambda: b.step(k64, FP64, 0))
     b.check_errors()
     value64 = N * k64 / (ms64 * 1e-3)
+
+    # ---- deterministic full-list traversals (each pair from both sides) ----
+    full = {}
+    for name, prec in (("mixed", xnb.PREC_MIXED), ("fp64", xnb.PREC_FP64)):
+        b.step(2, prec, 0)
+        msf = timed(lambda: b.step(k64, prec, 0))
+        full[name] = N * k64 / (msf * 1e-3)
+    b.check_errors()
 
     # ---- force error of the mixed path against FP64 on one state ----
     b.lennard_jones_force(s, xnb.PREC_FP64, False)
     P = b.download(s)
     f64 = np.stack([P["fx"], P["fy"], P["fz"]], 1)
-    b.lennard_jones_force(s, xnb.PREC_MIXED, False)
+    b.lennard_jones_force(s, MIXED, False)
     P = b.download(s)
     fmx = np.stack([P["fx"], P["fy"], P["fz"]], 1)
     d = np.linalg.norm(fmx - f64, axis=1)
@@ -284,8 +297,8 @@ def run_ours(args):
 
     # ---- dominant kernel timing (force traversal alone, same launch as in the step) ----
     reps = 10
-    ms_force = timed(lambda: b.lennard_jones_force(s, xnb.PREC_MIXED, False), reps) / reps
-    ms_force64 = timed(lambda: b.lennard_jones_force(s, xnb.PREC_FP64, False), 3) / 3
+    ms_force = timed(lambda: b.lennard_jones_force(s, MIXED, False), reps) / reps
+    ms_force64 = timed(lambda: b.lennard_jones_force(s, FP64, False), 3) / 3
     peak64 = fp64_peak_tflops(torch, dev)
     achieved = FLOP64_PER_ATOM_MIXED * N / (ms_force * 1e-3) / 1e12
     b.close()
@@ -298,8 +311,8 @@ def run_ours(args):
         def e2e_run():
             bb = new_batch()
             ss = bb.add_system(params, w["r"], w["v"], w["id"], list_factor=1.2)
-            bb.init_particles(ss, xnb.PREC_MIXED)
-            bb.step(args.steps, xnb.PREC_MIXED, 0)
+            bb.init_particles(ss, MIXED)
+            bb.step(args.steps, MIXED, 0)
             got = bb.download(ss)
             bb.check_errors()
             bb.close()
@@ -351,11 +364,14 @@ def run_ours(args):
                                 precision="mixed", rebuilds_in_timed_steps=rebuilds),
             "fp64": {"value": value64, "unit": "atom-steps/s", "steps": k64,
                      "speedup_mixed_vs_fp64": value / world / value64},
+            "full_list_deterministic": {"mixed": full["mixed"], "fp64": full["fp64"], "unit": "atom-steps/s",
+                                        "note": "each pair evaluated from both sides, bitwise reproducible"},
             "force_error_mixed_vs_fp64": {"max": err_max, "rms": err_rms, "tolerance": 1e-5},
             "clocks": clocks,
             "e2e": e2e,
             "gpu_launches": launches,
-            "roofline": {"bound": "fp64", "kernel": "k_force<mixed>", "achieved": achieved, "peak": peak64,
+            "roofline": {"bound": "fp64", "kernel": "k_force_half<mixed> (+ zero/finish launches)",
+                         "achieved": achieved, "peak": peak64,
                          "unit": "TFLOP/s", "frac": achieved / peak64,
                          "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
                          "ms_per_launch": ms_force, "ms_per_launch_fp64_kernel": ms_force64,

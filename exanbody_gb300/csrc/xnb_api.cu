@@ -311,6 +311,17 @@ int clear_rebuild(xnb_batch* b, cudaStream_t st) {
   return XNB_OK;
 }
 
+// precision argument: base precision in the low bits, XNB_PREC_NEWTON as a flag
+int decode_precision(int32_t precision, int* base, bool* newton) {
+  *base = precision & 0xF;
+  *newton = (precision & XNB_PREC_NEWTON) != 0;
+  if (*base < 0 || *base > 2 || (precision & ~(0xF | XNB_PREC_NEWTON)))
+    return fail(XNB_ERR_ARG, "bad precision");
+  if (*newton && *base == XNB_PREC_FP64_EXACT)
+    return fail(XNB_ERR_ARG, "the Newton half-list traversal is not bit-exact: use it with FP64 or MIXED");
+  return XNB_OK;
+}
+
 int check_launch() {
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(XNB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
@@ -354,6 +365,7 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   rc = rc ? rc : dalloc(b, &a.id, P);
   rc = rc ? rc : dalloc(b, &a.pf, P);
   rc = rc ? rc : dalloc(b, &a.pflo, P);
+  rc = rc ? rc : dalloc(b, &a.nbr_half, P);
   rc = rc ? rc : dalloc(b, &a.nbr_masks, P * kMaskWords);
   rc = rc ? rc : dalloc(b, &a.any_rebuild, 4);
   rc = rc ? rc : dalloc(b, &a.t_id, P);
@@ -648,7 +660,11 @@ int xnb_system_energy(xnb_batch* b, int32_t s, double* ke, double* pe, void* str
 int xnb_init_particles(xnb_batch* b, int32_t s, int32_t precision, void* stream) {
   int rc = check_sys(b, s);
   if (rc) return rc;
-  if (precision < 0 || precision > 2) return fail(XNB_ERR_ARG, "bad precision");
+  int base = 0;
+  bool newton = false;
+  rc = decode_precision(precision, &base, &newton);
+  if (rc) return rc;
+  precision = base;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   XCK(cudaSetDevice(b->device));
   const Extent ex = b->extent();
@@ -657,7 +673,7 @@ int xnb_init_particles(xnb_batch* b, int32_t s, int32_t precision, void* stream)
   b->launches += launch_rebin(ex, b->d_sys, b->d_st, b->a, st);
   rc = neighbors_sync(b, st);
   if (rc) return rc;
-  b->launches += launch_force(ex, b->d_sys, b->d_st, b->a, precision, true, false, s, st);
+  b->launches += launch_force(ex, b->d_sys, b->d_st, b->a, precision, true, false, s, st, newton);
   rc = pull_states(b, st);
   if (rc) return rc;
   for (int q = 0; q < ex.nsys; ++q) {
@@ -750,9 +766,13 @@ int xnb_backup_r(xnb_batch* b, int32_t s, void* stream) {
 int xnb_lennard_jones_force(xnb_batch* b, int32_t s, int32_t precision, int32_t with_energy, void* stream) {
   int rc = check_sys(b, s);
   if (rc) return rc;
-  if (precision < 0 || precision > 2) return fail(XNB_ERR_ARG, "bad precision");
+  int base = 0;
+  bool newton = false;
+  rc = decode_precision(precision, &base, &newton);
+  if (rc) return rc;
   const Extent ex = b->extent();
-  b->launches += launch_force(ex, b->d_sys, b->d_st, b->a, precision, with_energy != 0, false, s, static_cast<cudaStream_t>(stream));
+  b->launches += launch_force(ex, b->d_sys, b->d_st, b->a, base, with_energy != 0, false, s,
+                              static_cast<cudaStream_t>(stream), newton);
   return check_launch();
 }
 
@@ -760,7 +780,11 @@ int xnb_ghost_update_r(xnb_batch* b, int32_t s, void*) { return check_sys(b, s);
 
 int xnb_step(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, void* stream) {
   if (!b) return fail(XNB_ERR_ARG, "null batch");
-  if (precision < 0 || precision > 2) return fail(XNB_ERR_ARG, "bad precision");
+  int base = 0;
+  bool newton = false;
+  int rc0 = decode_precision(precision, &base, &newton);
+  if (rc0) return rc0;
+  precision = base;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const Extent ex = b->extent();
   const bool exact = precision == XNB_PREC_FP64_EXACT;
@@ -788,7 +812,7 @@ int xnb_step(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, voi
       }
     }
     // compute_all_forces_energy + verlet_second_half
-    b->launches += launch_force(ex, b->d_sys, b->d_st, b->a, precision, energy, true, -1, st);
+    b->launches += launch_force(ex, b->d_sys, b->d_st, b->a, precision, energy, true, -1, st, newton);
     b->launches += launch_clear_moved(ex, b->d_st, st);
   }
   return check_launch();

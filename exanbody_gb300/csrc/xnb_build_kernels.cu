@@ -478,6 +478,8 @@ __global__ void __launch_bounds__(128)
     const uint32_t ncand = __shfl_sync(0xffffffffu, g_off, 26);
     g_off -= g_n;
     const bool use_masks = ncand <= kMaskWords * 32u;
+    // candidates before cell a's own group come first (groups g < 13), then cell a
+    const uint32_t off_self = __shfl_sync(0xffffffffu, g_off, 13);
 
     const float nb_hi = S.nbh2_f + S.nbh_margin_f;
     const float nb_lo = S.nbh2_f - S.nbh_margin_f;
@@ -512,6 +514,9 @@ __global__ void __launch_bounds__(128)
         uint32_t* maskp = a.nbr_masks + static_cast<size_t>(i) * kMaskWords + c0 / 32;
         uint32_t cursor = 0;
         if (FILL) cursor = a.nbr_cursor[i];
+        // entries taken before candidate index lower_end form the lower half
+        const uint32_t lower_end = off_self + pa;
+        uint32_t half = 0;
         if (!test) {
           // fill from the count pass's ballots: the particle's mask words arrive in one
           // coalesced load (lane w holds word w) and are broadcast by shuffles
@@ -522,6 +527,9 @@ __global__ void __launch_bounds__(128)
             if (mask) {
               if ((mask >> lane) & 1u) a.nbr[S.list_base + cursor + __popc(mask & lt)] = sent[t0 + lane];
               cursor += __popc(mask);
+              const uint32_t gbase = c0 + t0;
+              if (gbase < lower_end)
+                half += __popc(lower_end - gbase >= 32u ? mask : (mask & ((1u << (lower_end - gbase)) - 1u)));
             }
           }
         } else {
@@ -545,6 +553,9 @@ __global__ void __launch_bounds__(128)
             if (FILL) {
               if (hit) a.nbr[S.list_base + cursor + __popc(mask & lt)] = ent & ~kAmbiguousBit;
               cursor += __popc(mask);
+              const uint32_t gbase = c0 + t0;
+              if (gbase < lower_end)
+                half += __popc(lower_end - gbase >= 32u ? mask : (mask & ((1u << (lower_end - gbase)) - 1u)));
             } else {
               cnt += __popc(mask);
               if (use_masks && lane == 0) maskp[t0 / 32] = mask;
@@ -553,7 +564,10 @@ __global__ void __launch_bounds__(128)
           if (!FILL && lane == 0) a.nbr_cnt[i] = (c0 == 0 ? 0u : a.nbr_cnt[i]) + cnt;
           cell_total += cnt;
         }
-        if (FILL && lane == 0) a.nbr_cursor[i] = cursor;
+        if (FILL && lane == 0) {
+          a.nbr_cursor[i] = cursor;
+          a.nbr_half[i] = (c0 == 0 ? 0u : a.nbr_half[i]) + half;
+        }
       }
       __syncwarp();
     }

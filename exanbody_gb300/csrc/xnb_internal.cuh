@@ -106,6 +106,8 @@ struct DevArrays {
   uint32_t* nbr_cnt;               // per particle
   uint32_t* nbr_cursor;            // per particle fill cursor (scratch)
   uint32_t* nbr_masks;             // per particle kMaskWords candidate ballots (scratch)
+  uint32_t* nbr_half;              // per particle: entries before it in the reference order
+                                   // ((cell_b, p_b) < (cell_a, p_a)), the Newton half list
   uint32_t* nbr;                   // all segments
   // scan scratch
   unsigned long long* scan_blocks;

@@ -26,8 +26,10 @@ int launch_first_half(const Extent& ex, const SysDesc* sys, SysState* st, const 
 
 // zero_particle_force + lennard_jones_force (+ divide_force_by_type_scalar when the
 // system asks for it), optionally fused with the second-half kick push_f_v(0.5).
+// newton: FP64 / mixed paths walk the lower half of each list and deliver
+// reactions with FP64 reductions (three kernels: zero, traverse, finish).
 int launch_force(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int precision,
-                  bool with_pe, bool second_half, int sys_only, cudaStream_t stream);
+                 bool with_pe, bool second_half, int sys_only, cudaStream_t stream, bool newton = false);
 
 // Marks systems for rebuild: all of them (init), or those with moved > 0.
 int launch_mark_rebuild(const Extent& ex, SysState* st, int mode, int sys_only, unsigned int* any,

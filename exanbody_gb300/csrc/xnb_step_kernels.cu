@@ -290,6 +290,175 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Newton-third-law form of the same traversal for the FP64 and mixed paths:
+// particle a walks only the lower half of its sorted list ((cell_b, p_b) <
+// (cell_a, p_a), the reference's symmetric split, compute_cell_particle_pairs_
+// impl_default.h:181), keeps f_a in registers and hands -f_pair to b with an FP64
+// reduction in L2. Each pair inside rc is evaluated once. The order in which
+// reactions arrive varies from run to run, so results agree to rounding, not
+// bit for bit; FP64_EXACT always uses the full-list kernel above.
+template <int P, bool PE>
+__global__ void __launch_bounds__(256)
+    k_force_half(uint32_t n_part, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a,
+                 int sys_only) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
+    const uint32_t c = a.pcell[i];
+    if (c == kInvalid) continue;
+    const uint32_t s = a.cell_sys[c];
+    if (sys_only >= 0 && s != static_cast<uint32_t>(sys_only)) continue;
+    if (st[s].error) continue;
+    const SysDesc& S = sys[s];
+    const double xa = a.rx[i], ya = a.ry[i], za = a.rz[i];
+    const uint32_t* __restrict__ L = a.nbr + S.list_base + a.nbr_start[i];
+    const uint32_t n = a.nbr_half[i];
+    const uint32_t pbase = S.part_base;
+    const double px = S.period[0], py = S.period[1], pz = S.period[2];
+    const double rcut2 = S.rcut2;
+    const float4 paf = a.pf[i];
+    const float4 pal = (P == kMixed) ? a.pflo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float pre_hi = S.rc2_f + S.pre_margin_f;
+    const float pfx = S.period_f[0], pfy = S.period_f[1], pfz = S.period_f[2];
+    double fx = 0.0, fy = 0.0, fz = 0.0, pe = 0.0;
+    uint32_t k = 0;
+    for (;;) {
+      uint32_t j = 0, code = 0;
+      bool found = false;
+      while (k < n) {
+        const uint32_t e = __ldg(L + k);
+        ++k;
+        j = pbase + (e >> 5);
+        code = e & 31u;
+        const float4 pbf = __ldg(a.pf + j);
+        float bx = pbf.x, by = pbf.y, bz = pbf.z;
+        if (code != static_cast<uint32_t>(kImageCenter)) {
+          bx = image_coord_f(bx, pfx, static_cast<int>(code % 3u));
+          by = image_coord_f(by, pfy, static_cast<int>((code / 3u) % 3u));
+          bz = image_coord_f(bz, pfz, static_cast<int>(code / 9u));
+        }
+        const float ex = bx - paf.x, ey = by - paf.y, ez = bz - paf.z;
+        if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= pre_hi) {
+          found = true;
+          break;
+        }
+      }
+      if (!found) break;
+      double xb = __ldg(a.rx + j), yb = __ldg(a.ry + j), zb = __ldg(a.rz + j);
+      if (code != static_cast<uint32_t>(kImageCenter)) {
+        xb = image_coord(xb, px, static_cast<int>(code % 3u));
+        yb = image_coord(yb, py, static_cast<int>((code / 3u) % 3u));
+        zb = image_coord(zb, pz, static_cast<int>(code / 9u));
+      }
+      bool in;
+      double pd = 0.0, en = 0.0;
+      if (P == kFp64) {
+        const double d2 = norm2_rn(__dsub_rn(xb, xa), __dsub_rn(yb, ya), __dsub_rn(zb, za));
+        in = d2 > 0.0 && d2 <= rcut2;
+        if (in) {
+          const double ir2 = rcp_nr(d2);
+          const double s2 = S.sig2 * ir2;
+          const double s6 = s2 * s2 * s2;
+          pd = S.eps24 * s6 * fma(-2.0, s6, 1.0) * ir2;
+          if (PE) en = fma(S.eps4 * s6, s6 - 1.0, -S.e_shift);
+        }
+      } else {
+        float dxf, dyf, dzf;
+        if (code == static_cast<uint32_t>(kImageCenter)) {
+          const float4 hb = __ldg(a.pf + j), lb = __ldg(a.pflo + j);
+          dxf = (hb.x - paf.x) + (lb.x - pal.x);
+          dyf = (hb.y - paf.y) + (lb.y - pal.y);
+          dzf = (hb.z - paf.z) + (lb.z - pal.z);
+        } else {
+          dxf = static_cast<float>(__dsub_rn(xb, xa));
+          dyf = static_cast<float>(__dsub_rn(yb, ya));
+          dzf = static_cast<float>(__dsub_rn(zb, za));
+        }
+        const float r2 = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
+        if (r2 > S.rc2_f + S.rc_margin_f) {
+          in = false;
+        } else if (r2 < S.rc2_f - S.rc_margin_f && r2 > S.rc_margin_f) {
+          in = true;
+        } else {
+          const double d2 = norm2_rn(__dsub_rn(xb, xa), __dsub_rn(yb, ya), __dsub_rn(zb, za));
+          in = (d2 > 0.0 && d2 <= rcut2);
+        }
+        if (in) {
+          const float ir2 = __frcp_rn(r2);
+          const float s2 = S.sig2_f * ir2;
+          const float s6 = s2 * s2 * s2;
+          pd = static_cast<double>(S.eps24_f * s6 * fmaf(-2.0f, s6, 1.0f) * ir2);
+          if (PE) en = static_cast<double>(fmaf(S.eps4_f * s6, s6 - 1.0f, -S.e_shift_f));
+        }
+      }
+      if (in) {
+        // FP64 displacement and FP64 pair force; a keeps +f, b receives -f
+        const double gx = pd * __dsub_rn(xb, xa);
+        const double gy = pd * __dsub_rn(yb, ya);
+        const double gz = pd * __dsub_rn(zb, za);
+        fx += gx;
+        fy += gy;
+        fz += gz;
+        atomicAdd(a.fx + j, -gx);
+        atomicAdd(a.fy + j, -gy);
+        atomicAdd(a.fz + j, -gz);
+        if (PE) {
+          pe += 0.5 * en;
+          atomicAdd(a.pe + j, 0.5 * en);
+        }
+      }
+    }
+    atomicAdd(a.fx + i, fx);
+    atomicAdd(a.fy + i, fy);
+    atomicAdd(a.fz + i, fz);
+    if (PE) atomicAdd(a.pe + i, pe);
+  }
+}
+
+// Clears f (and pe) of the selected systems before the reactions arrive.
+__global__ void __launch_bounds__(256)
+    k_zero_force(uint32_t n_part, const SysState* __restrict__ st, DevArrays a, int sys_only, bool with_pe) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
+    const uint32_t c = a.pcell[i];
+    if (c == kInvalid) continue;
+    const uint32_t s = a.cell_sys[c];
+    if (sys_only >= 0 && s != static_cast<uint32_t>(sys_only)) continue;
+    if (st[s].error) continue;
+    a.fx[i] = 0.0;
+    a.fy[i] = 0.0;
+    a.fz[i] = 0.0;
+    if (with_pe) a.pe[i] = 0.0;
+  }
+}
+
+// After the half-list traversal: divide_force_by_type_scalar and the second-half kick.
+__global__ void __launch_bounds__(256)
+    k_force_finish(uint32_t n_part, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a,
+                   int sys_only, bool kick) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
+    const uint32_t c = a.pcell[i];
+    if (c == kInvalid) continue;
+    const uint32_t s = a.cell_sys[c];
+    if (sys_only >= 0 && s != static_cast<uint32_t>(sys_only)) continue;
+    if (st[s].error) continue;
+    const SysDesc& S = sys[s];
+    double fx = a.fx[i], fy = a.fy[i], fz = a.fz[i];
+    if (S.divide_by_mass) {
+      fx = __ddiv_rn(fx, S.mass);
+      fy = __ddiv_rn(fy, S.mass);
+      fz = __ddiv_rn(fz, S.mass);
+      a.fx[i] = fx;
+      a.fy[i] = fy;
+      a.fz[i] = fz;
+    }
+    if (kick) {
+      const double h = S.dt_half;
+      a.vx[i] = fma(fx, h, a.vx[i]);
+      a.vy[i] = fma(fy, h, a.vy[i]);
+      a.vz[i] = fma(fz, h, a.vz[i]);
+    }
+  }
+}
+
 __global__ void k_mark_rebuild(int nsys, SysState* st, int mode, int sys_only, unsigned int* any) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsys) return;
@@ -344,8 +513,22 @@ int launch_first_half(const Extent& ex, const SysDesc* sys, SysState* st, const 
 }
 
 int launch_force(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int precision, bool with_pe,
-                  bool second_half, int sys_only, cudaStream_t stream) {
+                  bool second_half, int sys_only, cudaStream_t stream, bool newton) {
   if (ex.n_part == 0) return 0;
+  if (newton && precision != kFp64Exact) {
+    const int threads = 256;
+    const int g = grid_for(ex.n_part, threads, ex.sm_count, 8);
+    k_zero_force<<<g, threads, 0, stream>>>(ex.n_part, st, a, sys_only, with_pe);
+    if (precision == kFp64) {
+      if (with_pe) k_force_half<kFp64, true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);
+      else k_force_half<kFp64, false><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);
+    } else {
+      if (with_pe) k_force_half<kMixed, true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);
+      else k_force_half<kMixed, false><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);
+    }
+    k_force_finish<<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only, second_half);
+    return 3;
+  }
 #define XNB_FORCE_CASE(PP)                                                           \
   if (precision == PP) {                                                             \
     if (with_pe && second_half) force_dispatch<PP, true, true>(ex, sys, st, a, sys_only, stream);   \

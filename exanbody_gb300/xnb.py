@@ -14,7 +14,9 @@ from . import build as _build
 PREC_FP64_EXACT = 0
 PREC_FP64 = 1
 PREC_MIXED = 2
-PRECISIONS = {"fp64_exact": PREC_FP64_EXACT, "fp64": PREC_FP64, "mixed": PREC_MIXED}
+PREC_NEWTON = 0x10
+PRECISIONS = {"fp64_exact": PREC_FP64_EXACT, "fp64": PREC_FP64, "mixed": PREC_MIXED,
+              "fp64_newton": PREC_FP64 | PREC_NEWTON, "mixed_newton": PREC_MIXED | PREC_NEWTON}
 
 STEP_HOST_SYNC = 1
 STEP_ENERGY = 2

@@ -40,6 +40,12 @@ extern "C" {
 #define XNB_PREC_FP64_EXACT 0 /* the reference functor's operations, bit-identical to its CPU path */
 #define XNB_PREC_FP64 1       /* FP64, same pair set, reciprocal by Newton-Raphson, FMA */
 #define XNB_PREC_MIXED 2      /* FP64 positions/displacements/accumulation/integration; FP32 r^2, r^-6, |F| */
+/* Flag OR-ed into XNB_PREC_FP64 or XNB_PREC_MIXED: each pair inside rc is evaluated
+ * once (lower half of the sorted list, the reference's symmetric split) and the
+ * reaction is added to the partner with FP64 atomic reductions. Faster; results
+ * then agree with the full-list traversal to rounding, not bit for bit, and may
+ * differ in the last bits between runs. */
+#define XNB_PREC_NEWTON 0x10
 
 /* xnb_step flags */
 #define XNB_STEP_HOST_SYNC 1 /* read the trigger on the host and skip the rebuild launches when idle */

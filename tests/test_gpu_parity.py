@@ -215,3 +215,49 @@ def test_list_overflow_is_reported_and_recovered():
     b.step(200, xnb.PREC_MIXED, xnb.STEP_HOST_SYNC)
     b.check_errors()
     assert b.info(s).rebuilds >= 1
+
+
+def test_newton_half_list_forces_and_energy():
+    """Each pair once (lower half of the sorted list) with FP64 reductions for the
+    reaction: FP64 <= 1e-12 and MIXED <= 1e-5 against the full-list FP64 forces,
+    potential energy to 1e-12 relative."""
+    w = workloads.lj_fcc_system(20, 0.8442, 1.44, 12345)
+    b, s = gpu_system(w)
+    b.init_particles(s, xnb.PREC_FP64_EXACT)
+    b.step(30, xnb.PREC_FP64_EXACT, xnb.STEP_HOST_SYNC)
+    b.lennard_jones_force(s, xnb.PREC_FP64, True)
+    ref = b.download(s)
+    _, pe_ref = b.energy(s)
+    b.lennard_jones_force(s, xnb.PREC_FP64 | xnb.PREC_NEWTON, True)
+    g64 = b.download(s)
+    _, pe64 = b.energy(s)
+    b.lennard_jones_force(s, xnb.PREC_MIXED | xnb.PREC_NEWTON, True)
+    gmx = b.download(s)
+    e64, _ = force_error(forces(g64), forces(ref))
+    emx, _ = force_error(forces(gmx), forces(ref))
+    assert e64 <= FP64_TOL, e64
+    assert emx <= MIXED_TOL, emx
+    assert abs(pe64 - pe_ref) <= 1e-12 * abs(pe_ref)
+    # momentum: the pair forces cancel exactly in pairs up to FP64 rounding
+    assert np.abs(forces(g64).sum(axis=0)).max() < 1e-9
+
+
+def test_newton_batched_systems_match_alone_within_tolerance():
+    specs = workloads.ensemble_specs(4, seed=78, nmin=4, nmax=8)
+    ws = [workloads.lj_fcc_system(sp["n"], sp["rho"], sp["T"], sp["seed"]) for sp in specs]
+    prec = xnb.PREC_MIXED | xnb.PREC_NEWTON
+    big = new_batch([w["n_atoms"] for w in ws], [ncells(w["geom"]) for w in ws])
+    ids = [big.add_system(xnb.lj_params(w["geom"]), w["r"], w["v"], w["id"]) for w in ws]
+    big.init_particles(-1, prec)
+    big.step(40, prec, 0)
+    big.check_errors()
+    for w, s in zip(ws, ids):
+        b, so = gpu_system(w)
+        b.init_particles(so, prec)
+        b.step(40, prec, 0)
+        G, A = big.download(s), b.download(so)
+        assert np.array_equal(G["id"], A["id"])
+        for k in ("rx", "ry", "rz"):
+            assert np.max(np.abs(G[k] - A[k])) < 1e-9
+        e, _ = force_error(forces(G), forces(A))
+        assert e <= MIXED_TOL
