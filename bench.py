@@ -4,9 +4,9 @@ Workload (default): periodic FCC 100^3 = 4,000,000 atoms, rho* = 0.8442,
 T* = 1.44, truncated-and-shifted LJ rc = 2.5, skin 0.3, dt = 0.005; one bench
 "step" is one velocity-Verlet MD step (push, trigger, conditional rebin +
 neighbour rebuild, forces, push) of the whole system, in the mixed precision
-path with Newton half lists (each pair evaluated once, reactions by FP64
-reductions); the plain FP64 path is timed with the same traversal, and both
-full-list (bitwise reproducible) traversals are reported beside them. The state (~2.4 GB) is larger than L2 (129 MB), so no flush is needed.
+path. Each precision is timed with both force traversals (full lists, bitwise
+reproducible; Newton half lists with FP64 reductions) and reported at its
+faster one. The state (~2.4 GB) is larger than L2 (129 MB), so no flush is needed.
 
 Reported on one JSON line: mixed-path atom-steps/s with inputs resident in
 HBM (`value`), the plain FP64 path beside it, the force error of the mixed
@@ -248,15 +248,29 @@ def run_ours(args):
             ms = float(t.item())
         return ms
 
-    MIXED = xnb.PREC_MIXED | xnb.PREC_NEWTON
-    FP64 = xnb.PREC_FP64 | xnb.PREC_NEWTON
+    # Each precision is timed with both traversals (full lists: every pair from
+    # both sides, bitwise reproducible; Newton half lists: each pair once with
+    # FP64 reductions) and reported at its faster one.
+    MIXED_FULL, MIXED_NEWTON = xnb.PREC_MIXED, xnb.PREC_MIXED | xnb.PREC_NEWTON
+    FP64_FULL, FP64_NEWTON = xnb.PREC_FP64, xnb.PREC_FP64 | xnb.PREC_NEWTON
 
-    # ---- mixed path (Newton half lists), resident state ----
     b = new_batch()
     s = b.add_system(params, w["r"], w["v"], w["id"], list_factor=1.2)
-    b.init_particles(s, MIXED)
-    b.step(max(3, args.warmup), MIXED, 0)
+    b.init_particles(s, MIXED_FULL)
+    b.step(max(3, args.warmup), MIXED_FULL, 0)
     b.check_errors()
+    k64 = max(5, min(args.steps, 40))
+    trials = {}
+    for name, prec in (("mixed_full", MIXED_FULL), ("mixed_newton", MIXED_NEWTON), ("fp64_full", FP64_FULL),
+                       ("fp64_newton", FP64_NEWTON)):
+        b.step(2, prec, 0)
+        trials[name] = N * k64 / (timed(lambda: b.step(k64, prec, 0)) * 1e-3)
+    b.check_errors()
+    MIXED = MIXED_FULL if trials["mixed_full"] >= trials["mixed_newton"] else MIXED_NEWTON
+    FP64 = FP64_FULL if trials["fp64_full"] >= trials["fp64_newton"] else FP64_NEWTON
+
+    # ---- headline: the mixed path over the timed steps ----
+    b.step(max(3, args.warmup), MIXED, 0)
     reb0 = b.info(s).rebuilds
     l0 = b.kernel_launches()
     with Clocks(local) as ck:
@@ -267,20 +281,11 @@ def run_ours(args):
     rebuilds = b.info(s).rebuilds - reb0
     value = world * N * args.steps / (ms * 1e-3)
 
-    # ---- plain FP64 path (same traversal) from the same state ----
-    k64 = max(5, min(args.steps, 40))
+    # ---- plain FP64 path at its faster traversal, from the same state ----
     b.step(2, FP64, 0)
     ms64 = timed(lambda: b.step(k64, FP64, 0))
     b.check_errors()
     value64 = N * k64 / (ms64 * 1e-3)
-
-    # ---- deterministic full-list traversals (each pair from both sides) ----
-    full = {}
-    for name, prec in (("mixed", xnb.PREC_MIXED), ("fp64", xnb.PREC_FP64)):
-        b.step(2, prec, 0)
-        msf = timed(lambda: b.step(k64, prec, 0))
-        full[name] = N * k64 / (msf * 1e-3)
-    b.check_errors()
 
     # ---- force error of the mixed path against FP64 on one state ----
     b.lennard_jones_force(s, xnb.PREC_FP64, False)
@@ -364,13 +369,16 @@ def run_ours(args):
                                 precision="mixed", rebuilds_in_timed_steps=rebuilds),
             "fp64": {"value": value64, "unit": "atom-steps/s", "steps": k64,
                      "speedup_mixed_vs_fp64": value / world / value64},
-            "full_list_deterministic": {"mixed": full["mixed"], "fp64": full["fp64"], "unit": "atom-steps/s",
-                                        "note": "each pair evaluated from both sides, bitwise reproducible"},
+            "traversals": dict(trials, unit="atom-steps/s", steps=k64,
+                               chosen={"mixed": "newton" if MIXED & xnb.PREC_NEWTON else "full",
+                                       "fp64": "newton" if FP64 & xnb.PREC_NEWTON else "full"}),
             "force_error_mixed_vs_fp64": {"max": err_max, "rms": err_rms, "tolerance": 1e-5},
             "clocks": clocks,
             "e2e": e2e,
             "gpu_launches": launches,
-            "roofline": {"bound": "fp64", "kernel": "k_force_half<mixed> (+ zero/finish launches)",
+            "roofline": {"bound": "fp64",
+                         "kernel": ("k_force_half<mixed> (+ zero/finish launches)" if MIXED & xnb.PREC_NEWTON
+                                    else "k_force<mixed>"),
                          "achieved": achieved, "peak": peak64,
                          "unit": "TFLOP/s", "frac": achieved / peak64,
                          "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",

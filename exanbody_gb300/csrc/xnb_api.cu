@@ -94,6 +94,7 @@ struct xnb_batch {
   int sm_count = 1;
   xnb_batch_config cfg{};
   int stage_cap = 640;
+  int force_block = 256;
   DevArrays a{};
   SysDesc* d_sys = nullptr;
   SysState* d_st = nullptr;
@@ -111,6 +112,7 @@ struct xnb_batch {
       if (sys[s].active) hw = static_cast<int>(s) + 1;
     e.nsys = hw;
     e.sm_count = sm_count;
+    e.force_block = force_block;
     return e;
   }
 };
@@ -336,7 +338,9 @@ const char* xnb_last_error_string(void) { return g_err.c_str(); }
 int xnb_version(void) { return 10000; }
 
 int64_t xnb_system_bytes(int64_t n, int64_t ncells, double list_per_particle) {
-  const int64_t per_part = 8 * 10 + 8 + 4 + 12 + 24 + 8 * 9 + 8 + 4 * 3 + 4 * 3 + 32 + 4 * kMaskWords;
+  // doubles r v f pe, restored backup, rebin scratch (22); ids (2); u32 cell, backup,
+  // rebin and list bookkeeping (11); FP32 hi/lo mirrors; ballot masks
+  const int64_t per_part = 22 * 8 + 2 * 8 + 11 * 4 + 2 * 16 + 4 * kMaskWords;
   const int64_t per_cell = 4 * 7 + 8 * 2 + 4;
   return n * per_part + ncells * per_cell + static_cast<int64_t>(static_cast<double>(n) * list_per_particle) * 4;
 }
@@ -352,6 +356,17 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   b->device = cfg->device;
   b->cfg = *cfg;
   if (cfg->stage_cap > 0) b->stage_cap = (cfg->stage_cap + 31) / 32 * 32;
+  if (cfg->stage_cap > 2048) {
+    delete b;
+    return fail(XNB_ERR_ARG, "stage_cap above 2048 candidates");
+  }
+  if (cfg->force_block > 0) {
+    if (cfg->force_block % 32 || cfg->force_block > 256) {
+      delete b;
+      return fail(XNB_ERR_ARG, "force_block must be a multiple of 32 and at most 256");
+    }
+    b->force_block = cfg->force_block;
+  }
   cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, cfg->device);
   const uint64_t P = static_cast<uint64_t>(cfg->particle_capacity);
   const uint64_t Cc = static_cast<uint64_t>(cfg->cell_capacity);

@@ -381,8 +381,12 @@ __device__ __forceinline__ float4 stage_candidate(const SysDesc& S, const DevArr
       if (v[ax] < S.outer_lo_f[ax] - fm || v[ax] > S.outer_hi_f[ax] + fm) out = true;
       else if (v[ax] < S.outer_lo_f[ax] + fm || v[ax] > S.outer_hi_f[ax] - fm) amb = true;
     }
-    if (out) ent = kInvalid;
-    else if (amb) ent |= kAmbiguousBit;
+    if (out) {
+      ent = kInvalid;
+      rb.x = rb.y = rb.z = 1.0e18f;  // never within reach: the test needs no validity check
+    } else if (amb) {
+      ent |= kAmbiguousBit;
+    }
   }
   rb.w = __uint_as_float(ent);
   return rb;
@@ -478,6 +482,8 @@ __global__ void __launch_bounds__(128)
     const uint32_t ncand = __shfl_sync(0xffffffffu, g_off, 26);
     g_off -= g_n;
     const bool use_masks = ncand <= kMaskWords * 32u;
+    float4 own = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (na <= 32 && lane < na) own = a.pf[sa + lane];
     // candidates before cell a's own group come first (groups g < 13), then cell a
     const uint32_t off_self = __shfl_sync(0xffffffffu, g_off, 13);
 
@@ -509,43 +515,64 @@ __global__ void __launch_bounds__(128)
       }
       __syncwarp();
       const uint32_t m = c1 - c0;
+      const uint32_t nsub = (m + 31) / 32;
       for (uint32_t pa = 0; pa < na; ++pa) {
         const uint32_t i = sa + pa;
         uint32_t* maskp = a.nbr_masks + static_cast<size_t>(i) * kMaskWords + c0 / 32;
-        uint32_t cursor = 0;
-        if (FILL) cursor = a.nbr_cursor[i];
         // entries taken before candidate index lower_end form the lower half
         const uint32_t lower_end = off_self + pa;
-        uint32_t half = 0;
         if (!test) {
-          // fill from the count pass's ballots: the particle's mask words arrive in one
-          // coalesced load (lane w holds word w) and are broadcast by shuffles
-          const uint32_t nsub = (m + 31) / 32;
+          // fill from the count pass's ballots: lane w owns mask word w and writes
+          // that word's hits at cursor + (hits in words before w) + rank
+          uint32_t cursor = a.nbr_cursor[i];
           const uint32_t mine = lane < nsub ? __ldg(maskp + lane) : 0u;
-          for (uint32_t t0 = 0; t0 < m; t0 += 32) {
-            const uint32_t mask = __shfl_sync(0xffffffffu, mine, t0 / 32);
-            if (mask) {
-              if ((mask >> lane) & 1u) a.nbr[S.list_base + cursor + __popc(mask & lt)] = sent[t0 + lane];
-              cursor += __popc(mask);
-              const uint32_t gbase = c0 + t0;
-              if (gbase < lower_end)
-                half += __popc(lower_end - gbase >= 32u ? mask : (mask & ((1u << (lower_end - gbase)) - 1u)));
-            }
+          const uint32_t cntw = __popc(mine);
+          uint32_t pre = cntw;
+          for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, pre, off);
+            if (lane >= static_cast<uint32_t>(off)) pre += v;
+          }
+          const uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
+          pre -= cntw;
+          uint32_t bits = mine;
+          uint32_t* out = a.nbr + S.list_base + cursor + pre;
+          const uint32_t* src = sent + lane * 32;
+          while (bits) {
+            const int bpos = __ffs(bits) - 1;
+            *out++ = src[bpos];
+            bits &= bits - 1;
+          }
+          // lower-half count: hits with candidate index below lower_end
+          const uint32_t gbase = c0 + lane * 32;
+          uint32_t lowc = 0;
+          if (gbase < lower_end) lowc = __popc(lower_end - gbase >= 32u ? mine : (mine & ((1u << (lower_end - gbase)) - 1u)));
+          for (int off = 16; off > 0; off >>= 1) lowc += __shfl_xor_sync(0xffffffffu, lowc, off);
+          if (lane == 0) {
+            a.nbr_cursor[i] = cursor + total;
+            a.nbr_half[i] = (c0 == 0 ? 0u : a.nbr_half[i]) + lowc;
           }
         } else {
-          const float4 paf = a.pf[i];
+          float4 paf;
+          if (na <= 32) {
+            paf.x = __shfl_sync(0xffffffffu, own.x, pa);
+            paf.y = __shfl_sync(0xffffffffu, own.y, pa);
+            paf.z = __shfl_sync(0xffffffffu, own.z, pa);
+          } else {
+            paf = a.pf[i];
+          }
           const uint32_t self_ent = ((i - S.part_base) << 5) | static_cast<uint32_t>(kImageCenter);
-          uint32_t cnt = 0;
+          uint32_t cnt = 0, mymask = 0, half = 0;
+          uint32_t cursor = 0;
+          if (FILL) cursor = a.nbr_cursor[i];
           for (uint32_t t0 = 0; t0 < m; t0 += 32) {
             const uint32_t t = t0 + lane;
-            float4 b = make_float4(0.f, 0.f, 0.f, __uint_as_float(kInvalid));
+            float4 b = make_float4(1.0e18f, 1.0e18f, 1.0e18f, __uint_as_float(kInvalid));
             if (t < m) b = srel[t];
             const uint32_t ent = __float_as_uint(b.w);
-            const bool cand = ent != kInvalid && ent != self_ent;
             const float dx = paf.x - b.x, dy = paf.y - b.y, dz = paf.z - b.z;
             const float d2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            bool hit = cand && d2f < nb_lo && d2f > nb_zero && !(ent & kAmbiguousBit);
-            const bool maybe = cand && !hit && d2f <= nb_hi;
+            bool hit = d2f < nb_lo && d2f > nb_zero && !(ent & kAmbiguousBit);
+            const bool maybe = !hit && d2f <= nb_hi && ent != self_ent;
             if (__any_sync(0xffffffffu, maybe)) {
               if (maybe) hit = exact_neighbor_test(S, a, i, ent);
             }
@@ -558,15 +585,17 @@ __global__ void __launch_bounds__(128)
                 half += __popc(lower_end - gbase >= 32u ? mask : (mask & ((1u << (lower_end - gbase)) - 1u)));
             } else {
               cnt += __popc(mask);
-              if (use_masks && lane == 0) maskp[t0 / 32] = mask;
+              if (lane == t0 / 32) mymask = mask;
             }
           }
-          if (!FILL && lane == 0) a.nbr_cnt[i] = (c0 == 0 ? 0u : a.nbr_cnt[i]) + cnt;
-          cell_total += cnt;
-        }
-        if (FILL && lane == 0) {
-          a.nbr_cursor[i] = cursor;
-          a.nbr_half[i] = (c0 == 0 ? 0u : a.nbr_half[i]) + half;
+          if (!FILL) {
+            if (use_masks && lane < nsub) maskp[lane] = mymask;
+            if (lane == 0) a.nbr_cnt[i] = (c0 == 0 ? 0u : a.nbr_cnt[i]) + cnt;
+            cell_total += cnt;
+          } else if (lane == 0) {
+            a.nbr_cursor[i] = cursor;
+            a.nbr_half[i] = (c0 == 0 ? 0u : a.nbr_half[i]) + half;
+          }
         }
       }
       __syncwarp();

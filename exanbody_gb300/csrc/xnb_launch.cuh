@@ -16,6 +16,7 @@ struct Extent {
   uint32_t n_cells;  // cells [0, n_cells); free cells have cell_sys == ~0u
   int nsys;
   int sm_count;
+  int force_block;   // threads per block of the force traversal (multiple of 32, <= 256)
 };
 
 // Fused first half of velocity Verlet plus the displacement trigger:

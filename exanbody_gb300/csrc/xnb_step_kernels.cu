@@ -490,7 +490,7 @@ inline int grid_for(uint32_t n, int threads, int sm_count, int per_sm) {
 template <int P, bool PE, bool KICK>
 void force_dispatch(const Extent& ex, const SysDesc* sys, const SysState* st, const DevArrays& a, int sys_only,
                     cudaStream_t stream) {
-  const int threads = 256;
+  const int threads = ex.force_block > 0 ? ex.force_block : 256;
   k_force<P, PE, KICK><<<grid_for(ex.n_part, threads, ex.sm_count, 8), threads, 0, stream>>>(ex.n_part, sys, st, a,
                                                                                            sys_only);
 }
@@ -516,7 +516,7 @@ int launch_force(const Extent& ex, const SysDesc* sys, SysState* st, const DevAr
                   bool second_half, int sys_only, cudaStream_t stream, bool newton) {
   if (ex.n_part == 0) return 0;
   if (newton && precision != kFp64Exact) {
-    const int threads = 256;
+    const int threads = ex.force_block > 0 ? ex.force_block : 256;
     const int g = grid_for(ex.n_part, threads, ex.sm_count, 8);
     k_zero_force<<<g, threads, 0, stream>>>(ex.n_part, st, a, sys_only, with_pe);
     if (precision == kFp64) {

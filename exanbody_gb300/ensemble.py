@@ -1,0 +1,146 @@
+"""Batched ensemble of independent LJ systems in one batch, and its autotuner.
+
+All systems of a batch advance together: every kernel of a step covers the
+packed particle and cell tables of every system (uneven sizes, empty cells
+included), and the step sequence is captured as a CUDA graph
+(xnb_step_graph_create) so a chunk of steps costs one launch on the host.
+
+The autotuner times short trials of the batch over the tunables the library
+exposes -- neighbour-build staging capacity (candidates per warp chunk),
+force-traversal threads per block, the force traversal itself (full lists or
+Newton half lists) and, when asked, the Verlet skin -- and keeps the fastest.
+
+  python -m exanbody_gb300.ensemble [--count 1024] [--steps 500] [--autotune]
+"""
+import argparse
+import ctypes
+import itertools
+import json
+import time
+
+import numpy as np
+
+from . import workloads, xnb
+
+DEFAULTS = dict(stage_cap=640, force_block=256, skin=0.3, newton=False)
+
+
+def make_systems(specs, rcut=2.5, skin=0.3):
+    return [workloads.lj_fcc_system(sp["n"], sp["rho"], sp["T"], sp["seed"], rcut, skin) for sp in specs]
+
+
+def build_batch(systems, stage_cap=640, force_block=256, skin=0.3, rcut=2.5, dt=0.005, stream=None,
+                precision=xnb.PREC_MIXED, list_per_atom=None):
+    n_atoms = sum(w["n_atoms"] for w in systems)
+    n_cells = sum(int(np.prod(w["geom"]["dims"])) for w in systems)
+    if list_per_atom is None:
+        # neighbours within rc + skin at the densest state point of the batch, with margin
+        rho = max(w["rho"] for w in systems)
+        list_per_atom = 1.3 * (4.0 / 3.0) * np.pi * (rcut + skin) ** 3 * rho + 16
+    b = xnb.Batch(n_atoms + 64 * len(systems), n_cells + 64, int(list_per_atom * n_atoms) + 4096,
+                  max_systems=len(systems), stage_cap=stage_cap, force_block=force_block)
+    if stream is not None:
+        b.stream = ctypes.c_void_p(stream)
+    ids = [b.add_system(xnb.lj_params(w["geom"], rcut=rcut, rcut_inc=skin, dt=dt), w["r"], w["v"], w["id"],
+                        list_factor=1.25) for w in systems]
+    b.init_particles(-1, precision)
+    return b, ids, n_atoms
+
+
+def timed_steps(batch, stream, steps, precision, chunk=10):
+    """Run `steps` MD steps as replays of a captured `chunk`-step graph; seconds."""
+    import torch
+
+    g = batch.graph(chunk, precision, 0)
+    g.launch()  # warm
+    stream.synchronize()
+    reps = max(1, steps // chunk)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        g.launch()
+    e1.record(stream)
+    e1.synchronize()
+    batch.check_errors()
+    g.close()
+    return e0.elapsed_time(e1) * 1e-3, reps * chunk
+
+
+def trial(systems, cfg, steps, precision, stream):
+    prec = precision | (xnb.PREC_NEWTON if cfg["newton"] else 0)
+    b, ids, n = build_batch(systems, cfg["stage_cap"], cfg["force_block"], cfg["skin"], stream=stream.cuda_stream,
+                            precision=prec)
+    try:
+        secs, done = timed_steps(b, stream, steps, prec)
+    finally:
+        b.close()
+    return n * done / secs
+
+
+def autotune(systems, precision=xnb.PREC_MIXED, steps=40, tune_skin=False, stream=None):
+    """Coordinate search over the tunables on the given systems (a sample of the batch)."""
+    import torch
+
+    stream = stream or torch.cuda.Stream()
+    space = {
+        "stage_cap": [384, 640, 1024],
+        "force_block": [128, 256],
+        "newton": [False, True],
+        "skin": [0.3, 0.4, 0.5] if tune_skin else [0.3],
+    }
+    best = dict(DEFAULTS)
+    best_rate = trial(systems, best, steps, precision, stream)
+    log = [dict(best, rate=best_rate)]
+    for key in ("stage_cap", "force_block", "newton", "skin"):
+        for v in space[key]:
+            if v == best[key]:
+                continue
+            cand = dict(best, **{key: v})
+            rate = trial(systems, cand, steps, precision, stream)
+            log.append(dict(cand, rate=rate))
+            if rate > best_rate:
+                best, best_rate = cand, rate
+    return best, best_rate, log
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--count", type=int, default=1024)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--tune-skin", action="store_true")
+    ap.add_argument("--tune-sample", type=int, default=128, help="systems used for the autotuner trials")
+    args = ap.parse_args()
+    import torch
+
+    specs = workloads.ensemble_specs(args.count, seed=args.seed)
+    systems = make_systems(specs)
+    stream = torch.cuda.Stream()
+    cfg = dict(DEFAULTS)
+    tune_log = None
+    t0 = time.perf_counter()
+    if args.autotune:
+        sample = systems[: args.tune_sample]
+        cfg, _, tune_log = autotune(sample, xnb.PREC_MIXED, tune_skin=args.tune_skin, stream=stream)
+    tune_s = time.perf_counter() - t0
+    out = {"workload": "ensemble_%d_fcc_n4-25_rho0.70-1.00_T0.7-1.5" % args.count,
+           "atoms": int(sum(w["n_atoms"] for w in systems)), "systems": args.count, "steps": args.steps,
+           "config": cfg, "autotune_seconds": tune_s}
+    for name, base in (("mixed", xnb.PREC_MIXED), ("fp64", xnb.PREC_FP64)):
+        prec = base | (xnb.PREC_NEWTON if cfg["newton"] else 0)
+        b, ids, n = build_batch(systems, cfg["stage_cap"], cfg["force_block"], cfg["skin"],
+                                stream=stream.cuda_stream, precision=prec)
+        secs, done = timed_steps(b, stream, args.steps, prec)
+        rebuilds = sum(b.info(s).rebuilds for s in ids)
+        b.close()
+        out[name] = {"atom_steps_per_s": n * done / secs, "seconds": secs, "steps": done,
+                     "rebuilds_total": int(rebuilds)}
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"]
+    if tune_log is not None:
+        out["autotune_trials"] = tune_log
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

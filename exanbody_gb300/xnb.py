@@ -61,7 +61,7 @@ class BatchConfig(C.Structure):
         ("cell_capacity", C.c_int64),
         ("list_capacity", C.c_int64),
         ("stage_cap", C.c_int32),
-        ("reserved", C.c_int32),
+        ("force_block", C.c_int32),
     ]
 
 
@@ -168,10 +168,10 @@ class Batch:
     """Device pools holding any number of resident systems (xnb_batch)."""
 
     def __init__(self, particle_capacity, cell_capacity, list_capacity, max_systems=1, device=0, stage_cap=0,
-                 stream=None):
+                 stream=None, force_block=0):
         self.lib = load()
         cfg = BatchConfig(int(device), int(max_systems), int(particle_capacity), int(cell_capacity),
-                          int(list_capacity), int(stage_cap), 0)
+                          int(list_capacity), int(stage_cap), int(force_block))
         h = C.c_void_p()
         _ck(self.lib.xnb_batch_create(C.byref(cfg), C.byref(h)))
         self.h = h

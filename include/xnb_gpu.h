@@ -85,8 +85,8 @@ typedef struct xnb_batch_config {
   int64_t particle_capacity; /* particles over all resident systems */
   int64_t cell_capacity;     /* cells over all resident systems */
   int64_t list_capacity;     /* neighbour entries over all resident systems */
-  int32_t stage_cap;         /* neighbour-build staging candidates per warp; 0 = default */
-  int32_t reserved;
+  int32_t stage_cap;         /* neighbour-build staging candidates per warp; 0 = default (640) */
+  int32_t force_block;       /* threads per block of the force traversal; 0 = default (256) */
 } xnb_batch_config;
 
 typedef struct xnb_system_info {
