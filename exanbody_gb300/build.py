@@ -43,6 +43,26 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+HOST = os.path.join(HERE, "host")
+EXEC = os.path.join(OUT, "xnb-exec")
+
+
+def build_host(verbose=False):
+    """xnb-exec: the C++ operator/deck runner over libxnb_gpu.so."""
+    srcs = sorted(os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".cpp"))
+    deps = srcs + [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".hpp")] + [LIB]
+    if not _stale(EXEC, deps):
+        return EXEC
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), *srcs,
+           "-L", OUT, "-lxnb_gpu", "-Wl,-rpath,$ORIGIN", "-o", EXEC + ".tmp"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    if subprocess.call(cmd) != 0:
+        raise RuntimeError("xnb-exec build failed")
+    os.replace(EXEC + ".tmp", EXEC)
+    return EXEC
+
+
 def build(verbose=False, extra_flags=None):
     os.makedirs(OUT, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
@@ -67,6 +87,7 @@ def build(verbose=False, extra_flags=None):
         if subprocess.call(cmd) != 0:
             raise RuntimeError("link failed")
         os.replace(LIB + ".tmp", LIB)
+    build_host(verbose)
     return LIB
 
 

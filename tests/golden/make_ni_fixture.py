@@ -29,3 +29,11 @@ dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "check_values_lj_
 with open(dst, "w") as f:
     json.dump(out, f, indent=0)
 print("wrote", dst, len(rows), "rows")
+# the same rows in the check_values file layout (values: - [id, 9 hex floats]),
+# read by the deck runner's check_values operator
+dat = os.path.join(os.path.dirname(os.path.abspath(__file__)), "check_values_lj_Ni.dat")
+with open(dat, "w") as f:
+    f.write("length_unit: 1.0 ang\nvalues:\n")
+    for r in rows:
+        f.write("- [%d, %s]\n" % (r["id"], ", ".join(r["hex"])))
+print("wrote", dat)
