@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--n", type=int, default=WORKLOAD["n"], help="FCC unit cells per side")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--force-block", type=int, default=0, help="threads per block of the force kernel (0: library default)")
+    ap.add_argument("--stage-cap", type=int, default=0, help="neighbour-build staging candidates (0: library default)")
     return ap.parse_args()
 
 
@@ -226,7 +228,8 @@ def run_ours(args):
     params = xnb.lj_params(g, rcut=WORKLOAD["rcut"], rcut_inc=WORKLOAD["skin"], dt=WORKLOAD["dt"])
 
     def new_batch():
-        b = xnb.Batch(N + 64, ncell + 64, int(N * 120) + 4096, max_systems=1, device=local)
+        b = xnb.Batch(N + 64, ncell + 64, int(N * 160) + 4096, max_systems=1, device=local,
+                      stage_cap=args.stage_cap, force_block=args.force_block)
         b.stream = sp
         return b
 

@@ -65,7 +65,7 @@ def build_host(verbose=False):
 
 def build(verbose=False, extra_flags=None):
     os.makedirs(OUT, exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "xnb_gpu.h"))
     flags = NVCC_FLAGS + (extra_flags or [])
     objs, procs = [], []

@@ -94,7 +94,7 @@ struct xnb_batch {
   int sm_count = 1;
   xnb_batch_config cfg{};
   int stage_cap = 640;
-  int force_block = 256;
+  int force_block = 128;
   DevArrays a{};
   SysDesc* d_sys = nullptr;
   SysState* d_st = nullptr;
@@ -262,49 +262,80 @@ int pull_states(xnb_batch* b, cudaStream_t st) {
   return XNB_OK;
 }
 
-// Neighbour lists for flagged systems: count pass, segment sizing on the host
-// (synchronising), fill pass.
+// Per-warp list buffer of the neighbour build: the largest slot of the resident
+// systems, rounded up to 32 entries, at most kMaxListBuf (larger slots are
+// written without buffering).
+constexpr uint32_t kMaxListBuf = 1024;
+int list_buf(const xnb_batch* b) {
+  uint32_t m = 0;
+  for (const SysHost& h : b->sys)
+    if (h.active && h.d.list_slot > m) m = h.d.list_slot;
+  m = (m + 31) / 32 * 32;
+  return static_cast<int>(m > kMaxListBuf ? 0 : m);
+}
+
+// (Re)sizes system s's list segment for a largest per-particle count `need`:
+// slot = list_factor * max(need, 1.2 x the mean count of a uniform fluid of the
+// system's density) + 16 entries, rounded up to 8 (32-byte list starts). The
+// density term covers a lattice start whose counts sit below the fluid's.
+int size_lists(xnb_batch* b, int s, uint32_t need, cudaStream_t st) {
+  SysHost& h = b->sys[s];
+  const double vol = std::fabs(h.d.period[0] * h.d.period[1] * h.d.period[2]);
+  const double nbh = std::sqrt(h.d.nbh2);
+  const double fluid = vol > 0 ? 1.2 * 4.18879020478639 * nbh * nbh * nbh * static_cast<double>(h.d.npart) / vol : 0.0;
+  const double base = std::max(static_cast<double>(need), std::ceil(fluid));
+  uint64_t slot = static_cast<uint64_t>(std::ceil(base * h.list_factor)) + 16;
+  slot = (slot + 7) / 8 * 8;
+  if (slot < h.d.list_slot) slot = h.d.list_slot;
+  const uint64_t entries = static_cast<uint64_t>(h.d.npart) * slot;
+  if (entries >= (1ull << 32)) return fail(XNB_ERR_ARG, "neighbour lists of one system above 2^32 entries");
+  if (h.list_off >= 0) b->lists.release(static_cast<uint64_t>(h.list_off));
+  // every segment is a multiple of 8 entries, so each list starts on a 32-byte boundary
+  const int64_t off = b->lists.alloc(std::max<uint64_t>(entries, 8));
+  if (off < 0) {
+    h.list_off = -1;
+    h.list_cap = 0;
+    h.d.list_base = 0;
+    h.d.list_slot = 0;
+    upload_desc(b, s, st);
+    return fail(XNB_ERR_NOMEM, "neighbour list pool exhausted");
+  }
+  h.list_off = off;
+  h.list_cap = entries;
+  h.d.list_base = static_cast<uint64_t>(off);
+  h.d.list_slot = static_cast<uint32_t>(slot);
+  int rc = upload_desc(b, s, st);
+  if (rc) return rc;
+  // the build against the old slot flagged an overflow: clear it
+  const uint32_t err = b->h_st[s].error & ~kErrListOverflow;
+  XCK(cudaMemcpyAsync(&b->d_st[s].error, &err, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  b->h_st[s].error = err;
+  return XNB_OK;
+}
+
+// Neighbour lists for flagged systems, synchronising with the host: one build
+// pass; a system without a segment yet (slot 0: the pass only counts) or whose
+// largest count outgrew its slot gets a segment sized from that count, and the
+// pass runs again. Counts depend only on positions, so the second pass fits.
 int neighbors_sync(xnb_batch* b, cudaStream_t st) {
   const Extent ex = b->extent();
-  b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, st, 1);
-  int rc = pull_states(b, st);
-  if (rc) return rc;
-  bool changed = false;
-  for (int s = 0; s < ex.nsys; ++s) {
-    SysHost& h = b->sys[s];
-    if (!h.active || !b->h_st[s].rebuild) continue;
-    const uint64_t need = b->h_st[s].list_used;
-    if (need > h.list_cap || h.list_off < 0) {
-      if (h.list_off >= 0) b->lists.release(static_cast<uint64_t>(h.list_off));
-      const uint64_t cap = static_cast<uint64_t>(std::ceil(static_cast<double>(need) * h.list_factor)) + 64;
-      const int64_t off = b->lists.alloc(cap);
-      if (off < 0) {
-        h.list_off = -1;
-        h.list_cap = 0;
-        h.d.list_base = 0;
-        h.d.list_cap = 0;
-        upload_desc(b, s, st);
-        return fail(XNB_ERR_NOMEM, "neighbour list pool exhausted");
-      }
-      h.list_off = off;
-      h.list_cap = cap;
-      h.d.list_base = static_cast<uint64_t>(off);
-      h.d.list_cap = cap;
-      rc = upload_desc(b, s, st);
-      if (rc) return rc;
-      changed = true;
-    }
-  }
-  if (changed) {
-    // clear the overflow bit set by the check against the old capacity
+  for (int pass = 0; pass < 3; ++pass) {
+    b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, list_buf(b), st);
+    int rc = pull_states(b, st);
+    if (rc) return rc;
+    bool again = false;
     for (int s = 0; s < ex.nsys; ++s) {
-      if (!b->sys[s].active || !b->h_st[s].rebuild) continue;
-      const uint32_t err = b->h_st[s].error & ~kErrListOverflow;
-      XCK(cudaMemcpyAsync(&b->d_st[s].error, &err, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+      SysHost& h = b->sys[s];
+      if (!h.active || !b->h_st[s].rebuild) continue;
+      const uint32_t need = b->h_st[s].max_nbr;
+      if (h.list_off >= 0 && need <= h.d.list_slot) continue;
+      rc = size_lists(b, s, need, st);
+      if (rc) return rc;
+      again = true;
     }
+    if (!again) return XNB_OK;
   }
-  b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, st, 2);
-  return XNB_OK;
+  return fail(XNB_ERR_DEVICE, "neighbour lists did not fit their resized slots");
 }
 
 int clear_rebuild(xnb_batch* b, cudaStream_t st) {
@@ -339,9 +370,9 @@ int xnb_version(void) { return 10000; }
 
 int64_t xnb_system_bytes(int64_t n, int64_t ncells, double list_per_particle) {
   // doubles r v f pe, restored backup, rebin scratch (22); ids (2); u32 cell, backup,
-  // rebin and list bookkeeping (11); FP32 hi/lo mirrors; ballot masks
-  const int64_t per_part = 22 * 8 + 2 * 8 + 11 * 4 + 2 * 16 + 4 * kMaskWords;
-  const int64_t per_cell = 4 * 7 + 8 * 2 + 4;
+  // rebin and list bookkeeping (10); FP32 hi/lo mirrors
+  const int64_t per_part = 22 * 8 + 2 * 8 + 10 * 4 + 2 * 16;
+  const int64_t per_cell = 4 * 6 + 8 + 4;
   return n * per_part + ncells * per_cell + static_cast<int64_t>(static_cast<double>(n) * list_per_particle) * 4;
 }
 
@@ -381,17 +412,14 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   rc = rc ? rc : dalloc(b, &a.pf, P);
   rc = rc ? rc : dalloc(b, &a.pflo, P);
   rc = rc ? rc : dalloc(b, &a.nbr_half, P);
-  rc = rc ? rc : dalloc(b, &a.nbr_masks, P * kMaskWords);
   rc = rc ? rc : dalloc(b, &a.any_rebuild, 4);
   rc = rc ? rc : dalloc(b, &a.t_id, P);
   uint32_t** u32p[] = {&a.pcell, &a.bkx, &a.bky, &a.bkz, &a.pdest, &a.plocal, &a.mover_list,
-                       &a.nbr_start, &a.nbr_cnt, &a.nbr_cursor};
+                       &a.nbr_start, &a.nbr_cnt};
   for (uint32_t** p : u32p) rc = rc ? rc : dalloc(b, p, P);
-  uint32_t** u32c[] = {&a.cell_start, &a.cell_n, &a.cell_sys, &a.cell_cnt, &a.cell_stay, &a.cell_nmov,
-                       &a.cell_nbr_tot};
+  uint32_t** u32c[] = {&a.cell_start, &a.cell_n, &a.cell_sys, &a.cell_cnt, &a.cell_stay, &a.cell_nmov};
   for (uint32_t** p : u32c) rc = rc ? rc : dalloc(b, p, Cc + 1);
   rc = rc ? rc : dalloc(b, &a.cell_scan, Cc + 1);
-  rc = rc ? rc : dalloc(b, &a.cell_nbr_off, Cc + 1);
   rc = rc ? rc : dalloc(b, &a.scan_blocks, scan_scratch_elems(static_cast<uint32_t>(Cc + 1)) + 8);
   rc = rc ? rc : dalloc(b, &a.nbr, L);
   rc = rc ? rc : dalloc(b, &b->d_sys, static_cast<uint64_t>(cfg->max_systems));
@@ -583,7 +611,7 @@ int xnb_system_info_get(xnb_batch* b, int32_t s, xnb_system_info* info, void* st
   info->error_bits = b->h_st[s].error;
   info->max_cell = b->h_st[s].max_cell;
   info->active = h.active ? 1 : 0;
-  info->reserved = 0;
+  info->max_nbr = b->h_st[s].max_nbr;
   return XNB_OK;
 }
 
@@ -624,7 +652,7 @@ int xnb_system_pairs(xnb_batch* b, int32_t s, uint64_t* id_a, uint64_t* id_b, in
   const size_t n = h.d.npart, o = h.d.part_base;
   std::vector<uint32_t> start(n), cnt(n);
   std::vector<uint64_t> ids(n);
-  const uint64_t used = b->h_st[s].list_used;
+  const uint64_t used = h.list_off >= 0 ? h.list_cap : 0;
   std::vector<uint32_t> list(used);
   if (n) {
     XCK(cudaMemcpyAsync(start.data(), b->a.nbr_start + o, n * 4, cudaMemcpyDeviceToHost, st));
@@ -823,7 +851,7 @@ int xnb_step(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, voi
         int rc = neighbors_sync(b, st);
         if (rc) return rc;
       } else {
-        b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, st, 3);
+        b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, list_buf(b), st);
       }
     }
     // compute_all_forces_energy + verlet_second_half

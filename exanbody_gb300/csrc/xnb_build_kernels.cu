@@ -355,15 +355,11 @@ __global__ void k_arm(int nsys, SysState* st, const unsigned int* any) {
 // in (cell_enc, p_b) order. Ghost particles outside the partner block enlarged
 // by ghost_dist are not candidates (update_ghosts_comm_scheme.cpp:462-469).
 //
-// One warp per cell. Candidates are staged in shared memory as float4 (FP32
-// position relative to the system origin, entry bits in .w); lanes test 32
-// candidates at a time against one particle of the cell and a ballot keeps the
-// hits in order. The FP32 distance decides whenever it lies farther than a
+// Candidates are staged in shared memory as float4 (FP32 position relative to
+// the system origin, entry bits in .w); lanes test 32 candidates at a time
+// against one particle of the cell and a ballot keeps the hits in order. The FP32 distance decides whenever it lies farther than a
 // proven error bound from the threshold; otherwise the reference's FP64 d2 (and
 // the FP64 ghost filter) decide, so the pair set is bit-exact.
-// The count pass stores every 32-candidate ballot of a particle (kMaskWords
-// words); the fill pass then writes entries from the masks without testing
-// again. Cells with more than kMaskWords*32 candidates are tested again.
 constexpr uint32_t kAmbiguousBit = 0x80000000u;  // entry flag: ghost filter undecided in FP32
 
 __device__ __forceinline__ float4 stage_candidate(const SysDesc& S, const DevArrays& a, uint32_t j, uint32_t gc) {
@@ -408,54 +404,74 @@ __device__ __noinline__ bool exact_neighbor_test(const SysDesc& S, const DevArra
   return keep && d2 > 0.0 && d2 <= S.nbh2;
 }
 
-template <bool FILL>
+// Per-warp list statistics, flushed to the system's state when the warp moves
+// on to another system's cells and at the end.
+__device__ __forceinline__ void flush_list_stats(SysState* st, const SysDesc* sys, uint32_t s, uint32_t mx,
+                                                 unsigned long long sum) {
+  if (s == kInvalid) return;
+  if (mx > sys[s].list_slot) atomicOr(&st[s].error, kErrListOverflow);
+  atomicMax(&st[s].max_nbr, mx);
+  atomicAdd(&st[s].list_used, sum);
+}
+
+// Writes one particle's finished list: the buffered entries in full lines, its
+// count, lower-half length and slot start.
+__device__ __forceinline__ void finish_particle(const DevArrays& a, uint32_t* seg, const uint32_t* sbuf, bool buffered,
+                                                uint32_t i, uint32_t base, uint32_t slot, uint32_t cursor,
+                                                uint32_t half, bool first_round, uint32_t lane) {
+  if (buffered) {
+    __syncwarp();
+    const uint32_t nw = min(cursor, slot);
+    for (uint32_t q = lane; q < nw; q += 32) seg[base + q] = sbuf[q];
+    __syncwarp();
+  }
+  if (lane == 0) {
+    a.nbr_cnt[i] = cursor;
+    a.nbr_half[i] = half;
+    if (first_round) a.nbr_start[i] = base;
+  }
+}
+
+// One block per cell. The block stages the cell's candidates (up to `cap` per
+// round) once in shared memory for all its warps; warp w takes the cell's
+// particles w, w + 4, ... two at a time, so each candidate load serves two
+// tests. Each particle's hits go into its fixed slot of S.list_slot entries at
+// (i - part_base) * list_slot: no count pass, scan or second traversal. When the
+// cell's candidates fit one round and the slot fits the warp's list buffers
+// (lbuf entries each), a particle's hits are gathered in shared memory and its
+// list leaves in full 128-byte lines; otherwise each ballot's hits are stored
+// directly. A particle with more hits than the slot holds keeps its true count,
+// writes nothing past the slot and flags the system (kErrListOverflow); max_nbr
+// records the largest count for resizing.
 __global__ void __launch_bounds__(128)
-    k_neighbors(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap) {
+    k_neighbors(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap, int lbuf) {
   if (*a.any_rebuild == 0) return;
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ float4 stage_all[];
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t wib = threadIdx.x >> 5;
-  float4* srel = reinterpret_cast<float4*>(smem_raw) + static_cast<size_t>(wib) * cap;
-  uint32_t* sent = reinterpret_cast<uint32_t*>(srel);  // fill pass from masks: entries only, same per-warp region
+  const uint32_t nwarp = blockDim.x >> 5;
+  float4* srel = stage_all;
+  uint32_t* sbuf0 = reinterpret_cast<uint32_t*>(stage_all + cap) + static_cast<size_t>(wib) * 2 * lbuf;
+  uint32_t* sbuf1 = sbuf0 + lbuf;
   const unsigned lt = lanemask_lt();
-  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + wib; c < n_cells; c += warps) {
+  uint32_t acc_s = kInvalid, acc_max = 0;
+  unsigned long long acc_sum = 0;
+  for (uint32_t c = blockIdx.x; c < n_cells; c += gridDim.x) {
+    // every condition below depends on the cell only: the block stays together
     const uint32_t s = a.cell_sys[c];
-    if (s == kInvalid) continue;
-    if (!sys_flagged(st, s)) {
-      if (!FILL && lane == 0) a.cell_nbr_tot[c] = 0;
-      continue;
+    if (s == kInvalid || !sys_flagged(st, s)) continue;
+    const uint32_t na = a.cell_n[c];
+    if (na == 0) continue;
+    if (s != acc_s) {
+      if (lane == 0) flush_list_stats(st, sys, acc_s, acc_max, acc_sum);
+      acc_s = s;
+      acc_max = 0;
+      acc_sum = 0;
     }
-    if (FILL && (st[s].error & kErrListOverflow)) continue;
     const SysDesc& S = sys[s];
     const uint32_t sa = a.cell_start[c];
-    const uint32_t na = a.cell_n[c];
-    if (na == 0) {
-      if (!FILL && lane == 0) a.cell_nbr_tot[c] = 0;
-      continue;
-    }
     int ci, cj, ck;
     cell_ijk(S, c - S.cell_base, ci, cj, ck);
-
-    if (FILL) {
-      // per-particle list starts: cell offset + prefix of the counts
-      uint32_t run = static_cast<uint32_t>(a.cell_nbr_off[c] - a.cell_nbr_off[S.cell_base]);
-      for (uint32_t q0 = 0; q0 < na; q0 += 32) {
-        const uint32_t q = q0 + lane;
-        const uint32_t cnt = q < na ? a.nbr_cnt[sa + q] : 0;
-        uint32_t inc = cnt;
-        for (int off = 1; off < 32; off <<= 1) {
-          const uint32_t v = __shfl_up_sync(0xffffffffu, inc, off);
-          if (lane >= static_cast<uint32_t>(off)) inc += v;
-        }
-        if (q < na) {
-          a.nbr_start[sa + q] = run + inc - cnt;
-          a.nbr_cursor[sa + q] = run + inc - cnt;
-        }
-        run += __shfl_sync(0xffffffffu, inc, 31);
-      }
-      __syncwarp();
-    }
 
     // group table: lane g < 27 describes neighbour cell g in (dk, dj, di) order
     uint32_t g_start = 0, g_n = 0, g_code = kImageCenter;
@@ -481,7 +497,6 @@ __global__ void __launch_bounds__(128)
     }
     const uint32_t ncand = __shfl_sync(0xffffffffu, g_off, 26);
     g_off -= g_n;
-    const bool use_masks = ncand <= kMaskWords * 32u;
     float4 own = make_float4(0.f, 0.f, 0.f, 0.f);
     if (na <= 32 && lane < na) own = a.pf[sa + lane];
     // candidates before cell a's own group come first (groups g < 13), then cell a
@@ -490,130 +505,121 @@ __global__ void __launch_bounds__(128)
     const float nb_hi = S.nbh2_f + S.nbh_margin_f;
     const float nb_lo = S.nbh2_f - S.nbh_margin_f;
     const float nb_zero = S.nbh_margin_f;
-    uint32_t cell_total = 0;
+    const uint32_t slot = S.list_slot;
+    uint32_t* const seg = a.nbr + S.list_base;
+    const bool buffered = ncand <= static_cast<uint32_t>(cap) && slot <= static_cast<uint32_t>(lbuf);
 
     for (uint32_t c0 = 0; c0 < ncand; c0 += static_cast<uint32_t>(cap)) {
       const uint32_t c1 = min(ncand, c0 + static_cast<uint32_t>(cap));
-      const bool test = !FILL || !use_masks;
-      // stage candidates [c0, c1)
+      const uint32_t m = c1 - c0;
+      const uint32_t mpad = (m + 31u) & ~31u;  // <= cap (a multiple of 32)
+      __syncthreads();  // the previous round's readers are done with srel
       for (int g = 0; g < 27; ++g) {
         const uint32_t gs = __shfl_sync(0xffffffffu, g_start, g);
         const uint32_t gn = __shfl_sync(0xffffffffu, g_n, g);
         const uint32_t go = __shfl_sync(0xffffffffu, g_off, g);
         const uint32_t gc = __shfl_sync(0xffffffffu, g_code, g);
         if (go + gn <= c0 || go >= c1) continue;
-        for (uint32_t q = lane; q < gn; q += 32) {
+        for (uint32_t q = threadIdx.x; q < gn; q += blockDim.x) {
           const uint32_t t = go + q;
           if (t < c0 || t >= c1) continue;
-          const uint32_t j = gs + q;
-          if (test) {
-            srel[t - c0] = stage_candidate(S, a, j, gc);
-          } else {
-            sent[t - c0] = ((j - S.part_base) << 5) | gc;
-          }
+          srel[t - c0] = stage_candidate(S, a, gs + q, gc);
         }
       }
-      __syncwarp();
-      const uint32_t m = c1 - c0;
-      const uint32_t nsub = (m + 31) / 32;
-      for (uint32_t pa = 0; pa < na; ++pa) {
-        const uint32_t i = sa + pa;
-        uint32_t* maskp = a.nbr_masks + static_cast<size_t>(i) * kMaskWords + c0 / 32;
-        // entries taken before candidate index lower_end form the lower half
-        const uint32_t lower_end = off_self + pa;
-        if (!test) {
-          // fill from the count pass's ballots: lane w owns mask word w and writes
-          // that word's hits at cursor + (hits in words before w) + rank
-          uint32_t cursor = a.nbr_cursor[i];
-          const uint32_t mine = lane < nsub ? __ldg(maskp + lane) : 0u;
-          const uint32_t cntw = __popc(mine);
-          uint32_t pre = cntw;
-          for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, pre, off);
-            if (lane >= static_cast<uint32_t>(off)) pre += v;
-          }
-          const uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
-          pre -= cntw;
-          uint32_t bits = mine;
-          uint32_t* out = a.nbr + S.list_base + cursor + pre;
-          const uint32_t* src = sent + lane * 32;
-          while (bits) {
-            const int bpos = __ffs(bits) - 1;
-            *out++ = src[bpos];
-            bits &= bits - 1;
-          }
-          // lower-half count: hits with candidate index below lower_end
-          const uint32_t gbase = c0 + lane * 32;
-          uint32_t lowc = 0;
-          if (gbase < lower_end) lowc = __popc(lower_end - gbase >= 32u ? mine : (mine & ((1u << (lower_end - gbase)) - 1u)));
-          for (int off = 16; off > 0; off >>= 1) lowc += __shfl_xor_sync(0xffffffffu, lowc, off);
-          if (lane == 0) {
-            a.nbr_cursor[i] = cursor + total;
-            a.nbr_half[i] = (c0 == 0 ? 0u : a.nbr_half[i]) + lowc;
-          }
+      // padding up to a whole ballot: unreachable dummies, so the test needs no bound check
+      for (uint32_t t = m + threadIdx.x; t < mpad; t += blockDim.x)
+        srel[t] = make_float4(1.0e18f, 1.0e18f, 1.0e18f, __uint_as_float(kInvalid));
+      __syncthreads();
+      const bool last_round = c1 == ncand;
+      for (uint32_t pa = wib; pa < na; pa += 2 * nwarp) {
+        const uint32_t pb = pa + nwarp;  // second particle of the pair
+        const bool two = pb < na;
+        const uint32_t i0 = sa + pa, i1 = sa + (two ? pb : pa);
+        float4 p0, p1;
+        if (na <= 32) {
+          p0.x = __shfl_sync(0xffffffffu, own.x, pa);
+          p0.y = __shfl_sync(0xffffffffu, own.y, pa);
+          p0.z = __shfl_sync(0xffffffffu, own.z, pa);
+          const uint32_t src1 = two ? pb : pa;
+          p1.x = __shfl_sync(0xffffffffu, own.x, src1);
+          p1.y = __shfl_sync(0xffffffffu, own.y, src1);
+          p1.z = __shfl_sync(0xffffffffu, own.z, src1);
         } else {
-          float4 paf;
-          if (na <= 32) {
-            paf.x = __shfl_sync(0xffffffffu, own.x, pa);
-            paf.y = __shfl_sync(0xffffffffu, own.y, pa);
-            paf.z = __shfl_sync(0xffffffffu, own.z, pa);
-          } else {
-            paf = a.pf[i];
+          p0 = a.pf[i0];
+          p1 = a.pf[i1];
+        }
+        // entries taken before candidate index lower_end form the lower half
+        const uint32_t low0 = off_self + pa, low1 = off_self + (two ? pb : pa);
+        const uint32_t self0 = ((i0 - S.part_base) << 5) | static_cast<uint32_t>(kImageCenter);
+        const uint32_t self1 = ((i1 - S.part_base) << 5) | static_cast<uint32_t>(kImageCenter);
+        const uint32_t base0 = (i0 - S.part_base) * slot;  // the host keeps npart * slot below 2^32
+        const uint32_t base1 = (i1 - S.part_base) * slot;
+        uint32_t cur0 = 0, half0 = 0, cur1 = 0, half1 = 0;
+        if (c0 > 0) {
+          cur0 = a.nbr_cnt[i0];
+          half0 = a.nbr_half[i0];
+          cur1 = a.nbr_cnt[i1];
+          half1 = a.nbr_half[i1];
+        }
+        for (uint32_t t0 = 0; t0 < mpad; t0 += 32) {
+          const float4 b = srel[t0 + lane];
+          const uint32_t ent = __float_as_uint(b.w);
+          const bool amb = (ent & kAmbiguousBit) != 0;
+          const float ax = p0.x - b.x, ay = p0.y - b.y, az = p0.z - b.z;
+          const float bx = p1.x - b.x, by = p1.y - b.y, bz = p1.z - b.z;
+          const float d0 = fmaf(ax, ax, fmaf(ay, ay, az * az));
+          const float d1 = fmaf(bx, bx, fmaf(by, by, bz * bz));
+          bool hit0 = d0 < nb_lo && d0 > nb_zero && !amb;
+          bool hit1 = two && d1 < nb_lo && d1 > nb_zero && !amb;
+          const bool may0 = !hit0 && d0 <= nb_hi && ent != self0;
+          const bool may1 = two && !hit1 && d1 <= nb_hi && ent != self1;
+          if (__any_sync(0xffffffffu, may0 || may1)) {
+            if (may0) hit0 = exact_neighbor_test(S, a, i0, ent);
+            if (may1) hit1 = exact_neighbor_test(S, a, i1, ent);
           }
-          const uint32_t self_ent = ((i - S.part_base) << 5) | static_cast<uint32_t>(kImageCenter);
-          uint32_t cnt = 0, mymask = 0, half = 0;
-          uint32_t cursor = 0;
-          if (FILL) cursor = a.nbr_cursor[i];
-          for (uint32_t t0 = 0; t0 < m; t0 += 32) {
-            const uint32_t t = t0 + lane;
-            float4 b = make_float4(1.0e18f, 1.0e18f, 1.0e18f, __uint_as_float(kInvalid));
-            if (t < m) b = srel[t];
-            const uint32_t ent = __float_as_uint(b.w);
-            const float dx = paf.x - b.x, dy = paf.y - b.y, dz = paf.z - b.z;
-            const float d2f = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            bool hit = d2f < nb_lo && d2f > nb_zero && !(ent & kAmbiguousBit);
-            const bool maybe = !hit && d2f <= nb_hi && ent != self_ent;
-            if (__any_sync(0xffffffffu, maybe)) {
-              if (maybe) hit = exact_neighbor_test(S, a, i, ent);
-            }
-            const unsigned mask = __ballot_sync(0xffffffffu, hit);
-            if (FILL) {
-              if (hit) a.nbr[S.list_base + cursor + __popc(mask & lt)] = ent & ~kAmbiguousBit;
-              cursor += __popc(mask);
-              const uint32_t gbase = c0 + t0;
-              if (gbase < lower_end)
-                half += __popc(lower_end - gbase >= 32u ? mask : (mask & ((1u << (lower_end - gbase)) - 1u)));
-            } else {
-              cnt += __popc(mask);
-              if (lane == t0 / 32) mymask = mask;
-            }
+          const unsigned m0 = __ballot_sync(0xffffffffu, hit0);
+          const unsigned m1 = __ballot_sync(0xffffffffu, hit1);
+          const uint32_t e = ent & ~kAmbiguousBit;
+          const uint32_t q0 = cur0 + __popc(m0 & lt);
+          const uint32_t q1 = cur1 + __popc(m1 & lt);
+          if (hit0 && q0 < slot) {
+            if (buffered) sbuf0[q0] = e;
+            else seg[base0 + q0] = e;
           }
-          if (!FILL) {
-            if (use_masks && lane < nsub) maskp[lane] = mymask;
-            if (lane == 0) a.nbr_cnt[i] = (c0 == 0 ? 0u : a.nbr_cnt[i]) + cnt;
-            cell_total += cnt;
-          } else if (lane == 0) {
-            a.nbr_cursor[i] = cursor;
-            a.nbr_half[i] = (c0 == 0 ? 0u : a.nbr_half[i]) + half;
+          if (hit1 && q1 < slot) {
+            if (buffered) sbuf1[q1] = e;
+            else seg[base1 + q1] = e;
+          }
+          // the lower half ends at candidate lower_end, inside exactly one ballot
+          const uint32_t w0 = low0 - (c0 + t0), w1 = low1 - (c0 + t0);
+          if (w0 < 32u) half0 = cur0 + __popc(m0 & ((1u << w0) - 1u));
+          if (w1 < 32u) half1 = cur1 + __popc(m1 & ((1u << w1) - 1u));
+          cur0 += __popc(m0);
+          cur1 += __popc(m1);
+        }
+        finish_particle(a, seg, sbuf0, buffered, i0, base0, slot, cur0, half0, c0 == 0, lane);
+        if (two) finish_particle(a, seg, sbuf1, buffered, i1, base1, slot, cur1, half1, c0 == 0, lane);
+        if (last_round) {
+          acc_max = max(acc_max, cur0);
+          acc_sum += cur0;
+          if (two) {
+            acc_max = max(acc_max, cur1);
+            acc_sum += cur1;
           }
         }
       }
-      __syncwarp();
     }
-    if (!FILL && lane == 0) a.cell_nbr_tot[c] = cell_total;
   }
+  if (lane == 0) flush_list_stats(st, sys, acc_s, acc_max, acc_sum);
 }
 
-// Segment capacity check after the per-cell scan.
-__global__ void k_nbr_check(int nsys, const SysDesc* __restrict__ sys, SysState* st, const DevArrays a) {
-  if (*a.any_rebuild == 0) return;
+// Clears the per-build list statistics of the flagged systems.
+__global__ void k_nbr_reset(int nsys, SysState* st, const unsigned int* any) {
+  if (*any == 0) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsys || !st[s].rebuild) return;
-  const SysDesc& S = sys[s];
-  if (S.ncells == 0) return;
-  const unsigned long long tot = a.cell_nbr_off[S.cell_base + S.ncells] - a.cell_nbr_off[S.cell_base];
-  st[s].list_used = tot;
-  if (tot > S.list_cap) atomicOr(&st[s].error, kErrListOverflow);
+  st[s].list_used = 0;
+  st[s].max_nbr = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -761,29 +767,18 @@ int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevA
   return 2;
 }
 
-int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int cap,
-                     cudaStream_t stream, int mode) {
+int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int cap, int lbuf,
+                     cudaStream_t stream) {
   if (ex.n_cells == 0) return 0;
-  int count = 0;
-  const size_t smem = static_cast<size_t>(4) * cap * sizeof(float4);
+  const size_t smem = static_cast<size_t>(cap) * sizeof(float4) + static_cast<size_t>(4) * 2 * lbuf * sizeof(uint32_t);
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_neighbors<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_neighbors<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_neighbors, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     attr_set = true;
   }
-  const int wg = warp_grid(ex.n_cells, 4, ex.sm_count);
-  if (mode & 1) {
-    k_neighbors<false><<<wg, 128, smem, stream>>>(ex.n_cells, sys, st, a, cap);
-    count += 2 + launch_scan_u32_to_u64(a.cell_nbr_tot, a.cell_nbr_off, ex.n_cells, a.scan_blocks, stream,
-                                        a.any_rebuild);
-    k_nbr_check<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, sys, st, a);
-  }
-  if (mode & 2) {
-    k_neighbors<true><<<wg, 128, smem, stream>>>(ex.n_cells, sys, st, a, cap);
-    ++count;
-  }
-  return count;
+  k_nbr_reset<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild);
+  k_neighbors<<<warp_grid(ex.n_cells, 1, ex.sm_count), 128, smem, stream>>>(ex.n_cells, sys, st, a, cap, lbuf);
+  return 2;
 }
 
 }  // namespace xnb

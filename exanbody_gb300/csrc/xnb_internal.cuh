@@ -18,10 +18,11 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "xnb_widen.h"
+
 namespace xnb {
 
 constexpr int kImageCenter = 13;  // image code of the unshifted image: (0+1) + 3*(0+1) + 9*(0+1)
-constexpr uint32_t kMaskWords = 24;  // neighbour-build ballots kept per particle (768 candidates)
 
 enum ErrorBits : uint32_t {
   kErrListOverflow = 1u << 0,   // neighbour list segment too small
@@ -61,17 +62,20 @@ struct SysDesc {
   int32_t amr_enabled;
   uint32_t cell_base, ncells;
   uint32_t part_base, npart;
-  uint64_t list_base, list_cap;
+  uint64_t list_base;  // first entry of the system's list segment
+  uint32_t list_slot;  // entries reserved per particle: particle i's list starts at (i - part_base) * list_slot
 };
 
 // Per-system mutable state, device resident (SysState[nsys]).
 struct SysState {
   unsigned long long moved;     // particles over the displacement threshold (this step)
-  unsigned long long list_used; // entries of the current neighbour lists
+  unsigned long long list_used; // entries of the current neighbour lists (sum of counts)
   uint32_t rebuild;             // 1 when the rebuild path must run for this system
   uint32_t error;               // ErrorBits
   uint32_t max_cell;            // largest cell occupancy after the last rebin
   uint32_t rebuild_armed;        // 1 once backup_r has run (the trigger needs a backup)
+  uint32_t max_nbr;              // largest per-particle list count of the last build
+  uint32_t pad_;
   unsigned long long rebuilds;
 };
 
@@ -99,13 +103,9 @@ struct DevArrays {
   uint32_t* cell_cnt;              // per-cell scratch counts
   uint32_t* cell_stay;             // staying particles per cell
   uint32_t* cell_nmov;             // movers leaving each cell
-  unsigned long long* cell_nbr_off;// per-cell neighbour-entry offset (scan scratch)
-  uint32_t* cell_nbr_tot;          // per-cell neighbour-entry totals
   // neighbour lists
-  uint32_t* nbr_start;             // per particle, relative to its system segment
+  uint32_t* nbr_start;             // per particle, relative to its system segment ((i - part_base) * list_slot)
   uint32_t* nbr_cnt;               // per particle
-  uint32_t* nbr_cursor;            // per particle fill cursor (scratch)
-  uint32_t* nbr_masks;             // per particle kMaskWords candidate ballots (scratch)
   uint32_t* nbr_half;              // per particle: entries before it in the reference order
                                    // ((cell_b, p_b) < (cell_a, p_a)), the Newton half list
   uint32_t* nbr;                   // all segments
@@ -177,6 +177,10 @@ __device__ __forceinline__ float image_coord_f(float x, float period, int d) {
 __device__ __forceinline__ double image_coord(double x, double period, int d) {
   // apply_coord_modifier: x + (SIDE ? 1.0 : -1.0) * (rmax - rmin) when shifted, x otherwise
   return d == 1 ? x : __dadd_rn(x, __dmul_rn(d == 2 ? 1.0 : -1.0, period));
+}
+
+__device__ __forceinline__ double widen_f32(float f) {
+  return __longlong_as_double(static_cast<long long>(widen_f32_bits(__float_as_uint(f))));
 }
 
 }  // namespace xnb

@@ -41,10 +41,11 @@ int launch_clear_moved(const Extent& ex, SysState* st, cudaStream_t stream);
 int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream);
 // backup_r alone.
 int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream);
-// chunk_neighbors for systems with rebuild != 0. mode bit 1: count pass, scan
-// and segment check; bit 2: fill pass.
+// chunk_neighbors for systems with rebuild != 0: one pass writing each list
+// into its particle's slot (statistics reset + build, two kernels). lbuf: the
+// per-warp shared-memory list buffer in entries (slots up to lbuf are buffered).
 int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int stage_cap,
-                      cudaStream_t stream, int mode);
+                     int lbuf, cudaStream_t stream);
 
 // Exclusive scan of u32 counts into u64 offsets (n elements; out has n+1 entries).
 // With gate != nullptr the kernels return at once while *gate == 0.

@@ -110,6 +110,72 @@ __device__ __forceinline__ double rcp_nr(double d) {
 }
 
 // ---------------------------------------------------------------------------
+// FP32 prefilter of a window of up to 128 list entries [kw, kend): bit k - kw of
+// the four mask words is set for each entry whose FP32 distance to the particle
+// (mirror paf) may lie within rc (pre_hi = rc^2 + proven margin); unmarked
+// entries are provably beyond rc. Entries are read 8 at a time with two 16-byte
+// loads (each list starts on a 32-byte boundary, its slot is a multiple of 8
+// entries) and the 8 position gathers are independent of one another, so they
+// are in flight together. Positions past kend gather the particle's own mirror.
+struct Marks {
+  uint32_t w[4];
+};
+
+__device__ __forceinline__ Marks prefilter_window(const uint32_t* __restrict__ L, uint32_t kw, uint32_t kend,
+                                                  const float4* __restrict__ pf, uint32_t pbase, uint32_t self_e,
+                                                  float4 paf, float pfx, float pfy, float pfz, float pre_hi) {
+  Marks m{{0u, 0u, 0u, 0u}};
+  for (uint32_t kb = kw; kb < kend; kb += 8) {
+    const uint4 ea = __ldg(reinterpret_cast<const uint4*>(L + kb));
+    const uint4 eb = __ldg(reinterpret_cast<const uint4*>(L + kb + 4));
+    const uint32_t ev[8] = {ea.x, ea.y, ea.z, ea.w, eb.x, eb.y, eb.z, eb.w};
+    uint32_t bits = 0;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const bool valid = kb + static_cast<uint32_t>(t) < kend;
+      const uint32_t e = valid ? ev[t] : self_e;
+      const uint32_t code = e & 31u;
+      const float4 pbf = __ldg(pf + pbase + (e >> 5));
+      float bx = pbf.x, by = pbf.y, bz = pbf.z;
+      if (code != static_cast<uint32_t>(kImageCenter)) {
+        bx = image_coord_f(bx, pfx, static_cast<int>(code % 3u));
+        by = image_coord_f(by, pfy, static_cast<int>((code / 3u) % 3u));
+        bz = image_coord_f(bz, pfz, static_cast<int>(code / 9u));
+      }
+      const float ex = bx - paf.x, ey = by - paf.y, ez = bz - paf.z;
+      if (valid && fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= pre_hi) bits |= 1u << t;
+    }
+    const uint32_t off = kb - kw;
+    const uint32_t sh = off & 31u;
+    if (off < 32u) m.w[0] |= bits << sh;
+    else if (off < 64u) m.w[1] |= bits << sh;
+    else if (off < 96u) m.w[2] |= bits << sh;
+    else m.w[3] |= bits << sh;
+  }
+  return m;
+}
+
+// Next marked entry of a window in list order (offset into the window), or false.
+__device__ __forceinline__ bool next_mark(Marks& m, uint32_t& b) {
+  if (m.w[0]) {
+    b = static_cast<uint32_t>(__ffs(m.w[0]) - 1);
+    m.w[0] &= m.w[0] - 1u;
+  } else if (m.w[1]) {
+    b = 32u + static_cast<uint32_t>(__ffs(m.w[1]) - 1);
+    m.w[1] &= m.w[1] - 1u;
+  } else if (m.w[2]) {
+    b = 64u + static_cast<uint32_t>(__ffs(m.w[2]) - 1);
+    m.w[2] &= m.w[2] - 1u;
+  } else if (m.w[3]) {
+    b = 96u + static_cast<uint32_t>(__ffs(m.w[3]) - 1);
+    m.w[3] &= m.w[3] - 1u;
+  } else {
+    return false;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
 // zero_particle_force + lennard_jones_force over the neighbour lists.
 // compute_cell_particle_pairs_cell (compute/include/exanb/compute/
 // compute_cell_particle_pairs_impl_default.h:148-238) walks each particle's
@@ -124,7 +190,10 @@ __device__ __forceinline__ double rcp_nr(double d) {
 //   P = kMixed     : FP64 displacement and FP64 accumulation; r^2, r^-6 and the
 //                    force magnitude in FP32; the cutoff decision is made in FP32
 //                    where a proven margin allows and in FP64 otherwise, so the
-//                    pair set is the FP64 one.
+//                    pair set is the FP64 one. The displacement is applied
+//                    once per particle (sum pd*r_b - r_a*sum pd, all in FP64)
+//                    and the FP32 factor is widened on the integer pipes: a
+//                    pair costs 3 DFMA + 1 DADD on the FP64 pipe.
 template <int P, bool PE, bool KICK>
 __global__ void __launch_bounds__(256)
     k_force(uint32_t n_part, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a,
@@ -146,33 +215,18 @@ __global__ void __launch_bounds__(256)
     const float4 pal = (P == kMixed) ? a.pflo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float pre_hi = S.rc2_f + S.pre_margin_f;
     const float pfx = S.period_f[0], pfy = S.period_f[1], pfz = S.period_f[2];
-    double fx = 0.0, fy = 0.0, fz = 0.0, pe = 0.0;
-    uint32_t k = 0;
-    for (;;) {
-      // FP32 prefilter: each lane skips, on its own, the entries provably beyond
-      // rc, so the warp runs the FP64 block below once per in-range entry of
-      // its busiest lane rather than once per list entry.
-      uint32_t j = 0, code = 0;
-      bool found = false;
-      while (k < n) {
-        const uint32_t e = __ldg(L + k);
-        ++k;
-        j = pbase + (e >> 5);
-        code = e & 31u;
-        const float4 pbf = __ldg(a.pf + j);
-        float bx = pbf.x, by = pbf.y, bz = pbf.z;
-        if (code != static_cast<uint32_t>(kImageCenter)) {
-          bx = image_coord_f(bx, pfx, static_cast<int>(code % 3u));
-          by = image_coord_f(by, pfy, static_cast<int>((code / 3u) % 3u));
-          bz = image_coord_f(bz, pfz, static_cast<int>(code / 9u));
-        }
-        const float ex = bx - paf.x, ey = by - paf.y, ez = bz - paf.z;
-        if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= pre_hi) {
-          found = true;
-          break;
-        }
-      }
-      if (!found) break;
+    double fx = 0.0, fy = 0.0, fz = 0.0, pe = 0.0, psum = 0.0;
+    const uint32_t self_e = ((i - pbase) << 5) | static_cast<uint32_t>(kImageCenter);
+    // Windows of 128 entries: the FP32 prefilter marks the entries that may lie
+    // within rc, then the FP64 block runs for the marked ones in list order, so
+    // a warp executes it as often as its busiest lane has marked entries.
+    for (uint32_t kw = 0; kw < n; kw += 128) {
+     Marks mk = prefilter_window(L, kw, min(n, kw + 128u), a.pf, pbase, self_e, paf, pfx, pfy, pfz, pre_hi);
+     uint32_t b;
+     while (next_mark(mk, b)) {
+      const uint32_t e = __ldg(L + kw + b);
+      const uint32_t j = pbase + (e >> 5);
+      const uint32_t code = e & 31u;
       double xb = __ldg(a.rx + j), yb = __ldg(a.ry + j), zb = __ldg(a.rz + j);
       if (code != static_cast<uint32_t>(kImageCenter)) {
         xb = image_coord(xb, px, static_cast<int>(code % 3u));
@@ -244,21 +298,29 @@ __global__ void __launch_bounds__(256)
           in = (d2 > 0.0 && d2 <= rcut2);
         }
         if (in) {
-          // the force vector uses the FP64 displacement
-          const double dx = __dsub_rn(xb, xa);
-          const double dy = __dsub_rn(yb, ya);
-          const double dz = __dsub_rn(zb, za);
+          // FP64 displacement folded into the FP64 accumulation:
+          //   sum_b pd_b (r_b - r_a) = sum_b pd_b r_b - r_a sum_b pd_b,
+          // so a pair costs 3 DFMA + 1 DADD instead of 3 DADD + 3 DFMA; the
+          // subtraction happens once per particle below (cancellation error
+          // <= ~u_64 |r| sum|pd|, about 1e-12 of |F| at box sizes of 10^3 sigma).
           const float ir2 = __frcp_rn(r2);
           const float s2 = S.sig2_f * ir2;
           const float s6 = s2 * s2 * s2;
           const float pd = S.eps24_f * s6 * fmaf(-2.0f, s6, 1.0f) * ir2;
-          const double pdd = static_cast<double>(pd);
-          fx = fma(pdd, dx, fx);
-          fy = fma(pdd, dy, fy);
-          fz = fma(pdd, dz, fz);
+          const double pdd = widen_f32(pd);  // exact, on the integer pipes
+          fx = fma(pdd, xb, fx);
+          fy = fma(pdd, yb, fy);
+          fz = fma(pdd, zb, fz);
+          psum += pdd;
           if (PE) pe += static_cast<double>(0.5f * fmaf(S.eps4_f * s6, s6 - 1.0f, -S.e_shift_f));
         }
       }
+     }
+    }
+    if (P == kMixed) {
+      fx = fma(-xa, psum, fx);
+      fy = fma(-ya, psum, fy);
+      fz = fma(-za, psum, fz);
     }
     // the force field was zeroed (zero_particle_force.cu:39-46) and receives the sum
     fx = __dadd_rn(0.0, fx);
@@ -386,7 +448,7 @@ __global__ void __launch_bounds__(256)
           const float ir2 = __frcp_rn(r2);
           const float s2 = S.sig2_f * ir2;
           const float s6 = s2 * s2 * s2;
-          pd = static_cast<double>(S.eps24_f * s6 * fmaf(-2.0f, s6, 1.0f) * ir2);
+          pd = widen_f32(S.eps24_f * s6 * fmaf(-2.0f, s6, 1.0f) * ir2);
           if (PE) en = static_cast<double>(fmaf(S.eps4_f * s6, s6 - 1.0f, -S.e_shift_f));
         }
       }
@@ -480,18 +542,29 @@ __global__ void k_clear_moved(int nsys, SysState* st) {
   if (s < nsys) st[s].moved = 0;
 }
 
-inline int grid_for(uint32_t n, int threads, int sm_count, int per_sm) {
+// One thread per particle: the block scheduler balances the uneven per-particle
+// work and the last partial wave is one short block, not a third of the grid.
+inline int grid_for(uint32_t n, int threads) {
+  const long long g = (static_cast<long long>(n) + threads - 1) / threads;
+  return static_cast<int>(g < 1 ? 1 : g);
+}
+
+// Grid-stride launch of at most per_sm blocks per SM. The Newton traversal keeps
+// it: threads running together then hold particles far apart, so their FP64
+// reactions rarely meet on one address (one particle per thread made them
+// collide and cost ~25% on GB300).
+inline int grid_capped(uint32_t n, int threads, int sm_count, int per_sm) {
   const long long want = (static_cast<long long>(n) + threads - 1) / threads;
   const long long cap = static_cast<long long>(sm_count) * per_sm;
-  long long g = want < cap ? want : cap;
+  const long long g = want < cap ? want : cap;
   return static_cast<int>(g < 1 ? 1 : g);
 }
 
 template <int P, bool PE, bool KICK>
 void force_dispatch(const Extent& ex, const SysDesc* sys, const SysState* st, const DevArrays& a, int sys_only,
                     cudaStream_t stream) {
-  const int threads = ex.force_block > 0 ? ex.force_block : 256;
-  k_force<P, PE, KICK><<<grid_for(ex.n_part, threads, ex.sm_count, 8), threads, 0, stream>>>(ex.n_part, sys, st, a,
+  const int threads = ex.force_block > 0 ? ex.force_block : 128;
+  k_force<P, PE, KICK><<<grid_for(ex.n_part, threads), threads, 0, stream>>>(ex.n_part, sys, st, a,
                                                                                            sys_only);
 }
 
@@ -502,7 +575,7 @@ int launch_first_half(const Extent& ex, const SysDesc* sys, SysState* st, const 
                        int sys_only, cudaStream_t stream) {
   if (ex.n_part == 0) return 0;
   const int threads = 256;
-  const int g = grid_for(ex.n_part, threads, ex.sm_count, 8);
+  const int g = grid_for(ex.n_part, threads);
   if (exact)
     k_first_half<true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, do_push_r, do_push_v, do_trigger,
                                                   dt_scale_r, dt_scale_v, sys_only);
@@ -516,8 +589,8 @@ int launch_force(const Extent& ex, const SysDesc* sys, SysState* st, const DevAr
                   bool second_half, int sys_only, cudaStream_t stream, bool newton) {
   if (ex.n_part == 0) return 0;
   if (newton && precision != kFp64Exact) {
-    const int threads = ex.force_block > 0 ? ex.force_block : 256;
-    const int g = grid_for(ex.n_part, threads, ex.sm_count, 8);
+    const int threads = 256;
+    const int g = grid_capped(ex.n_part, threads, ex.sm_count, 8);
     k_zero_force<<<g, threads, 0, stream>>>(ex.n_part, st, a, sys_only, with_pe);
     if (precision == kFp64) {
       if (with_pe) k_force_half<kFp64, true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);

@@ -22,21 +22,21 @@ import numpy as np
 
 from . import workloads, xnb
 
-DEFAULTS = dict(stage_cap=640, force_block=256, skin=0.3, newton=False)
+DEFAULTS = dict(stage_cap=640, force_block=128, skin=0.3, newton=False)
 
 
 def make_systems(specs, rcut=2.5, skin=0.3):
     return [workloads.lj_fcc_system(sp["n"], sp["rho"], sp["T"], sp["seed"], rcut, skin) for sp in specs]
 
 
-def build_batch(systems, stage_cap=640, force_block=256, skin=0.3, rcut=2.5, dt=0.005, stream=None,
+def build_batch(systems, stage_cap=640, force_block=128, skin=0.3, rcut=2.5, dt=0.005, stream=None,
                 precision=xnb.PREC_MIXED, list_per_atom=None):
     n_atoms = sum(w["n_atoms"] for w in systems)
     n_cells = sum(int(np.prod(w["geom"]["dims"])) for w in systems)
     if list_per_atom is None:
         # neighbours within rc + skin at the densest state point of the batch, with margin
         rho = max(w["rho"] for w in systems)
-        list_per_atom = 1.3 * (4.0 / 3.0) * np.pi * (rcut + skin) ** 3 * rho + 16
+        list_per_atom = 1.6 * (4.0 / 3.0) * np.pi * (rcut + skin) ** 3 * rho + 24
     b = xnb.Batch(n_atoms + 64 * len(systems), n_cells + 64, int(list_per_atom * n_atoms) + 4096,
                   max_systems=len(systems), stage_cap=stage_cap, force_block=force_block)
     if stream is not None:

@@ -248,7 +248,7 @@ struct InitParticlesOp : OperatorNode {
       const double nb = p.rcut + p.rcut_inc;
       const double rho = static_cast<double>(n) / ((p.extent[0] - p.origin[0]) * (p.extent[1] - p.origin[1]) *
                                                    (p.extent[2] - p.origin[2]));
-      cfg.list_capacity = static_cast<int64_t>(1.6 * 4.18879 * nb * nb * nb * rho * static_cast<double>(n)) + 4096;
+      cfg.list_capacity = static_cast<int64_t>((2.0 * 4.18879 * nb * nb * nb * rho + 32.0) * static_cast<double>(n)) + 4096;
       ck(xnb_batch_create(&cfg, &ctx.batch), "xnb_batch_create");
     }
     ck(xnb_system_add(ctx.batch, &p, n, h.rx.data(), h.ry.data(), h.rz.data(), h.vx.data(), h.vy.data(),

@@ -27,7 +27,7 @@ import numpy as np
 
 from . import workloads, xnb
 
-BYTES_LIST_PER_ATOM = 130.0  # neighbour entries reserved per atom for admission (rho <= 1, x1.25 margin)
+BYTES_LIST_PER_ATOM = 160.0  # neighbour slot entries per atom for admission (rho <= 1, x1.25 margin)
 
 
 def request_system(req):

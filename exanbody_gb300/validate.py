@@ -41,7 +41,7 @@ def run(w, steps, every, stream):
     out = {}
     mixed_state = None
     for name, prec in (("mixed", xnb.PREC_MIXED), ("fp64", xnb.PREC_FP64)):
-        b = xnb.Batch(N + 64, ncell + 64, int(N * 120) + 4096)
+        b = xnb.Batch(N + 64, ncell + 64, int(N * 160) + 4096)
         b.stream = ctypes.c_void_p(stream.cuda_stream)
         s = b.add_system(xnb.lj_params(g), w["r"], w["v"], w["id"], list_factor=1.2)
         b.init_particles(s, prec)

@@ -75,7 +75,7 @@ class SystemInfo(C.Structure):
         ("error_bits", C.c_uint32),
         ("max_cell", C.c_uint32),
         ("active", C.c_int32),
-        ("reserved", C.c_int32),
+        ("max_nbr", C.c_uint32),
     ]
 
 

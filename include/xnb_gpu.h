@@ -86,19 +86,19 @@ typedef struct xnb_batch_config {
   int64_t cell_capacity;     /* cells over all resident systems */
   int64_t list_capacity;     /* neighbour entries over all resident systems */
   int32_t stage_cap;         /* neighbour-build staging candidates per warp; 0 = default (640) */
-  int32_t force_block;       /* threads per block of the force traversal; 0 = default (256) */
+  int32_t force_block;       /* threads per block of the full-list force traversal; 0 = default (128) */
 } xnb_batch_config;
 
 typedef struct xnb_system_info {
   int64_t n_particles;
   int64_t n_cells;
-  int64_t list_used;
-  int64_t list_cap;
+  int64_t list_used;  /* neighbour entries of the current lists (sum of the counts) */
+  int64_t list_cap;   /* entries reserved: n_particles * per-particle slot */
   int64_t rebuilds;   /* neighbour-list rebuilds since xnb_init_particles */
   uint32_t error_bits;
   uint32_t max_cell;  /* largest cell occupancy after the last rebin */
   int32_t active;
-  int32_t reserved;
+  uint32_t max_nbr;   /* largest per-particle list count of the last build */
 } xnb_system_info;
 
 const char* xnb_last_error_string(void);
@@ -108,15 +108,17 @@ int xnb_version(void);
 int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out);
 int xnb_batch_destroy(xnb_batch* b);
 /* Bytes of device memory a system of n particles and ncells cells needs, with
- * list_per_particle neighbour entries per particle (admission control). */
+ * a neighbour slot of list_per_particle entries per particle (admission control). */
 int64_t xnb_system_bytes(int64_t n, int64_t ncells, double list_per_particle);
 
 /* Upload one system. cell_counts == NULL: particles are placed in the cell of
  * their periodic location, in input order (stable). Otherwise the arrays are
  * given per interior cell (linear order (k*Dj+j)*Di+i) as the reference grid
  * holds them, and positions may lie outside their cell (the reference's
- * lattice generator then relies on init's move_particles). list_factor scales
- * the neighbour segment reserved at init (>= 1; 0 = 1.3). */
+ * lattice generator then relies on init's move_particles). Each particle's
+ * neighbour list has a fixed slot; a host-synchronised build sizes the slot to
+ * list_factor x the largest count + 16 (>= 1; 0 = 1.3), and a build without
+ * host synchronisation that outgrows it flags XNB_ERRBIT_LIST_OVERFLOW. */
 int xnb_system_add(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double* rx, const double* ry,
                    const double* rz, const double* vx, const double* vy, const double* vz, const uint64_t* id,
                    const int64_t* cell_counts, double list_factor, void* stream, int32_t* sys_out);

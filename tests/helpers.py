@@ -13,7 +13,7 @@ def oracle_threads():
     return max(1, os.cpu_count() or 1)
 
 
-def new_batch(systems_atoms, systems_cells, list_per_atom=110.0, max_systems=None):
+def new_batch(systems_atoms, systems_cells, list_per_atom=170.0, max_systems=None):
     P = int(sum(systems_atoms)) + 64
     Cc = int(sum(systems_cells)) + 64
     L = int(list_per_atom * P) + 4096

@@ -32,7 +32,7 @@ def test_serving_results_equal_alone_and_admission_by_budget():
     assert len([r for r in rec.values() if "latency" in r]) == len(reqs)
     assert ast == sum(w["n_atoms"] * r["steps"] for w, r in zip(built, reqs))
     for k, (w, r) in enumerate(zip(built, reqs)):
-        b = xnb.Batch(w["n_atoms"] + 64, int(np.prod(w["geom"]["dims"])) + 64, w["n_atoms"] * 130 + 4096)
+        b = xnb.Batch(w["n_atoms"] + 64, int(np.prod(w["geom"]["dims"])) + 64, w["n_atoms"] * 170 + 4096)
         s = b.add_system(xnb.lj_params(w["geom"]), w["r"], w["v"], w["id"], list_factor=1.25)
         b.init_particles(s, xnb.PREC_MIXED)
         b.step(r["steps"], xnb.PREC_MIXED, 0)

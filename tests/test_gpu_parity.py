@@ -146,7 +146,7 @@ def test_ni_golden_deck_on_gpu():
     counts = o.cell_counts()
     r = np.stack([P0["rx"], P0["ry"], P0["rz"]], 1)
     v = np.stack([P0["vx"], P0["vy"], P0["vz"]], 1)
-    b = new_batch([len(r)], [64], list_per_atom=130.0)
+    b = new_batch([len(r)], [64], list_per_atom=260.0)
     s = b.add_system(ni_deck_params(), r, v, P0["id"], cell_counts=counts)
     b.init_particles(s, xnb.PREC_FP64_EXACT)
     o.init()

@@ -1,0 +1,64 @@
+"""The force kernels widen the FP32 pair-force factor to FP64 with integer
+operations (exanbody_gb300/csrc/xnb_widen.h). The same header compiled for the
+host must agree bit for bit with the C++ float -> double conversion: every
+subnormal, every exponent with a stride through the fraction, zeros, infinities
+and NaNs (NaN: any NaN with the same sign)."""
+import os
+import shutil
+import subprocess
+import tempfile
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "exanbody_gb300", "csrc")
+
+CHECK = r"""
+#include <cstdio>
+#include <cstring>
+#include "xnb_widen.h"
+static unsigned long long bad = 0, tested = 0;
+static void one(uint32_t u) {
+  float f; std::memcpy(&f, &u, 4);
+  const double d = static_cast<double>(f);
+  uint64_t want; std::memcpy(&want, &d, 8);
+  const uint64_t got = xnb::widen_f32_bits(u);
+  ++tested;
+  if ((u & 0x7f800000u) == 0x7f800000u && (u & 0x7fffffu)) {
+    const bool ok = (got & 0x7ff0000000000000ull) == 0x7ff0000000000000ull && (got & 0xfffffffffffffull) &&
+                    (got >> 63) == (u >> 31);
+    bad += !ok;
+    return;
+  }
+  if (got != want) {
+    if (bad < 5) std::printf("mismatch u=%08x got=%016llx want=%016llx\n", u, (unsigned long long)got,
+                             (unsigned long long)want);
+    ++bad;
+  }
+}
+int main() {
+  for (uint32_t sign = 0; sign < 2; ++sign) {
+    for (uint32_t m = 0; m < (1u << 23); ++m) one((sign << 31) | m);             // zero and every subnormal
+    for (uint32_t e = 1; e < 256; ++e)
+      for (uint32_t m = 0; m < (1u << 23); m += 61) one((sign << 31) | (e << 23) | m);
+    for (uint32_t e = 1; e < 256; ++e) one((sign << 31) | (e << 23) | 0x7fffffu);
+  }
+  std::printf("tested %llu mismatches %llu\n", tested, bad);
+  return bad != 0;
+}
+"""
+
+
+def test_widen_matches_cast():
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "widen_check.cpp")
+        exe = os.path.join(d, "widen_check")
+        with open(src, "w") as f:
+            f.write(CHECK)
+        subprocess.check_call([gxx, "-O2", "-std=c++17", "-I", CSRC, src, "-o", exe])
+        out = subprocess.run([exe], capture_output=True, text=True)
+        assert out.returncode == 0, out.stdout + out.stderr
+        assert "mismatches 0" in out.stdout
