@@ -237,6 +237,15 @@ SysDesc make_desc(const xnb_lj_params& p) {
   //  force cutoff test of the mixed path: each FP32 axis difference is within
   //  2u|d| of the FP64 one (converted, or compensated hi/lo), so
   //  |r2_f32 - d2_f64| <= 6 u d2; margin = 4x at rc^2 (+1 absolute guard so tiny d2 also go to FP64).
+  // FP32 cell index of the rebin: the mirror pf = fl32(x - origin) and
+  // fl32(1/cell_size) put pf * inv within 3.01 u |q| of the quotient q of the
+  // reference's division (|q| <= max dims + 2 before wrapping); a fraction farther
+  // than 4 u (max dims + 2) from an integer floors like the division does.
+  int dmax = 1;
+  for (int a = 0; a < 3; ++a) dmax = std::max(dmax, static_cast<int>(p.dims[a]));
+  d.inv_cell_f = static_cast<float>(1.0 / p.cell_size);
+  d.q_margin_f = static_cast<float>(4.0 * u * (dmax + 2.0));
+  d.inv_cell = 1.0 / p.cell_size;
   d.rc2_f = static_cast<float>(d.rcut2);
   d.rc_margin_f = static_cast<float>(4.0 * 6.0 * u * (d.rcut2 + 1.0));
   return d;
@@ -387,9 +396,9 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   b->device = cfg->device;
   b->cfg = *cfg;
   if (cfg->stage_cap > 0) b->stage_cap = (cfg->stage_cap + 31) / 32 * 32;
-  if (cfg->stage_cap > 2048) {
+  if (cfg->stage_cap > 1024) {
     delete b;
-    return fail(XNB_ERR_ARG, "stage_cap above 2048 candidates");
+    return fail(XNB_ERR_ARG, "stage_cap above 1024 candidates");
   }
   if (cfg->force_block > 0) {
     if (cfg->force_block % 32 || cfg->force_block > 256) {
@@ -713,7 +722,7 @@ int xnb_init_particles(xnb_batch* b, int32_t s, int32_t precision, void* stream)
   const Extent ex = b->extent();
   // init marks every selected system; the counter then starts from zero
   b->launches += launch_mark_rebuild(ex, b->d_st, 0, s, b->a.any_rebuild, st);
-  b->launches += launch_rebin(ex, b->d_sys, b->d_st, b->a, st);
+  b->launches += launch_rebin(ex, b->d_sys, b->d_st, b->a, st, precision == XNB_PREC_FP64_EXACT);
   rc = neighbors_sync(b, st);
   if (rc) return rc;
   b->launches += launch_force(ex, b->d_sys, b->d_st, b->a, precision, true, false, s, st, newton);
@@ -846,7 +855,7 @@ int xnb_step(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, voi
     }
     if (rebuild) {
       // update_particles_full
-      b->launches += launch_rebin(ex, b->d_sys, b->d_st, b->a, st);
+      b->launches += launch_rebin(ex, b->d_sys, b->d_st, b->a, st, exact);
       if (flags & XNB_STEP_HOST_SYNC) {
         int rc = neighbors_sync(b, st);
         if (rc) return rc;

@@ -46,6 +46,36 @@ __global__ void __launch_bounds__(256)
     const SysDesc& S = sys[s];
     int ci, cj, ck;
     cell_ijk(S, c - S.cell_base, ci, cj, ck);
+    {
+      // FP32 pre-decision from the position mirror: a particle whose quotient lies
+      // farther than q_margin_f from a cell boundary, inside the grid, gets the
+      // reference's cell without the FP64 division, and lies strictly inside it
+      // (distance to the cell bounds 0, no wrapping).
+      const float4 pq = a.pf[i];
+      const float qv[3] = {pq.x * S.inv_cell_f, pq.y * S.inv_cell_f, pq.z * S.inv_cell_f};
+      int lf[3];
+      bool sure = true;
+      for (int ax = 0; ax < 3; ++ax) {
+        const float fl = floorf(qv[ax]);
+        const float fr = qv[ax] - fl;
+        sure = sure && fr > S.q_margin_f && fr < 1.0f - S.q_margin_f && fl >= 0.0f &&
+               fl < static_cast<float>(S.dims[ax]);
+        lf[ax] = static_cast<int>(fl);
+      }
+      if (sure) {
+        if (lf[0] == ci && lf[1] == cj && lf[2] == ck) {
+          a.pdest[i] = c;
+        } else {
+          const int dd[3] = {pmod_i(lf[0] - ci, S.dims[0]), pmod_i(lf[1] - cj, S.dims[1]),
+                             pmod_i(lf[2] - ck, S.dims[2])};
+          for (int ax = 0; ax < 3; ++ax)
+            if (!(dd[ax] == 0 || dd[ax] == 1 || dd[ax] == S.dims[ax] - 1)) atomicOr(&st[s].error, kErrFarMover);
+          a.pdest[i] = (S.cell_base + static_cast<uint32_t>((lf[2] * S.dims[1] + lf[1]) * S.dims[0] + lf[0])) |
+                       kMoverBit;
+        }
+        continue;
+      }
+    }
     const double ro[3] = {a.rx[i], a.ry[i], a.rz[i]};
     double r[3] = {ro[0], ro[1], ro[2]};
     int loc[3];
@@ -318,10 +348,23 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// backup_r alone (io/backup_r.cpp:42-79) for flagged systems.
+// backup_r alone (io/backup_r.cpp:42-79) for flagged systems. EXACT = false
+// (the FP64 and mixed paths) keeps the backup position itself instead of its
+// 32-bit cell-relative encoding: the displacement trigger then differs from the
+// reference's by the encoding's quantum (cell_size / 2^32) at most.
+template <bool EXACT>
 __global__ void __launch_bounds__(256)
     k_backup(uint32_t n_part, const SysDesc* __restrict__ sys, SysState* st, DevArrays a) {
   if (*a.any_rebuild == 0) return;
+  if constexpr (!EXACT) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
+      const uint32_t c = a.pcell[i];
+      if (c == kInvalid || !sys_flagged(st, a.cell_sys[c])) continue;
+      a.rbx[i] = a.rx[i];
+      a.rby[i] = a.ry[i];
+      a.rbz[i] = a.rz[i];
+    }
+  } else {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
     const uint32_t c = a.pcell[i];
     if (c == kInvalid) continue;
@@ -331,13 +374,14 @@ __global__ void __launch_bounds__(256)
     int ci, cj, ck;
     cell_ijk(S, c - S.cell_base, ci, cj, ck);
     const double lo[3] = {cell_lo(S, 0, ci), cell_lo(S, 1, cj), cell_lo(S, 2, ck)};
-    const uint32_t bx = encode_u32(a.rx[i], lo[0], S.cell_size);
-    const uint32_t by = encode_u32(a.ry[i], lo[1], S.cell_size);
-    const uint32_t bz = encode_u32(a.rz[i], lo[2], S.cell_size);
+    const uint32_t bx = encode_u32(a.rx[i], lo[0], S.cell_size, S.inv_cell);
+    const uint32_t by = encode_u32(a.ry[i], lo[1], S.cell_size, S.inv_cell);
+    const uint32_t bz = encode_u32(a.rz[i], lo[2], S.cell_size, S.inv_cell);
     a.bkx[i] = bx; a.bky[i] = by; a.bkz[i] = bz;
     a.rbx[i] = restore_u32(bx, lo[0], S.cell_size);
     a.rby[i] = restore_u32(by, lo[1], S.cell_size);
     a.rbz[i] = restore_u32(bz, lo[2], S.cell_size);
+  }
   }
 }
 
@@ -443,7 +487,9 @@ __device__ __forceinline__ void finish_particle(const DevArrays& a, uint32_t* se
 // directly. A particle with more hits than the slot holds keeps its true count,
 // writes nothing past the slot and flags the system (kErrListOverflow); max_nbr
 // records the largest count for resizing.
-__global__ void __launch_bounds__(128)
+// 64 registers (8 blocks of 128 per SM): measured faster than the 90-register
+// schedule despite a few spills.
+__global__ void __launch_bounds__(128, 8)
     k_neighbors(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap, int lbuf) {
   if (*a.any_rebuild == 0) return;
   extern __shared__ float4 stage_all[];
@@ -561,6 +607,8 @@ __global__ void __launch_bounds__(128)
           cur1 = a.nbr_cnt[i1];
           half1 = a.nbr_half[i1];
         }
+        const uint32_t start0 = cur0, start1 = cur1;
+        uint32_t sv0 = 0, sv1 = 0;  // lane k keeps the ballots of the round's k-th step (<= 32 steps)
         for (uint32_t t0 = 0; t0 < mpad; t0 += 32) {
           const float4 b = srel[t0 + lane];
           const uint32_t ent = __float_as_uint(b.w);
@@ -590,12 +638,25 @@ __global__ void __launch_bounds__(128)
             if (buffered) sbuf1[q1] = e;
             else seg[base1 + q1] = e;
           }
-          // the lower half ends at candidate lower_end, inside exactly one ballot
-          const uint32_t w0 = low0 - (c0 + t0), w1 = low1 - (c0 + t0);
-          if (w0 < 32u) half0 = cur0 + __popc(m0 & ((1u << w0) - 1u));
-          if (w1 < 32u) half1 = cur1 + __popc(m1 & ((1u << w1) - 1u));
+          if ((t0 >> 5) == lane) {
+            sv0 = m0;
+            sv1 = m1;
+          }
           cur0 += __popc(m0);
           cur1 += __popc(m1);
+        }
+        // the lower half ends at candidate lower_end: hits of the earlier rounds
+        // plus, from the kept ballots, this round's hits below it
+        const uint32_t w0 = low0 - c0, w1 = low1 - c0;
+        if (w0 < m) {
+          const uint32_t v = lane < (w0 >> 5) ? __popc(sv0)
+                                             : (lane == (w0 >> 5) ? __popc(sv0 & ((1u << (w0 & 31u)) - 1u)) : 0u);
+          half0 = start0 + __reduce_add_sync(0xffffffffu, v);
+        }
+        if (w1 < m) {
+          const uint32_t v = lane < (w1 >> 5) ? __popc(sv1)
+                                             : (lane == (w1 >> 5) ? __popc(sv1 & ((1u << (w1 & 31u)) - 1u)) : 0u);
+          half1 = start1 + __reduce_add_sync(0xffffffffu, v);
         }
         finish_particle(a, seg, sbuf0, buffered, i0, base0, slot, cur0, half0, c0 == 0, lane);
         if (two) finish_particle(a, seg, sbuf1, buffered, i1, base1, slot, cur1, half1, c0 == 0, lane);
@@ -746,7 +807,8 @@ int launch_scan_u32_to_u64(const uint32_t* in, unsigned long long* out, uint32_t
   return 3;
 }
 
-int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream) {
+int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream,
+                 bool exact_backup) {
   if (ex.n_part == 0 || ex.n_cells == 0) return 0;
   k_rebin_dest<<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
   const int wg = warp_grid(ex.n_cells, 4, ex.sm_count);
@@ -755,14 +817,15 @@ int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevAr
   const int ns = launch_scan_u32_to_u64(a.cell_cnt, a.cell_scan, ex.n_cells, a.scan_blocks, stream, a.any_rebuild);
   k_rebin_scatter<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
   k_rebin_finalize<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
-  k_backup<<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
+  if (exact_backup) k_backup<true><<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
+  else k_backup<false><<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
   k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild);
   return 7 + ns;
 }
 
 int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream) {
   if (ex.n_part == 0) return 0;
-  k_backup<<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
+  k_backup<true><<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
   k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild);
   return 2;
 }

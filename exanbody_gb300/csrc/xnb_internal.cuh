@@ -56,6 +56,8 @@ struct SysDesc {
   float period_f[3];
   float outer_lo_f[3], outer_hi_f[3];
   float pre_margin_f, filter_margin_f;
+  float inv_cell_f, q_margin_f;  // FP32 cell-index pre-decision: 1/cell_size and its proven margin (cells)
+  double inv_cell;               // fl(1/cell_size): reciprocal pre-decision of the backup encoding
   double m24eps, eps4, sig2, eps24;  // -24*eps, 4*eps (lennard_jones.cu:54-55), sigma^2, 24*eps
   int32_t dims[3];
   int32_t divide_by_mass;
@@ -125,10 +127,24 @@ __device__ __forceinline__ double restore_u32(uint32_t x, double o, double r) {
   return __dadd_rn(o, __dmul_rn(__dmul_rn(static_cast<double>(x), r), 0x1p-32));
 }
 
-// encode_double_u32 (core/include/exanb/core/backup_r.h:36-51)
-__device__ __forceinline__ uint32_t encode_u32(double x, double o, double r) {
+// encode_double_u32 (core/include/exanb/core/backup_r.h:36-51). The quotient
+// (x - o) * 2^32 / r is first formed with the reciprocal rinv = fl(1/r): that
+// product lies within 2 ulp of the correctly rounded quotient, so when it is more
+// than 2^-18 (>= 4 ulp below 2^32) away from an integer both truncate to the same
+// value and the FP64 division is skipped; otherwise (and outside [0, 2^32)) the
+// division decides. The +-1 correction below is the reference's.
+__device__ __forceinline__ uint32_t encode_u32(double x, double o, double r, double rinv) {
   const double xo = __dsub_rn(x, o);
-  long long a = __double2ll_rz(__ddiv_rn(__dmul_rn(xo, 4294967296.0), r));
+  const double X = __dmul_rn(xo, 4294967296.0);  // exact (power of two)
+  const double qa = __dmul_rn(X, rinv);
+  const double t = trunc(qa);
+  const double fr = __dsub_rn(qa, t);
+  long long a;
+  if (qa >= 1.0 && qa < 4294967295.0 && fr > 0x1p-18 && fr < 1.0 - 0x1p-18) {
+    a = static_cast<long long>(t);
+  } else {
+    a = __double2ll_rz(__ddiv_rn(X, r));
+  }
   a = a < 0 ? 0 : a;
   a = a > 4294967295LL ? 4294967295LL : a;
   const uint32_t xa = static_cast<uint32_t>(a);

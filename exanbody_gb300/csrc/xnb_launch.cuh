@@ -38,7 +38,9 @@ int launch_mark_rebuild(const Extent& ex, SysState* st, int mode, int sys_only, 
 int launch_clear_moved(const Extent& ex, SysState* st, cudaStream_t stream);
 
 // move_particles + migrate + rebuild_amr + backup_r for systems with rebuild != 0.
-int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream);
+// exact_backup = false keeps the backup position unencoded (FP64 and mixed paths).
+int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream,
+                 bool exact_backup = true);
 // backup_r alone.
 int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream);
 // chunk_neighbors for systems with rebuild != 0: one pass writing each list

@@ -85,7 +85,7 @@ typedef struct xnb_batch_config {
   int64_t particle_capacity; /* particles over all resident systems */
   int64_t cell_capacity;     /* cells over all resident systems */
   int64_t list_capacity;     /* neighbour entries over all resident systems */
-  int32_t stage_cap;         /* neighbour-build staging candidates per warp; 0 = default (640) */
+  int32_t stage_cap;         /* neighbour-build candidates staged per cell round (<= 1024); 0 = default (640) */
   int32_t force_block;       /* threads per block of the full-list force traversal; 0 = default (128) */
 } xnb_batch_config;
 
