@@ -39,9 +39,22 @@ sys.path.insert(0, ROOT)
 FLOP64_PER_ATOM_FP64_PATH = 669.6
 FLOP64_PER_ATOM_MIXED = 282.2
 FLOP32_PER_ATOM_MIXED = 387.4
+# DRAM bytes (read + write) per atom of one mixed k_force launch, from an ncu capture of
+# the 256,000-atom case of this workload (profiles/k_force_mixed_lj256k.md); traffic grows
+# with the atom count at fixed density, so a launch moves this many bytes per atom.
+FORCE_DRAM_BYTES_PER_ATOM = 546.0
 
 WORKLOAD = dict(n=100, rho=0.8442, T=1.44, seed=12345, rcut=2.5, skin=0.3, dt=0.005)
 METRIC = "atom-steps/s, 4M-atom LJ MD step (mixed precision; FP64 path and force error reported beside it)"
+
+
+def hbm_peak_gbs():
+    """Measured HBM copy bandwidth of this machine's GB300 (MEASURED_PEAKS.json), else 6800."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
 
 
 def config_of(n, atoms, **extra):
@@ -386,7 +399,12 @@ def run_ours(args):
                          "unit": "TFLOP/s", "frac": achieved / peak64,
                          "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
                          "ms_per_launch": ms_force, "ms_per_launch_fp64_kernel": ms_force64,
-                         "traffic": None},
+                         "traffic": FORCE_DRAM_BYTES_PER_ATOM * N,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per atom on the "
+                                           "256,000-atom case, scaled to %d atoms" % N,
+                         "hbm": {"achieved_gbs": FORCE_DRAM_BYTES_PER_ATOM * N / (ms_force * 1e-3) / 1e9,
+                                 "peak_gbs": hbm_peak_gbs(),
+                                 "frac": FORCE_DRAM_BYTES_PER_ATOM * N / (ms_force * 1e-3) / 1e9 / hbm_peak_gbs()}},
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
