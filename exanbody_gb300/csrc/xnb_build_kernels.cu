@@ -560,21 +560,28 @@ __global__ void __launch_bounds__(128, 8)
       const uint32_t m = c1 - c0;
       const uint32_t mpad = (m + 31u) & ~31u;  // <= cap (a multiple of 32)
       __syncthreads();  // the previous round's readers are done with srel
-      for (int g = 0; g < 27; ++g) {
+      // every thread of the block stages candidates t, t + blockDim, ...; the group
+      // of candidate u is the last g with g_off[g] <= u (binary search over lanes
+      // 0..26; empty groups share their successor's offset and are skipped by it)
+      for (uint32_t t0 = 0; t0 < mpad; t0 += blockDim.x) {
+        const uint32_t t = t0 + threadIdx.x;
+        const uint32_t u = c0 + t;
+        uint32_t g = 0;
+        for (uint32_t step = 16; step > 0; step >>= 1) {
+          const uint32_t probe = g + step;
+          const uint32_t po = __shfl_sync(0xffffffffu, g_off, probe < 27u ? probe : 26u);
+          if (probe < 27u && po <= u) g = probe;
+        }
         const uint32_t gs = __shfl_sync(0xffffffffu, g_start, g);
-        const uint32_t gn = __shfl_sync(0xffffffffu, g_n, g);
         const uint32_t go = __shfl_sync(0xffffffffu, g_off, g);
         const uint32_t gc = __shfl_sync(0xffffffffu, g_code, g);
-        if (go + gn <= c0 || go >= c1) continue;
-        for (uint32_t q = threadIdx.x; q < gn; q += blockDim.x) {
-          const uint32_t t = go + q;
-          if (t < c0 || t >= c1) continue;
-          srel[t - c0] = stage_candidate(S, a, gs + q, gc);
+        if (t < m) {
+          srel[t] = stage_candidate(S, a, gs + (u - go), gc);
+        } else if (t < mpad) {
+          // padding up to a whole ballot: unreachable dummies, so the test needs no bound check
+          srel[t] = make_float4(1.0e18f, 1.0e18f, 1.0e18f, __uint_as_float(kInvalid));
         }
       }
-      // padding up to a whole ballot: unreachable dummies, so the test needs no bound check
-      for (uint32_t t = m + threadIdx.x; t < mpad; t += blockDim.x)
-        srel[t] = make_float4(1.0e18f, 1.0e18f, 1.0e18f, __uint_as_float(kInvalid));
       __syncthreads();
       const bool last_round = c1 == ncand;
       for (uint32_t pa = wib; pa < na; pa += 2 * nwarp) {
