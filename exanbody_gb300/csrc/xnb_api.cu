@@ -99,6 +99,8 @@ struct xnb_batch {
   SysDesc* d_sys = nullptr;
   SysState* d_st = nullptr;
   SysState* h_st = nullptr;  // pinned mirror
+  unsigned int* d_flag = nullptr;             // scratch error flag of the stream writer
+  unsigned long long* d_counts = nullptr;     // scratch counters of the stream checker
   std::vector<SysHost> sys;
   RangeAlloc parts, cells, lists;
   std::vector<void*> allocs;
@@ -433,6 +435,8 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   rc = rc ? rc : dalloc(b, &a.nbr, L);
   rc = rc ? rc : dalloc(b, &b->d_sys, static_cast<uint64_t>(cfg->max_systems));
   rc = rc ? rc : dalloc(b, &b->d_st, static_cast<uint64_t>(cfg->max_systems));
+  rc = rc ? rc : dalloc(b, &b->d_flag, 1);
+  rc = rc ? rc : dalloc(b, &b->d_counts, 8);
   if (!rc && cudaMallocHost(&b->h_st, sizeof(SysState) * cfg->max_systems) != cudaSuccess)
     rc = fail(XNB_ERR_NOMEM, "cudaMallocHost failed");
   if (rc) {
@@ -923,6 +927,66 @@ int xnb_check_errors(xnb_batch* b, void* stream) {
     if (e) return fail(XNB_ERR_DEVICE, "device error bits " + std::to_string(e) + " in system " + std::to_string(q));
   }
   return XNB_OK;
+}
+
+int xnb_chunk_neighbors_stream(xnb_batch* b, int32_t s, int32_t offset_tables, uint16_t* stream, int64_t cap,
+                               uint64_t* cell_offsets, int64_t* total_out, void* cuda_stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0) return fail(XNB_ERR_ARG, "streams are built for one system");
+  if (offset_tables < 0 || offset_tables > 2) return fail(XNB_ERR_ARG, "offset_tables must be 0, 1 or 2");
+  if (!cell_offsets) return fail(XNB_ERR_ARG, "cell_offsets is required");
+  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  XCK(cudaSetDevice(b->device));
+  rc = pull_states(b, st);
+  if (rc) return rc;
+  const SysHost& h = b->sys[s];
+  if (h.list_off < 0 || !b->h_st[s].lists_fresh)
+    return fail(XNB_ERR_ARG, "positions changed since the last neighbour build: call xnb_chunk_neighbors first");
+  if (b->h_st[s].error) return fail(XNB_ERR_DEVICE, "the system has device error bits set");
+  const uint32_t ncells = h.d.ncells;
+  uint32_t* len = b->a.cell_cnt + h.d.cell_base;  // rebin scratch, free outside a step
+  auto* off = reinterpret_cast<unsigned long long*>(cell_offsets);
+  b->launches += launch_stream_lengths(static_cast<uint32_t>(s), ncells, b->d_sys, b->a, offset_tables, len,
+                                       b->sm_count, st);
+  b->launches += launch_scan_u32_to_u64(len, off, ncells, b->a.scan_blocks, st);
+  unsigned long long total = 0;
+  XCK(cudaMemcpyAsync(&total, off + ncells, sizeof(total), cudaMemcpyDeviceToHost, st));
+  XCK(cudaStreamSynchronize(st));
+  if (total_out) *total_out = static_cast<int64_t>(total);
+  if (!stream) return check_launch();
+  if (static_cast<int64_t>(total) > cap) return fail(XNB_ERR_CAPACITY, "stream buffer too small");
+  XCK(cudaMemsetAsync(b->d_flag, 0, sizeof(unsigned int), st));
+  b->launches += launch_stream_write(static_cast<uint32_t>(s), ncells, b->d_sys, b->a, offset_tables, off, stream,
+                                     b->d_flag, b->sm_count, st);
+  unsigned int flag = 0;
+  XCK(cudaMemcpyAsync(&flag, b->d_flag, sizeof(flag), cudaMemcpyDeviceToHost, st));
+  XCK(cudaStreamSynchronize(st));
+  if (flag) return fail(XNB_ERR_ARG, "a cell holds more than 65535 particles: not representable in the u16 stream");
+  return check_launch();
+}
+
+int xnb_verify_chunk_neighbors(xnb_batch* b, int32_t s, int32_t offset_tables, const uint16_t* stream,
+                               int64_t stream_len, const uint64_t* cell_offsets, int64_t* counts_out,
+                               void* cuda_stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0) return fail(XNB_ERR_ARG, "streams are checked for one system");
+  if (offset_tables < 0 || offset_tables > 2) return fail(XNB_ERR_ARG, "offset_tables must be 0, 1 or 2");
+  if (!stream || !cell_offsets || !counts_out || stream_len < 0) return fail(XNB_ERR_ARG, "null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  XCK(cudaSetDevice(b->device));
+  const SysHost& h = b->sys[s];
+  XCK(cudaMemsetAsync(b->d_counts, 0, 6 * sizeof(unsigned long long), st));
+  b->launches += launch_stream_verify(static_cast<uint32_t>(s), h.d.ncells, b->d_sys, b->a, offset_tables, stream,
+                                      static_cast<uint64_t>(stream_len),
+                                      reinterpret_cast<const unsigned long long*>(cell_offsets), b->d_counts,
+                                      b->sm_count, st);
+  unsigned long long c[6];
+  XCK(cudaMemcpyAsync(c, b->d_counts, sizeof(c), cudaMemcpyDeviceToHost, st));
+  XCK(cudaStreamSynchronize(st));
+  for (int k = 0; k < 6; ++k) counts_out[k] = static_cast<int64_t>(c[k]);
+  return check_launch();
 }
 
 int64_t xnb_stats_kernel_launches(const xnb_batch* b) { return b ? static_cast<int64_t>(b->launches) : -1; }

@@ -688,6 +688,7 @@ __global__ void k_nbr_reset(int nsys, SysState* st, const unsigned int* any) {
   if (s >= nsys || !st[s].rebuild) return;
   st[s].list_used = 0;
   st[s].max_nbr = 0;
+  st[s].lists_fresh = 1;  // the build that follows reads the current positions
 }
 
 // ---------------------------------------------------------------------------

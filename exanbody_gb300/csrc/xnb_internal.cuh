@@ -77,7 +77,7 @@ struct SysState {
   uint32_t max_cell;            // largest cell occupancy after the last rebin
   uint32_t rebuild_armed;        // 1 once backup_r has run (the trigger needs a backup)
   uint32_t max_nbr;              // largest per-particle list count of the last build
-  uint32_t pad_;
+  uint32_t lists_fresh;          // 1 from a neighbour build until positions next change
   unsigned long long rebuilds;
 };
 

@@ -49,6 +49,18 @@ int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevA
 int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int stage_cap,
                      int lbuf, cudaStream_t stream);
 
+// Reference-format chunk-neighbour streams of system sid (xnb_stream.cu):
+// per-cell lengths (u16 units), the streams at cell_off, and the checker
+// (counts[6]: format, order, self, range, far, missing).
+int launch_stream_lengths(uint32_t sid, uint32_t ncells, const SysDesc* sys, const DevArrays& a, int T,
+                          uint32_t* cell_len, int sm_count, cudaStream_t stream);
+int launch_stream_write(uint32_t sid, uint32_t ncells, const SysDesc* sys, const DevArrays& a, int T,
+                        const unsigned long long* cell_off, uint16_t* out, unsigned int* errors, int sm_count,
+                        cudaStream_t stream);
+int launch_stream_verify(uint32_t sid, uint32_t ncells, const SysDesc* sys, const DevArrays& a, int T,
+                         const uint16_t* stream_data, uint64_t stream_len, const unsigned long long* cell_off,
+                         unsigned long long* counts, int sm_count, cudaStream_t stream);
+
 // Exclusive scan of u32 counts into u64 offsets (n elements; out has n+1 entries).
 // With gate != nullptr the kernels return at once while *gate == 0.
 int launch_scan_u32_to_u64(const uint32_t* in, unsigned long long* out, uint32_t n,

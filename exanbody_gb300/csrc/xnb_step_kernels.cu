@@ -19,9 +19,14 @@ constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 // trajectory); EXACT=false lets the compiler fuse them into FMAs.
 template <bool EXACT>
 __global__ void __launch_bounds__(256)
-    k_first_half(uint32_t n_part, const SysDesc* __restrict__ sys, SysState* __restrict__ st, DevArrays a,
+    k_first_half(uint32_t n_part, int nsys, const SysDesc* __restrict__ sys, SysState* __restrict__ st, DevArrays a,
                  bool push_r, bool push_v, bool trigger, double scale_r, double scale_v, int sys_only) {
   const bool canonical = (scale_r == 1.0 && scale_v == 0.5);
+  if (push_r && blockIdx.x == 0) {
+    // positions change: lists no longer describe the current positions exactly
+    for (int s = static_cast<int>(threadIdx.x); s < nsys; s += static_cast<int>(blockDim.x))
+      if (sys_only < 0 || s == sys_only) st[s].lists_fresh = 0;
+  }
   // every lane of a warp runs the same number of iterations, so full-warp
   // collectives below see all 32 lanes
   const uint32_t stride = gridDim.x * blockDim.x;
@@ -577,10 +582,10 @@ int launch_first_half(const Extent& ex, const SysDesc* sys, SysState* st, const 
   const int threads = 256;
   const int g = grid_for(ex.n_part, threads);
   if (exact)
-    k_first_half<true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, do_push_r, do_push_v, do_trigger,
+    k_first_half<true><<<g, threads, 0, stream>>>(ex.n_part, ex.nsys, sys, st, a, do_push_r, do_push_v, do_trigger,
                                                   dt_scale_r, dt_scale_v, sys_only);
   else
-    k_first_half<false><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, do_push_r, do_push_v, do_trigger,
+    k_first_half<false><<<g, threads, 0, stream>>>(ex.n_part, ex.nsys, sys, st, a, do_push_r, do_push_v, do_trigger,
                                                    dt_scale_r, dt_scale_v, sys_only);
   return 1;
 }

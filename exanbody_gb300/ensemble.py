@@ -127,8 +127,11 @@ def main():
     out = {"workload": "ensemble_%d_fcc_n4-25_rho0.70-1.00_T0.7-1.5" % args.count,
            "atoms": int(sum(w["n_atoms"] for w in systems)), "systems": args.count, "steps": args.steps,
            "config": cfg, "autotune_seconds": tune_s}
-    for name, base in (("mixed", xnb.PREC_MIXED), ("fp64", xnb.PREC_FP64)):
-        prec = base | (xnb.PREC_NEWTON if cfg["newton"] else 0)
+    # the mixed path runs the tuned configuration; the FP64 path is timed with both
+    # traversals (full lists, Newton half lists) and reported at its faster one
+    runs = [("mixed", xnb.PREC_MIXED | (xnb.PREC_NEWTON if cfg["newton"] else 0)),
+            ("fp64_full", xnb.PREC_FP64), ("fp64_newton", xnb.PREC_FP64 | xnb.PREC_NEWTON)]
+    for name, prec in runs:
         b, ids, n = build_batch(systems, cfg["stage_cap"], cfg["force_block"], cfg["skin"],
                                 stream=stream.cuda_stream, precision=prec)
         secs, done = timed_steps(b, stream, args.steps, prec)
@@ -136,6 +139,8 @@ def main():
         b.close()
         out[name] = {"atom_steps_per_s": n * done / secs, "seconds": secs, "steps": done,
                      "rebuilds_total": int(rebuilds)}
+    best = max(("fp64_full", "fp64_newton"), key=lambda k: out[k]["atom_steps_per_s"])
+    out["fp64"] = dict(out[best], traversal=best)
     out["speedup_mixed_vs_fp64"] = out["mixed"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"]
     if tune_log is not None:
         out["autotune_trials"] = tune_log

@@ -31,8 +31,11 @@ EXPORTED = [
     "xnb_system_energy", "xnb_init_particles", "xnb_push_f_v_r", "xnb_push_f_v", "xnb_particle_displ_over",
     "xnb_update_particles_full", "xnb_chunk_neighbors", "xnb_backup_r", "xnb_lennard_jones_force",
     "xnb_ghost_update_r", "xnb_step", "xnb_step_graph_create", "xnb_graph_launch", "xnb_graph_destroy",
-    "xnb_check_errors", "xnb_stats_kernel_launches", "xnb_chunk_neighbors_noalloc",
+    "xnb_check_errors", "xnb_stats_kernel_launches", "xnb_chunk_neighbors_noalloc", "xnb_chunk_neighbors_stream",
+    "xnb_verify_chunk_neighbors",
 ]
+
+STREAM_CHECKS = ("format", "order", "self", "range", "far", "missing")
 
 
 class LJParams(C.Structure):
@@ -134,6 +137,8 @@ def load(build_if_missing=True):
     lib.xnb_stats_kernel_launches.argtypes = [vp]
     u32p = P(C.c_uint32)
     lib.xnb_chunk_neighbors_noalloc.argtypes = [P(LJParams), i64, vp, vp, vp, vp, vp, vp, i64, vp, vp, P(i64), vp]
+    lib.xnb_chunk_neighbors_stream.argtypes = [vp, i32, i32, vp, i64, vp, P(i64), vp]
+    lib.xnb_verify_chunk_neighbors.argtypes = [vp, i32, i32, vp, i64, vp, P(i64), vp]
     _LIB = lib
     return lib
 
@@ -277,6 +282,29 @@ class Batch:
         _ck(self.lib.xnb_step_graph_create(self.h, int(nsteps), int(precision), int(flags), self.stream,
                                            C.byref(g)))
         return Graph(self, g)
+
+    def chunk_neighbors_stream(self, s, offset_tables=1, device="cuda"):
+        """Reference-format u16 streams of system s as device tensors
+        (stream[total] as int16 bit patterns, cell_offsets[n_cells + 1] as int64)."""
+        import torch
+
+        ncells = self.info(s).n_cells
+        off = torch.empty(ncells + 1, dtype=torch.int64, device=device)
+        total = C.c_int64()
+        _ck(self.lib.xnb_chunk_neighbors_stream(self.h, s, int(offset_tables), None, 0, C.c_void_p(off.data_ptr()),
+                                                C.byref(total), self.stream))
+        buf = torch.empty(max(1, total.value), dtype=torch.int16, device=device)
+        _ck(self.lib.xnb_chunk_neighbors_stream(self.h, s, int(offset_tables), C.c_void_p(buf.data_ptr()),
+                                                total.value, C.c_void_p(off.data_ptr()), C.byref(total), self.stream))
+        return buf[: total.value], off
+
+    def verify_chunk_neighbors(self, s, stream, cell_offsets, offset_tables=1):
+        """verify_chunk_neighbors counts (dict over STREAM_CHECKS) for device tensors."""
+        out = (C.c_int64 * 6)()
+        _ck(self.lib.xnb_verify_chunk_neighbors(self.h, s, int(offset_tables), C.c_void_p(stream.data_ptr()),
+                                                int(stream.numel()), C.c_void_p(cell_offsets.data_ptr()), out,
+                                                self.stream))
+        return dict(zip(STREAM_CHECKS, [int(x) for x in out]))
 
     def check_errors(self):
         _ck(self.lib.xnb_check_errors(self.h, self.stream))

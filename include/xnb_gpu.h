@@ -180,6 +180,38 @@ int xnb_check_errors(xnb_batch* b, void* stream);
  * the reference's equivalent bookkeeping lives in onika's profiling layer). */
 int64_t xnb_stats_kernel_launches(const xnb_batch* b);
 
+/* ---- reference-format neighbour streams ---- */
+
+/* chunk_neighbors' own output layout (GridChunkNeighbors::m_cell_stream,
+ * chunk_neighbors.h:42-120; encoding of chunk_neighbors_execute.h:249-398 with
+ * chunk size 1), so the reference's other pair functors can traverse lists built
+ * here. One u16 stream per interior cell of system `sys`, in the grid's linear
+ * cell order, concatenated into `stream` (device memory, `cap` u16 entries); cell
+ * c's stream is stream[cell_offsets[c] .. cell_offsets[c+1]) (device array of
+ * n_cells + 1 u64). offset_tables: 0, 1 (per-particle offsets, the reference's
+ * build_particle_offset) or 2 (plus the per-particle count of lower-ordered
+ * neighbours, dual_particle_offset). Particle indices in a periodic-image cell
+ * number the owner cell's particles that pass the ghost filter, as in the
+ * reference's ghost cells. stream == NULL: only the sizes (cell_offsets and
+ * *total_out). The lists must describe the current positions (call after
+ * xnb_chunk_neighbors / xnb_update_particles_full, before positions change);
+ * otherwise XNB_ERR_ARG. XNB_ERR_CAPACITY when *total_out > cap. Synchronises. */
+int xnb_chunk_neighbors_stream(xnb_batch* b, int32_t sys, int32_t offset_tables, uint16_t* stream, int64_t cap,
+                               uint64_t* cell_offsets, int64_t* total_out, void* cuda_stream);
+/* verify_chunk_neighbors (particle_neighbors/verify_chunk_neighbors.cpp:58-168) for
+ * streams in the layout above (device pointers; stream_len u16 entries, and a
+ * cell whose offsets leave [0, stream_len] counts as a format error), against the
+ * current positions:
+ * counts_out[6] = format (tables, lengths, reads past a stream), order (cells or
+ * indices not increasing, second table wrong), self, range (cell outside the
+ * 27-cell block or index past the cell's size), far (listed pair not within
+ * 0 < d2 <= nbh_dist^2), missing (per particle, |listed - found| by an exhaustive
+ * FP64 search of the 27-cell block with the ghost filter). All zero: the streams
+ * hold exactly the reference's neighbour sets. Synchronises. */
+int xnb_verify_chunk_neighbors(xnb_batch* b, int32_t sys, int32_t offset_tables, const uint16_t* stream,
+                               int64_t stream_len, const uint64_t* cell_offsets, int64_t* counts_out,
+                               void* cuda_stream);
+
 /* ---- allocation-free entry point ---- */
 
 /* No counterpart in the reference. chunk_neighbors for one system, for callers
