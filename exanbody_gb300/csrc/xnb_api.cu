@@ -101,6 +101,7 @@ struct xnb_batch {
   SysState* h_st = nullptr;  // pinned mirror
   unsigned int* d_flag = nullptr;             // scratch error flag of the stream writer
   unsigned long long* d_counts = nullptr;     // scratch counters of the stream checker
+  unsigned char* d_stats = nullptr;           // scratch of the simulation_stats reduction
   std::vector<SysHost> sys;
   RangeAlloc parts, cells, lists;
   std::vector<void*> allocs;
@@ -437,6 +438,7 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   rc = rc ? rc : dalloc(b, &b->d_st, static_cast<uint64_t>(cfg->max_systems));
   rc = rc ? rc : dalloc(b, &b->d_flag, 1);
   rc = rc ? rc : dalloc(b, &b->d_counts, 8);
+  rc = rc ? rc : dalloc(b, &b->d_stats, stats_scratch_bytes());
   if (!rc && cudaMallocHost(&b->h_st, sizeof(SysState) * cfg->max_systems) != cudaSuccess)
     rc = fail(XNB_ERR_NOMEM, "cudaMallocHost failed");
   if (rc) {
@@ -986,6 +988,80 @@ int xnb_verify_chunk_neighbors(xnb_batch* b, int32_t s, int32_t offset_tables, c
   XCK(cudaMemcpyAsync(c, b->d_counts, sizeof(c), cudaMemcpyDeviceToHost, st));
   XCK(cudaStreamSynchronize(st));
   for (int k = 0; k < 6; ++k) counts_out[k] = static_cast<int64_t>(c[k]);
+  return check_launch();
+}
+
+int xnb_simulation_stats(xnb_batch* b, int32_t s, xnb_sim_stats* out, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0 || !out) return fail(XNB_ERR_ARG, "simulation_stats needs one system and an output");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  XCK(cudaSetDevice(b->device));
+  const SysHost& h = b->sys[s];
+  b->launches += launch_stats(static_cast<uint32_t>(s), h.d.npart, b->d_sys, b->a, b->d_stats, b->sm_count, st);
+  double v[6];
+  unsigned long long n = 0;
+  if (copy_stats(b->d_stats, v, &n, st) != 0) return fail(XNB_ERR_CUDA, "simulation_stats copy failed");
+  out->particle_count = static_cast<int64_t>(n);
+  out->kinetic_sum = v[0];
+  out->potential_energy = v[1];
+  out->min_vel = v[2];
+  out->max_vel = v[3];
+  out->min_acc = v[4];
+  out->max_acc = v[5];
+  return check_launch();
+}
+
+int xnb_sample_particles(xnb_batch* b, int32_t s, const uint64_t* ids, int64_t n, double* values, int32_t* found,
+                         void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0) return fail(XNB_ERR_ARG, "sampling needs one system");
+  if (n < 0 || n > (1 << 24)) return fail(XNB_ERR_ARG, "n must be in [0, 2^24]");
+  if (n == 0) return XNB_OK;
+  if (!ids || !values || !found) return fail(XNB_ERR_ARG, "null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  XCK(cudaSetDevice(b->device));
+  const size_t m = static_cast<size_t>(n);
+  std::vector<size_t> order(m);
+  for (size_t k = 0; k < m; ++k) order[k] = k;
+  std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return ids[x] < ids[y]; });
+  std::vector<uint64_t> sorted(m);
+  for (size_t k = 0; k < m; ++k) sorted[k] = ids[order[k]];
+  for (size_t k = 1; k < m; ++k)
+    if (sorted[k] == sorted[k - 1]) return fail(XNB_ERR_ARG, "ids must be distinct");
+  uint64_t* d_ids = nullptr;
+  double* d_vals = nullptr;
+  int32_t* d_found = nullptr;
+  auto release = [&]() {
+    if (d_ids) cudaFree(d_ids);
+    if (d_vals) cudaFree(d_vals);
+    if (d_found) cudaFree(d_found);
+  };
+  if (cudaMalloc(&d_ids, m * sizeof(uint64_t)) != cudaSuccess || cudaMalloc(&d_vals, m * 9 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_found, m * sizeof(int32_t)) != cudaSuccess) {
+    release();
+    return fail(XNB_ERR_NOMEM, "sampling buffers");
+  }
+  std::vector<double> hv(m * 9, 0.0);
+  std::vector<int32_t> hf(m, 0);
+  bool ok = cudaMemcpyAsync(d_ids, sorted.data(), m * sizeof(uint64_t), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            cudaMemsetAsync(d_found, 0, m * sizeof(int32_t), st) == cudaSuccess;
+  if (ok) {
+    b->launches += launch_sample(static_cast<uint32_t>(s), b->sys[s].d.npart, b->d_sys, b->a, d_ids,
+                                 static_cast<uint32_t>(m), d_vals, d_found, b->sm_count, st);
+    ok = cudaMemcpyAsync(hv.data(), d_vals, m * 9 * sizeof(double), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+         cudaMemcpyAsync(hf.data(), d_found, m * sizeof(int32_t), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+         cudaStreamSynchronize(st) == cudaSuccess;
+  }
+  release();
+  if (!ok) return fail(XNB_ERR_CUDA, "sampling failed");
+  for (size_t k = 0; k < m; ++k) {
+    const size_t dst = order[k];
+    found[dst] = hf[k];
+    if (hf[k])
+      for (int q = 0; q < 9; ++q) values[dst * 9 + q] = hv[k * 9 + q];
+  }
   return check_launch();
 }
 

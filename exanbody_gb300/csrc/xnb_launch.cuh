@@ -61,6 +61,16 @@ int launch_stream_verify(uint32_t sid, uint32_t ncells, const SysDesc* sys, cons
                          const uint16_t* stream_data, uint64_t stream_len, const unsigned long long* cell_off,
                          unsigned long long* counts, int sm_count, cudaStream_t stream);
 
+// On-device observables (xnb_observe.cu): simulation_stats of system sid into a
+// scratch area of stats_scratch_bytes() (copy_stats reads it back: kinetic
+// sum, potential, min/max |v|, min/max |f| and the count), and id sampling.
+size_t stats_scratch_bytes();
+int launch_stats(uint32_t sid, uint32_t npart, const SysDesc* sys, const DevArrays& a, void* scratch, int sm_count,
+                 cudaStream_t stream);
+int copy_stats(void* scratch, double* out6, unsigned long long* count_out, cudaStream_t stream);
+int launch_sample(uint32_t sid, uint32_t npart, const SysDesc* sys, const DevArrays& a, const uint64_t* ids,
+                  uint32_t n, double* out, int32_t* found, int sm_count, cudaStream_t stream);
+
 // Exclusive scan of u32 counts into u64 offsets (n elements; out has n+1 entries).
 // With gate != nullptr the kernels return at once while *gate == 0.
 int launch_scan_u32_to_u64(const uint32_t* in, unsigned long long* out, uint32_t n,

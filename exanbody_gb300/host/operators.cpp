@@ -330,12 +330,17 @@ struct MessageOp : OperatorNode {
 
 // simulation_stats + print_simulation_stats (io/simulation_stats.cpp:60-124): kinetic
 // and potential energy of the system.
+// simulation_stats (debug/simulation_stats.cpp:60-124), reduced on the GPU; the
+// kinetic energy printed is 0.5 * m * sum |v|^2 with the species mass.
 struct StatsOp : OperatorNode {
   void execute(Context& ctx) override {
     if (ctx.dry_run || !gpu_ready(ctx)) return;
-    double ke = 0, pe = 0;
-    ck(xnb_system_energy(ctx.batch, ctx.sys, &ke, &pe, nullptr), "simulation_stats");
-    std::printf("T=%ld ke=%.10g pe=%.10g total=%.10g\n", ctx.timestep, ke, pe, ke + pe);
+    xnb_sim_stats st{};
+    ck(xnb_simulation_stats(ctx.batch, ctx.sys, &st, nullptr), "simulation_stats");
+    const double ke = 0.5 * ctx.params.mass * st.kinetic_sum;
+    std::printf("T=%ld n=%lld ke=%.10g pe=%.10g total=%.10g |v|=[%.6g,%.6g] |a|=[%.6g,%.6g]\n", ctx.timestep,
+                static_cast<long long>(st.particle_count), ke, st.potential_energy, ke + st.potential_energy,
+                st.min_vel, st.max_vel, st.min_acc, st.max_acc);
   }
 };
 
@@ -353,36 +358,29 @@ struct CheckValuesOp : OperatorNode {
     const Node* vals = golden.find("values");
     if (!vals || !vals->is_seq()) throw Error("check_values: no values in " + path);
     if (ctx.dry_run) return;
-    const int64_t n = static_cast<int64_t>(ctx.host.id.size());
-    std::vector<double> r[3], v[3], acc[3];
-    for (int a = 0; a < 3; ++a) {
-      r[a].resize(static_cast<size_t>(n));
-      v[a].resize(static_cast<size_t>(n));
-      acc[a].resize(static_cast<size_t>(n));
-    }
-    std::vector<uint64_t> ids(static_cast<size_t>(n));
-    ck(xnb_system_download(ctx.batch, ctx.sys, r[0].data(), r[1].data(), r[2].data(), v[0].data(), v[1].data(),
-                           v[2].data(), acc[0].data(), acc[1].data(), acc[2].data(), ids.data(), nullptr, nullptr,
-                           nullptr),
-       "check_values download");
-    std::map<uint64_t, size_t> where;
-    for (size_t q = 0; q < ids.size(); ++q) where[ids[q]] = q;
+    // only the sampled particles leave the GPU (xnb_sample_particles)
+    std::vector<uint64_t> ids;
+    for (const auto& row : vals->seq) ids.push_back(static_cast<uint64_t>(to_long(row.seq.at(0))));
+    std::vector<double> got(ids.size() * 9);
+    std::vector<int32_t> found(ids.size());
+    ck(xnb_sample_particles(ctx.batch, ctx.sys, ids.data(), static_cast<int64_t>(ids.size()), got.data(),
+                            found.data(), nullptr),
+       "check_values sampling");
     const auto& p = ctx.params;
     double er = 0, ea = 0, ev = 0;
-    for (const auto& row : vals->seq) {
-      const uint64_t id = static_cast<uint64_t>(to_long(row.seq.at(0)));
-      auto it = where.find(id);
-      if (it == where.end()) throw Error("check_values: id " + std::to_string(id) + " not found");
-      const size_t q = it->second;
+    for (size_t q = 0; q < ids.size(); ++q) {
+      if (!found[q]) throw Error("check_values: id " + std::to_string(ids[q]) + " not found");
+      const Node& row = vals->seq[q];
       double ref[9];
       for (int k = 0; k < 9; ++k) ref[k] = std::strtod(row.seq.at(static_cast<size_t>(k + 1)).scalar.c_str(), nullptr);
+      const double* g = got.data() + q * 9;  // r, f, v
       for (int a = 0; a < 3; ++a) {
         const double L = p.extent[a] - p.origin[a];
-        double d = r[a][q] - ref[a];
+        double d = g[a] - ref[a];
         d -= L * std::round(d / L);
         er += d * d;
-        ea += (acc[a][q] - ref[3 + a]) * (acc[a][q] - ref[3 + a]);
-        ev += (v[a][q] - ref[6 + a]) * (v[a][q] - ref[6 + a]);
+        ea += (g[3 + a] - ref[3 + a]) * (g[3 + a] - ref[3 + a]);
+        ev += (g[6 + a] - ref[6 + a]) * (g[6 + a] - ref[6 + a]);
       }
     }
     er = std::sqrt(er);

@@ -32,7 +32,7 @@ EXPORTED = [
     "xnb_update_particles_full", "xnb_chunk_neighbors", "xnb_backup_r", "xnb_lennard_jones_force",
     "xnb_ghost_update_r", "xnb_step", "xnb_step_graph_create", "xnb_graph_launch", "xnb_graph_destroy",
     "xnb_check_errors", "xnb_stats_kernel_launches", "xnb_chunk_neighbors_noalloc", "xnb_chunk_neighbors_stream",
-    "xnb_verify_chunk_neighbors",
+    "xnb_verify_chunk_neighbors", "xnb_simulation_stats", "xnb_sample_particles",
 ]
 
 STREAM_CHECKS = ("format", "order", "self", "range", "far", "missing")
@@ -53,6 +53,18 @@ class LJParams(C.Structure):
         ("divide_by_mass", C.c_int32),
         ("amr_enabled", C.c_int32),
         ("sub_grid_density", C.c_double),
+    ]
+
+
+class SimStats(C.Structure):
+    _fields_ = [
+        ("particle_count", C.c_int64),
+        ("kinetic_sum", C.c_double),
+        ("potential_energy", C.c_double),
+        ("min_vel", C.c_double),
+        ("max_vel", C.c_double),
+        ("min_acc", C.c_double),
+        ("max_acc", C.c_double),
     ]
 
 
@@ -139,6 +151,8 @@ def load(build_if_missing=True):
     lib.xnb_chunk_neighbors_noalloc.argtypes = [P(LJParams), i64, vp, vp, vp, vp, vp, vp, i64, vp, vp, P(i64), vp]
     lib.xnb_chunk_neighbors_stream.argtypes = [vp, i32, i32, vp, i64, vp, P(i64), vp]
     lib.xnb_verify_chunk_neighbors.argtypes = [vp, i32, i32, vp, i64, vp, P(i64), vp]
+    lib.xnb_simulation_stats.argtypes = [vp, i32, P(SimStats), vp]
+    lib.xnb_sample_particles.argtypes = [vp, i32, P(u64), i64, P(d), P(i32), vp]
     _LIB = lib
     return lib
 
@@ -305,6 +319,22 @@ class Batch:
                                                 int(stream.numel()), C.c_void_p(cell_offsets.data_ptr()), out,
                                                 self.stream))
         return dict(zip(STREAM_CHECKS, [int(x) for x in out]))
+
+    def simulation_stats(self, s):
+        """simulation_stats reduced on the GPU (dict of the xnb_sim_stats fields)."""
+        st = SimStats()
+        _ck(self.lib.xnb_simulation_stats(self.h, s, C.byref(st), self.stream))
+        return {k: getattr(st, k) for k, _ in SimStats._fields_}
+
+    def sample_particles(self, s, ids):
+        """(values[n, 9] = r, f, v; found[n]) for the given particle ids, gathered on the GPU."""
+        ids = np.ascontiguousarray(ids, np.uint64)
+        vals = np.zeros((len(ids), 9))
+        found = np.zeros(len(ids), np.int32)
+        _ck(self.lib.xnb_sample_particles(self.h, s, ids.ctypes.data_as(C.POINTER(C.c_uint64)), len(ids),
+                                          vals.ctypes.data_as(C.POINTER(C.c_double)),
+                                          found.ctypes.data_as(C.POINTER(C.c_int32)), self.stream))
+        return vals, found
 
     def check_errors(self):
         _ck(self.lib.xnb_check_errors(self.h, self.stream))

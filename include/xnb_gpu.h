@@ -212,6 +212,28 @@ int xnb_verify_chunk_neighbors(xnb_batch* b, int32_t sys, int32_t offset_tables,
                                int64_t stream_len, const uint64_t* cell_offsets, int64_t* counts_out,
                                void* cuda_stream);
 
+/* ---- on-device observables ---- */
+
+typedef struct xnb_sim_stats {
+  int64_t particle_count;
+  double kinetic_sum;      /* sum over particles of dot(v, v) * 1.0, as simulation_stats forms it (its mass is 1.0) */
+  double potential_energy; /* sum of the per-particle energies of the last force call made with energies */
+  double min_vel, max_vel; /* extremes of |v| */
+  double min_acc, max_acc; /* extremes of |f| (the force field the reference names ax, ay, az) */
+} xnb_sim_stats;
+
+/* simulation_stats (ComputeSimulationStatistics, debug/simulation_stats.cpp:60-124)
+ * reduced on the GPU for one system; sums in a fixed order (blocks folded in
+ * index order), so repeated calls agree bit for bit. Synchronises. */
+int xnb_simulation_stats(xnb_batch* b, int32_t sys, xnb_sim_stats* out, void* stream);
+/* Values of chosen particles by id, gathered on the GPU (what check_values,
+ * debug/check_values.cpp:230-401, compares): values[k*9 + 0..8] = rx ry rz fx fy fz
+ * vx vy vz of ids[k], found[k] = 1 when the id belongs to the system (0 and the
+ * values untouched otherwise). Host arrays; n <= 2^24; ids need not be sorted
+ * but must be distinct. Synchronises. */
+int xnb_sample_particles(xnb_batch* b, int32_t sys, const uint64_t* ids, int64_t n, double* values, int32_t* found,
+                         void* stream);
+
 /* ---- allocation-free entry point ---- */
 
 /* No counterpart in the reference. chunk_neighbors for one system, for callers
