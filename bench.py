@@ -329,13 +329,26 @@ def run_ours(args):
     if not args.no_e2e:
         out = {k: np.empty(N) for k in ("rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz")}
 
+        phases = {}
+
         def e2e_run():
             bb = new_batch()
+            t = time.perf_counter()
             ss = bb.add_system(params, w["r"], w["v"], w["id"], list_factor=1.2)
+            torch.cuda.synchronize()
+            phases["upload_s"] = time.perf_counter() - t
+            t = time.perf_counter()
             bb.init_particles(ss, MIXED)
+            torch.cuda.synchronize()
+            phases["init_s"] = time.perf_counter() - t
+            t = time.perf_counter()
             bb.step(args.steps, MIXED, 0)
+            torch.cuda.synchronize()
+            phases["steps_s"] = time.perf_counter() - t
+            t = time.perf_counter()
             got = bb.download(ss)
             bb.check_errors()
+            phases["download_s"] = time.perf_counter() - t
             bb.close()
             return got
 
@@ -350,7 +363,7 @@ def run_ours(args):
         e2e = {"value": world * N * args.steps / dt, "unit": "atom-steps/s",
                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
                "run": "host arrays -> xnb_system_add -> xnb_init_particles -> %d x xnb_step -> xnb_system_download"
-                      % args.steps}
+                      % args.steps, "phases": phases}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -473,6 +473,12 @@ int xnb_batch_destroy(xnb_batch* b) {
   return XNB_OK;
 }
 
+namespace {
+int place_system(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double* rx, const double* ry,
+                 const double* rz, const double* vx, const double* vy, const double* vz, const uint64_t* id,
+                 const int64_t* cell_counts, int64_t poff, int64_t coff, uint64_t ncells, int slot, cudaStream_t st);
+}  // namespace
+
 int xnb_system_add(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double* rx, const double* ry,
                    const double* rz, const double* vx, const double* vy, const double* vz, const uint64_t* id,
                    const int64_t* cell_counts, double list_factor, void* stream, int32_t* sys_out) {
@@ -497,6 +503,68 @@ int xnb_system_add(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double
   if (coff < 0) {
     b->parts.release(static_cast<uint64_t>(poff));
     return fail(XNB_ERR_NOMEM, "cell pool exhausted");
+  }
+  rc = place_system(b, p, n, rx, ry, rz, vx, vy, vz, id, cell_counts, poff, coff, ncells, slot, st);
+  if (rc) {
+    b->parts.release(static_cast<uint64_t>(poff));
+    b->cells.release(static_cast<uint64_t>(coff));
+    return rc;
+  }
+  SysHost& sh = b->sys[slot];
+  sh = SysHost{};
+  sh.d = make_desc(*p);
+  sh.d.cell_base = static_cast<uint32_t>(coff);
+  sh.d.ncells = static_cast<uint32_t>(ncells);
+  sh.d.part_base = static_cast<uint32_t>(poff);
+  sh.d.npart = static_cast<uint32_t>(n);
+  sh.list_factor = list_factor >= 1.0 ? list_factor : 1.3;
+  SysState zero{};
+  XCK(cudaMemcpyAsync(b->d_st + slot, &zero, sizeof(SysState), cudaMemcpyHostToDevice, st));
+  sh.active = true;
+  rc = upload_desc(b, slot, st);
+  if (rc) return rc;
+  // the caller's arrays and the host staging are pageable: finish the copies before returning
+  XCK(cudaStreamSynchronize(st));
+  *sys_out = slot;
+  return XNB_OK;
+}
+
+namespace {
+
+// Particles, cell table and mirrors of a new system. Flat input (cell_counts
+// NULL) is placed on the device (launch_place); input given per reference cell,
+// or a cell too dense for the device pass, is staged on the host.
+int place_system(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double* rx, const double* ry,
+                 const double* rz, const double* vx, const double* vy, const double* vz, const uint64_t* id,
+                 const int64_t* cell_counts, int64_t poff, int64_t coff, uint64_t ncells, int slot, cudaStream_t st) {
+  DevArrays& a = b->a;
+  if (!cell_counts && n > 0) {
+    const size_t nb = static_cast<size_t>(n);
+    const double* srcs[6] = {rx, ry, rz, vx, vy, vz};
+    double* dsts[6] = {a.t_rx, a.t_ry, a.t_rz, a.t_vx, a.t_vy, a.t_vz};
+    for (int k = 0; k < 6; ++k)
+      XCK(cudaMemcpyAsync(dsts[k] + poff, srcs[k], nb * sizeof(double), cudaMemcpyHostToDevice, st));
+    XCK(cudaMemcpyAsync(a.t_id + poff, id, nb * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    PlaceArgs P{};
+    for (int ax = 0; ax < 3; ++ax) {
+      P.origin[ax] = p->origin[ax];
+      P.dims[ax] = p->dims[ax];
+    }
+    P.cell_size = p->cell_size;
+    P.poff = static_cast<uint32_t>(poff);
+    P.coff = static_cast<uint32_t>(coff);
+    P.n = static_cast<uint32_t>(n);
+    P.ncells = static_cast<uint32_t>(ncells);
+    P.sys_slot = static_cast<uint32_t>(slot);
+    XCK(cudaMemsetAsync(b->d_flag, 0, sizeof(unsigned int), st));
+    b->launches += launch_place(P, a, b->d_flag, b->sm_count, st);
+    unsigned int flag = 0;
+    XCK(cudaMemcpyAsync(&flag, b->d_flag, sizeof(flag), cudaMemcpyDeviceToHost, st));
+    XCK(cudaStreamSynchronize(st));
+    int rc = check_launch();
+    if (rc) return rc;
+    if (flag & 1u) return fail(XNB_ERR_ARG, "a particle position lies outside every representable cell");
+    if (!(flag & 2u)) return XNB_OK;
   }
   // Host staging in storage order.
   std::vector<double> h[6];
@@ -545,15 +613,6 @@ int xnb_system_add(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double
       hcell[dst] = static_cast<uint32_t>(coff) + c;
     }
   }
-  SysHost& sh = b->sys[slot];
-  sh = SysHost{};
-  sh.d = make_desc(*p);
-  sh.d.cell_base = static_cast<uint32_t>(coff);
-  sh.d.ncells = static_cast<uint32_t>(ncells);
-  sh.d.part_base = static_cast<uint32_t>(poff);
-  sh.d.npart = static_cast<uint32_t>(n);
-  sh.list_factor = list_factor >= 1.0 ? list_factor : 1.3;
-  DevArrays& a = b->a;
   const size_t nb = static_cast<size_t>(n);
   double* dsts[6] = {a.rx, a.ry, a.rz, a.vx, a.vy, a.vz};
   for (int k = 0; k < 6; ++k)
@@ -581,16 +640,12 @@ int xnb_system_add(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double
   XCK(cudaMemcpyAsync(a.cell_start + coff, cstart.data(), ncells * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
   XCK(cudaMemcpyAsync(a.cell_n + coff, cn.data(), ncells * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
   XCK(cudaMemcpyAsync(a.cell_sys + coff, csys.data(), ncells * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-  SysState zero{};
-  XCK(cudaMemcpyAsync(b->d_st + slot, &zero, sizeof(SysState), cudaMemcpyHostToDevice, st));
-  sh.active = true;
-  rc = upload_desc(b, slot, st);
-  if (rc) return rc;
-  // host staging buffers are pageable and local: finish the copies before returning
+  // the staging vectors are local: finish the copies before they go
   XCK(cudaStreamSynchronize(st));
-  *sys_out = slot;
   return XNB_OK;
 }
+
+}  // namespace
 
 int xnb_system_remove(xnb_batch* b, int32_t s, void* stream) {
   int rc = check_sys(b, s);

@@ -71,6 +71,18 @@ int copy_stats(void* scratch, double* out6, unsigned long long* count_out, cudaS
 int launch_sample(uint32_t sid, uint32_t npart, const SysDesc* sys, const DevArrays& a, const uint64_t* ids,
                   uint32_t n, double* out, int32_t* found, int sm_count, cudaStream_t stream);
 
+// Device placement of a system uploaded in input order into the rebin scratch
+// (xnb_place.cu). flags: bit 0 a position outside any representable cell, bit 1
+// a cell above kPlaceMaxCell particles (the host then places the system).
+constexpr uint32_t kPlaceMaxCell = 4096;
+struct PlaceArgs {
+  double origin[3];
+  double cell_size;
+  int dims[3];
+  uint32_t poff, coff, n, ncells, sys_slot;
+};
+int launch_place(const PlaceArgs& P, const DevArrays& a, unsigned int* flags, int sm_count, cudaStream_t stream);
+
 // Exclusive scan of u32 counts into u64 offsets (n elements; out has n+1 entries).
 // With gate != nullptr the kernels return at once while *gate == 0.
 int launch_scan_u32_to_u64(const uint32_t* in, unsigned long long* out, uint32_t n,
