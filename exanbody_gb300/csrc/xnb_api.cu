@@ -164,6 +164,15 @@ int validate(const xnb_lj_params* p) {
   return XNB_OK;
 }
 
+// Bound on |d2_f32 - d2_f64| for pairs within distance R in a system of largest
+// period P and neighbour distance nbh (the derivation is in make_desc).
+double fp32_d2_error(double P, double nbh, double R) {
+  const double u = std::ldexp(1.0, -24);
+  const double X = P + nbh;
+  const double D = (3.0 * X + 2.0 * P + R) * u * 1.01;
+  return 2.0 * std::sqrt(3.0) * R * D + 3.0 * D * D + 4.0 * u * (R * R + 1.0);
+}
+
 SysDesc make_desc(const xnb_lj_params& p) {
   SysDesc d{};
   for (int a = 0; a < 3; ++a) {
@@ -223,10 +232,7 @@ SysDesc make_desc(const xnb_lj_params& p) {
   double P = 0.0;
   for (int a = 0; a < 3; ++a) P = std::max(P, std::fabs(d.period[a]));
   const double X = P + nbh;
-  auto err_at = [&](double R) {
-    const double D = (3.0 * X + 2.0 * P + R) * u * 1.01;
-    return 2.0 * std::sqrt(3.0) * R * D + 3.0 * D * D + 4.0 * u * (R * R + 1.0);
-  };
+  auto err_at = [&](double R) { return fp32_d2_error(P, nbh, R); };
   d.nbh2_f = static_cast<float>(d.nbh2);
   d.nbh_margin_f = static_cast<float>(4.0 * err_at(nbh));
   d.pre_margin_f = static_cast<float>(4.0 * err_at(p.rcut));
@@ -382,8 +388,8 @@ int xnb_version(void) { return 10000; }
 
 int64_t xnb_system_bytes(int64_t n, int64_t ncells, double list_per_particle) {
   // doubles r v f pe, restored backup, rebin scratch (22); ids (2); u32 cell, backup,
-  // rebin and list bookkeeping (10); FP32 hi/lo mirrors
-  const int64_t per_part = 22 * 8 + 2 * 8 + 10 * 4 + 2 * 16;
+  // rebin and list bookkeeping (10); FP32 hi/lo mirrors; types (2)
+  const int64_t per_part = 22 * 8 + 2 * 8 + 10 * 4 + 2 * 16 + 2;
   const int64_t per_cell = 4 * 6 + 8 + 4;
   return n * per_part + ncells * per_cell + static_cast<int64_t>(static_cast<double>(n) * list_per_particle) * 4;
 }
@@ -426,6 +432,8 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   rc = rc ? rc : dalloc(b, &a.nbr_half, P);
   rc = rc ? rc : dalloc(b, &a.any_rebuild, 4);
   rc = rc ? rc : dalloc(b, &a.t_id, P);
+  rc = rc ? rc : dalloc(b, &a.ptype, P);
+  rc = rc ? rc : dalloc(b, &a.t_ptype, P);
   uint32_t** u32p[] = {&a.pcell, &a.bkx, &a.bky, &a.bkz, &a.pdest, &a.plocal, &a.mover_list,
                        &a.nbr_start, &a.nbr_cnt};
   for (uint32_t** p : u32p) rc = rc ? rc : dalloc(b, p, P);
@@ -635,6 +643,7 @@ int place_system(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double* 
     XCK(cudaMemsetAsync(a.fz + poff, 0, nb * sizeof(double), st));
     XCK(cudaMemsetAsync(a.pe + poff, 0, nb * sizeof(double), st));
     XCK(cudaMemsetAsync(a.nbr_cnt + poff, 0, nb * sizeof(uint32_t), st));
+    XCK(cudaMemsetAsync(a.ptype + poff, 0, nb * sizeof(uint8_t), st));
     XCK(cudaMemsetAsync(a.nbr_start + poff, 0, nb * sizeof(uint32_t), st));
   }
   XCK(cudaMemcpyAsync(a.cell_start + coff, cstart.data(), ncells * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
@@ -1117,6 +1126,90 @@ int xnb_sample_particles(xnb_batch* b, int32_t s, const uint64_t* ids, int64_t n
     if (hf[k])
       for (int q = 0; q < 9; ++q) values[dst * 9 + q] = hv[k * 9 + q];
   }
+  return check_launch();
+}
+
+int xnb_system_set_types(xnb_batch* b, int32_t s, const uint64_t* ids, const uint8_t* types, int64_t n,
+                         int64_t* matched, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0) return fail(XNB_ERR_ARG, "types are set for one system");
+  if (n < 0 || n > (1 << 24)) return fail(XNB_ERR_ARG, "n must be in [0, 2^24]");
+  if (n > 0 && (!ids || !types)) return fail(XNB_ERR_ARG, "null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  XCK(cudaSetDevice(b->device));
+  const size_t m = static_cast<size_t>(n);
+  std::vector<size_t> order(m);
+  for (size_t k = 0; k < m; ++k) order[k] = k;
+  std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return ids[x] < ids[y]; });
+  std::vector<uint64_t> sid(m);
+  std::vector<uint8_t> sty(m);
+  for (size_t k = 0; k < m; ++k) {
+    sid[k] = ids[order[k]];
+    sty[k] = types[order[k]];
+    if (k && sid[k] == sid[k - 1]) return fail(XNB_ERR_ARG, "ids must be distinct");
+  }
+  uint64_t* d_ids = nullptr;
+  uint8_t* d_types = nullptr;
+  if (m && (cudaMalloc(&d_ids, m * sizeof(uint64_t)) != cudaSuccess ||
+            cudaMalloc(&d_types, m * sizeof(uint8_t)) != cudaSuccess)) {
+    if (d_ids) cudaFree(d_ids);
+    return fail(XNB_ERR_NOMEM, "type buffers");
+  }
+  bool ok = cudaMemsetAsync(b->d_counts, 0, sizeof(unsigned long long), st) == cudaSuccess;
+  if (ok && m) {
+    ok = cudaMemcpyAsync(d_ids, sid.data(), m * sizeof(uint64_t), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+         cudaMemcpyAsync(d_types, sty.data(), m, cudaMemcpyHostToDevice, st) == cudaSuccess;
+    if (ok)
+      b->launches += launch_set_types(static_cast<uint32_t>(s), b->sys[s].d.npart, b->d_sys, b->a, d_ids, d_types,
+                                      static_cast<uint32_t>(m), b->d_counts, b->sm_count, st);
+  }
+  unsigned long long got = 0;
+  ok = ok && cudaMemcpyAsync(&got, b->d_counts, sizeof(got), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+       cudaStreamSynchronize(st) == cudaSuccess;
+  if (d_ids) cudaFree(d_ids);
+  if (d_types) cudaFree(d_types);
+  if (!ok) return fail(XNB_ERR_CUDA, "setting types failed");
+  if (matched) *matched = static_cast<int64_t>(got);
+  return check_launch();
+}
+
+int xnb_gravitational_force(xnb_batch* b, int32_t s, double G, const double* type_mass, int32_t ntypes,
+                            double rcut, int32_t precision, int32_t flags, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (precision != XNB_PREC_FP64_EXACT && precision != XNB_PREC_FP64)
+    return fail(XNB_ERR_ARG, "gravitational_force runs in FP64_EXACT or FP64");
+  if (ntypes <= 0 || ntypes > kMaxTypes || !type_mass) return fail(XNB_ERR_ARG, "1 to 16 type masses");
+  if (!(rcut > 0.0)) return fail(XNB_ERR_ARG, "rcut must be positive");
+  if (flags & ~(XNB_FORCE_ENERGY | XNB_FORCE_ACCUMULATE)) return fail(XNB_ERR_ARG, "bad flags");
+  GravParams gp{};
+  gp.G = G;
+  gp.rcut2 = rcut * rcut;
+  gp.ntypes = ntypes;
+  for (int t = 0; t < ntypes; ++t) gp.mass[t] = type_mass[t];
+  // prefilter threshold: rcut^2 + the largest FP32 error bound of the systems it runs on
+  double margin = 0.0;
+  for (size_t q = 0; q < b->sys.size(); ++q) {
+    const SysHost& h = b->sys[q];
+    if (!h.active || (s >= 0 && static_cast<int32_t>(q) != s)) continue;
+    const double nbh = std::sqrt(h.d.nbh2);
+    if (rcut > nbh) return fail(XNB_ERR_ARG, "rcut above the neighbour distance of the lists");
+    double P = 0.0;
+    for (int a = 0; a < 3; ++a) P = std::max(P, std::fabs(h.d.period[a]));
+    margin = std::max(margin, 4.0 * fp32_d2_error(P, nbh, rcut));
+  }
+  gp.pre_hi_f = static_cast<float>(gp.rcut2 + margin);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  XCK(cudaSetDevice(b->device));
+  XCK(cudaMemsetAsync(b->d_flag, 0, sizeof(unsigned int), st));
+  const Extent ex = b->extent();
+  b->launches += launch_gravity(ex, b->d_sys, b->d_st, b->a, precision, (flags & XNB_FORCE_ENERGY) != 0,
+                                (flags & XNB_FORCE_ACCUMULATE) != 0, s, gp, b->d_flag, st);
+  unsigned int flag = 0;
+  XCK(cudaMemcpyAsync(&flag, b->d_flag, sizeof(flag), cudaMemcpyDeviceToHost, st));
+  XCK(cudaStreamSynchronize(st));
+  if (flag & 1u) return fail(XNB_ERR_ARG, "a particle type has no mass");
   return check_launch();
 }
 

@@ -261,6 +261,7 @@ __global__ void __launch_bounds__(128)
       a.t_vx[dst] = a.vx[src]; a.t_vy[dst] = a.vy[src]; a.t_vz[dst] = a.vz[src];
       a.t_fx[dst] = a.fx[src]; a.t_fy[dst] = a.fy[src]; a.t_fz[dst] = a.fz[src];
       a.t_id[dst] = a.id[src];
+      a.t_ptype[dst] = a.ptype[src];
     }
     const SrcInfo si = arrivals_of(S, a, c, lane);
     if (si.src != kInvalid && si.count > 0) {
@@ -275,6 +276,7 @@ __global__ void __launch_bounds__(128)
         a.t_vx[dst] = a.vx[p]; a.t_vy[dst] = a.vy[p]; a.t_vz[dst] = a.vz[p];
         a.t_fx[dst] = a.fx[p]; a.t_fy[dst] = a.fy[p]; a.t_fz[dst] = a.fz[p];
         a.t_id[dst] = a.id[p];
+        a.t_ptype[dst] = a.ptype[p];
       }
     }
   }
@@ -334,6 +336,7 @@ __global__ void __launch_bounds__(128)
       a.vx[dst] = a.t_vx[src]; a.vy[dst] = a.t_vy[src]; a.vz[dst] = a.t_vz[src];
       a.fx[dst] = a.t_fx[src]; a.fy[dst] = a.t_fy[src]; a.fz[dst] = a.t_fz[src];
       a.id[dst] = a.t_id[src];
+      a.ptype[dst] = a.t_ptype[src];
       float4 mhi, mlo;
       make_pf2(S, x, y, z, mhi, mlo);
       a.pf[dst] = mhi;

@@ -88,12 +88,14 @@ struct DevArrays {
   float4* pflo;                    // FP32 residual (x - origin) - hi, so hi + lo carries ~48 bits
   unsigned int* any_rebuild;       // number of systems flagged for the rebuild path this step
   uint64_t* id;
+  uint8_t* ptype;                  // particle type (field::type), 0 unless set
   uint32_t* pcell;                 // global cell of each particle
   uint32_t *bkx, *bky, *bkz;       // backup_r u32 encoding (backup_r.h:36-51)
   double *rbx, *rby, *rbz;         // the same backup restored once per rebuild (restore_u32_double)
   // rebin scratch
   double *t_rx, *t_ry, *t_rz, *t_vx, *t_vy, *t_vz, *t_fx, *t_fy, *t_fz;
   uint64_t* t_id;
+  uint8_t* t_ptype;
   uint32_t* pdest;                 // destination cell (rebin) / scratch
   uint32_t* plocal;                // new in-cell slot of staying particles
   uint32_t* mover_list;            // per source cell, its movers (global index), in the cell's own range

@@ -71,6 +71,24 @@ int copy_stats(void* scratch, double* out6, unsigned long long* count_out, cudaS
 int launch_sample(uint32_t sid, uint32_t npart, const SysDesc* sys, const DevArrays& a, const uint64_t* ids,
                   uint32_t n, double* out, int32_t* found, int sm_count, cudaStream_t stream);
 
+// gravitational_force over the per-particle lists (xnb_functors.cu). Masses per
+// particle type (at most kMaxTypes); pre_hi_f = rcut^2 + the FP32 prefilter's
+// proven margin. flags bit 0: a particle type without a mass.
+constexpr int kMaxTypes = 16;
+struct GravParams {
+  double G;
+  double rcut2;
+  float pre_hi_f;
+  int ntypes;
+  double mass[kMaxTypes];
+};
+int launch_gravity(const Extent& ex, const SysDesc* sys, const SysState* st, const DevArrays& a, int precision,
+                   bool with_pe, bool accumulate, int sys_only, const GravParams& gp, unsigned int* flags,
+                   cudaStream_t stream);
+// field::type by id for system sid (ids sorted ascending); matched += particles found
+int launch_set_types(uint32_t sid, uint32_t npart, const SysDesc* sys, const DevArrays& a, const uint64_t* ids,
+                     const uint8_t* types, uint32_t n, unsigned long long* matched, int sm_count, cudaStream_t stream);
+
 // Device placement of a system uploaded in input order into the rebin scratch
 // (xnb_place.cu). flags: bit 0 a position outside any representable cell, bit 1
 // a cell above kPlaceMaxCell particles (the host then places the system).

@@ -78,6 +78,7 @@ __global__ void __launch_bounds__(128)
       a.vy[dst] = a.t_vy[src];
       a.vz[dst] = a.t_vz[src];
       a.id[dst] = a.t_id[src];
+      a.ptype[dst] = 0;
       a.pcell[dst] = P.coff + c;
       const double ox = x - P.origin[0], oy = y - P.origin[1], oz = z - P.origin[2];
       const float4 hi = make_float4(static_cast<float>(ox), static_cast<float>(oy), static_cast<float>(oz), 0.f);

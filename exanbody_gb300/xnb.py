@@ -32,8 +32,12 @@ EXPORTED = [
     "xnb_update_particles_full", "xnb_chunk_neighbors", "xnb_backup_r", "xnb_lennard_jones_force",
     "xnb_ghost_update_r", "xnb_step", "xnb_step_graph_create", "xnb_graph_launch", "xnb_graph_destroy",
     "xnb_check_errors", "xnb_stats_kernel_launches", "xnb_chunk_neighbors_noalloc", "xnb_chunk_neighbors_stream",
-    "xnb_verify_chunk_neighbors", "xnb_simulation_stats", "xnb_sample_particles",
+    "xnb_verify_chunk_neighbors", "xnb_simulation_stats", "xnb_sample_particles", "xnb_system_set_types",
+    "xnb_gravitational_force",
 ]
+
+FORCE_ENERGY = 1
+FORCE_ACCUMULATE = 2
 
 STREAM_CHECKS = ("format", "order", "self", "range", "far", "missing")
 
@@ -153,6 +157,8 @@ def load(build_if_missing=True):
     lib.xnb_verify_chunk_neighbors.argtypes = [vp, i32, i32, vp, i64, vp, P(i64), vp]
     lib.xnb_simulation_stats.argtypes = [vp, i32, P(SimStats), vp]
     lib.xnb_sample_particles.argtypes = [vp, i32, P(u64), i64, P(d), P(i32), vp]
+    lib.xnb_system_set_types.argtypes = [vp, i32, P(u64), P(C.c_uint8), i64, P(i64), vp]
+    lib.xnb_gravitational_force.argtypes = [vp, i32, d, P(d), i32, d, i32, i32, vp]
     _LIB = lib
     return lib
 
@@ -354,6 +360,22 @@ class Batch:
                                           vals.ctypes.data_as(C.POINTER(C.c_double)),
                                           found.ctypes.data_as(C.POINTER(C.c_int32)), self.stream))
         return vals, found
+
+    def set_types(self, s, ids, types):
+        """field::type of the listed ids; returns how many particles of s were found."""
+        ids = np.ascontiguousarray(ids, np.uint64)
+        types = np.ascontiguousarray(types, np.uint8)
+        matched = C.c_int64()
+        _ck(self.lib.xnb_system_set_types(self.h, s, ids.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                          types.ctypes.data_as(C.POINTER(C.c_uint8)), len(ids), C.byref(matched),
+                                          self.stream))
+        return matched.value
+
+    def gravitational_force(self, s, G, masses, rcut, precision=PREC_FP64_EXACT, energy=False, accumulate=False):
+        masses = np.ascontiguousarray(masses, np.float64)
+        flags = (FORCE_ENERGY if energy else 0) | (FORCE_ACCUMULATE if accumulate else 0)
+        _ck(self.lib.xnb_gravitational_force(self.h, s, float(G), masses.ctypes.data_as(C.POINTER(C.c_double)),
+                                             len(masses), float(rcut), int(precision), flags, self.stream))
 
     def check_errors(self):
         _ck(self.lib.xnb_check_errors(self.h, self.stream))

@@ -212,6 +212,26 @@ int xnb_verify_chunk_neighbors(xnb_batch* b, int32_t sys, int32_t offset_tables,
                                int64_t stream_len, const uint64_t* cell_offsets, int64_t* counts_out,
                                void* cuda_stream);
 
+/* ---- other pair functors through the same lists ---- */
+
+/* Particle types (the reference's field::type, 0 until set) by id: types[k] for
+ * ids[k] (host arrays, n <= 2^24, distinct ids). *matched = particles of the
+ * system that were found. Types follow their particles through rebins. */
+int xnb_system_set_types(xnb_batch* b, int32_t sys, const uint64_t* ids, const uint8_t* types, int64_t n,
+                         int64_t* matched, void* stream);
+/* gravitational_force (GravitationalForceFunctor, contribs/pi/gravitational_force.cu:
+ * 42-141) over the current neighbour lists: for pairs within rcut (<= the lists'
+ * rcut + rcut_inc), f_a += G m_a m_b / r^3 * (r_b - r_a) with masses type_mass[type]
+ * (ntypes <= 16). precision XNB_PREC_FP64_EXACT (the functor's own roundings) or
+ * XNB_PREC_FP64. flags: XNB_FORCE_ENERGY also writes 0.5 * sum(-G m_a m_b / r) per
+ * particle; XNB_FORCE_ACCUMULATE adds onto the current forces (as the reference's
+ * buffer-less functors add onto the force field), otherwise forces start at zero
+ * (zero_particle_force). A particle type without a mass returns XNB_ERR_ARG. */
+#define XNB_FORCE_ENERGY 1
+#define XNB_FORCE_ACCUMULATE 2
+int xnb_gravitational_force(xnb_batch* b, int32_t sys, double G, const double* type_mass, int32_t ntypes,
+                            double rcut, int32_t precision, int32_t flags, void* stream);
+
 /* ---- on-device observables ---- */
 
 typedef struct xnb_sim_stats {

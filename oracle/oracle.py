@@ -51,6 +51,8 @@ def _lib(kind="parity"):
         getattr(lib, f).restype = i64
         getattr(lib, f).argtypes = [C.c_void_p]
     lib.xo_get_particles.argtypes = [C.c_void_p] + [P(d)] * 9 + [P(u64), P(i32), P(d)]
+    lib.xo_set_types.argtypes = [C.c_void_p, P(u64), P(C.c_uint8), i64]
+    lib.xo_gravitational_force.argtypes = [C.c_void_p, d, P(d), C.c_int32, d]
     lib.xo_get_cell_counts.argtypes = [C.c_void_p, P(i64)]
     lib.xo_get_pairs.argtypes = [C.c_void_p, P(u64), P(u64), P(i32)]
     lib.xo_cell_stream_size.restype = i64
@@ -160,6 +162,19 @@ class OracleSystem:
         if m:
             self.lib.xo_get_cell_stream(self.h, interior_cell, _ptr(out, C.c_uint16))
         return out
+
+    def set_types(self, ids, types):
+        ids = np.ascontiguousarray(ids, np.uint64)
+        types = np.ascontiguousarray(types, np.uint8)
+        rc = self.lib.xo_set_types(self.h, _ptr(ids, C.c_uint64), _ptr(types, C.c_uint8), len(ids))
+        if rc != 0:
+            raise RuntimeError("oracle set_types matched nothing")
+
+    def gravitational_force(self, G, masses, rcut):
+        masses = np.ascontiguousarray(masses, np.float64)
+        rc = self.lib.xo_gravitational_force(self.h, float(G), _ptr(masses, C.c_double), len(masses), float(rcut))
+        if rc != 0:
+            raise RuntimeError("oracle gravitational_force failed: %d" % rc)
 
     def energy(self):
         ke, pe = C.c_double(), C.c_double()

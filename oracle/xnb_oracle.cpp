@@ -35,33 +35,34 @@ inline double norm2(double x, double y, double z) { return (x * x + y * y) + z *
 struct Cell {
   std::vector<double> rx, ry, rz, vx, vy, vz, fx, fy, fz, pe;
   std::vector<uint64_t> id;
+  std::vector<uint8_t> type;  // particle type (field::type); 0 unless set
   size_t size() const { return rx.size(); }
   void clear() {
     rx.clear(); ry.clear(); rz.clear(); vx.clear(); vy.clear(); vz.clear();
-    fx.clear(); fy.clear(); fz.clear(); pe.clear(); id.clear();
+    fx.clear(); fy.clear(); fz.clear(); pe.clear(); id.clear(); type.clear();
   }
   void push(double x, double y, double z, double a, double b, double c, double f0, double f1,
-            double f2, uint64_t i) {
+            double f2, uint64_t i, uint8_t t = 0) {
     rx.push_back(x); ry.push_back(y); rz.push_back(z);
     vx.push_back(a); vy.push_back(b); vz.push_back(c);
     fx.push_back(f0); fy.push_back(f1); fz.push_back(f2);
-    pe.push_back(0.0); id.push_back(i);
+    pe.push_back(0.0); id.push_back(i); type.push_back(t);
   }
   void copy_from(size_t dst, const Cell& s, size_t src) {
     rx[dst] = s.rx[src]; ry[dst] = s.ry[src]; rz[dst] = s.rz[src];
     vx[dst] = s.vx[src]; vy[dst] = s.vy[src]; vz[dst] = s.vz[src];
     fx[dst] = s.fx[src]; fy[dst] = s.fy[src]; fz[dst] = s.fz[src];
-    pe[dst] = s.pe[src]; id[dst] = s.id[src];
+    pe[dst] = s.pe[src]; id[dst] = s.id[src]; type[dst] = s.type[src];
   }
   void resize(size_t n) {
     rx.resize(n); ry.resize(n); rz.resize(n); vx.resize(n); vy.resize(n); vz.resize(n);
-    fx.resize(n); fy.resize(n); fz.resize(n); pe.resize(n); id.resize(n);
+    fx.resize(n); fy.resize(n); fz.resize(n); pe.resize(n); id.resize(n); type.resize(n);
   }
   void swap_p(size_t a, size_t b) {
     std::swap(rx[a], rx[b]); std::swap(ry[a], ry[b]); std::swap(rz[a], rz[b]);
     std::swap(vx[a], vx[b]); std::swap(vy[a], vy[b]); std::swap(vz[a], vz[b]);
     std::swap(fx[a], fx[b]); std::swap(fy[a], fy[b]); std::swap(fz[a], fz[b]);
-    std::swap(pe[a], pe[b]); std::swap(id[a], id[b]);
+    std::swap(pe[a], pe[b]); std::swap(id[a], id[b]); std::swap(type[a], type[b]);
   }
 };
 
@@ -220,7 +221,7 @@ struct xo_sys {
           }
         }
     // Collect mover payloads before any cell is modified.
-    struct Payload { double v[3], f[3], pe; uint64_t id; };
+    struct Payload { double v[3], f[3], pe; uint64_t id; uint8_t type; };
     std::vector<std::vector<Payload>> pay(n_cells);
     for (size_t c = 0; c < n_cells; ++c) {
       for (const Mover& m : incoming[c]) {
@@ -228,7 +229,8 @@ struct xo_sys {
         pay[c].push_back(Payload{{s.vx[m.p], s.vy[m.p], s.vz[m.p]},
                                  {s.fx[m.p], s.fy[m.p], s.fz[m.p]},
                                  s.pe[m.p],
-                                 s.id[m.p]});
+                                 s.id[m.p],
+                                 s.type[m.p]});
       }
     }
     for (size_t c = 0; c < n_cells; ++c) {
@@ -255,7 +257,7 @@ struct xo_sys {
       for (size_t m = 0; m < incoming[c].size(); ++m) {
         const Mover& mv = incoming[c][m];
         const Payload& pl = pay[c][m];
-        cell.push(mv.r.x, mv.r.y, mv.r.z, pl.v[0], pl.v[1], pl.v[2], pl.f[0], pl.f[1], pl.f[2], pl.id);
+        cell.push(mv.r.x, mv.r.y, mv.r.z, pl.v[0], pl.v[1], pl.v[2], pl.f[0], pl.f[1], pl.f[2], pl.id, pl.type);
         cell.pe.back() = pl.pe;
       }
     }
@@ -388,7 +390,7 @@ struct xo_sys {
         if (all) {
           d.vx[q] = s.vx[pi]; d.vy[q] = s.vy[pi]; d.vz[q] = s.vz[pi];
           d.fx[q] = s.fx[pi]; d.fy[q] = s.fy[pi]; d.fz[q] = s.fz[pi];
-          d.pe[q] = 0.0; d.id[q] = s.id[pi];
+          d.pe[q] = 0.0; d.id[q] = s.id[pi]; d.type[q] = s.type[pi];
         }
       }
     }
@@ -553,6 +555,91 @@ struct xo_sys {
       }
     }
     return err ? -4 : 0;
+  }
+
+  /* zero_particle_force + gravitational_force (contribs/pi/gravitational_force.cu:42-
+   * 141): the buffer-less functor called per stream entry inside rcut
+   * (compute_cell_particle_pairs_impl_default.h:186-205), adding straight onto
+   * the zeroed force: r = sqrt(d2), inv_r = 1/r, e = -G m_a m_b inv_r,
+   * de = G m_a m_b inv_r inv_r, de *= w / r (w = 1), f_a += de * dr with
+   * dr = r_b - r_a; masses from the particle types. Energies (which the
+   * reference discards) as 0.5 * e per entry. */
+  int gravitational_forces(double Gc, const double* type_mass, int ntypes, double rcut_g) {
+    const double rc2 = rcut_g * rcut_g;
+    int err = 0;
+#pragma omp parallel for schedule(dynamic) reduction(| : err)
+    for (long c = 0; c < static_cast<long>(cells.size()); ++c) {
+      Cell& A = cells[c];
+      const L3 la = gloc(c);
+      for (size_t q = 0; q < A.size(); ++q) { A.fx[q] = 0.0; A.fy[q] = 0.0; A.fz[q] = 0.0; A.pe[q] = 0.0; }
+      if (is_ghost(la)) continue;
+      const size_t na = A.size();
+      if (na == 0) continue;
+      const uint16_t* base = streams[c].data();
+      const uint16_t* stream_base = base + (na + 1) * 2;
+      const uint32_t* offset = reinterpret_cast<const uint32_t*>(base);
+      for (size_t pa = 0; pa < na; ++pa) {
+        const uint16_t* st = stream_base + offset[pa] - 1;
+        int groups = *(st++);
+        if (A.type[pa] >= ntypes) { err |= 1; continue; }
+        const double mass_a = type_mass[A.type[pa]];
+        double fx = 0.0, fy = 0.0, fz = 0.0, e_sum = 0.0;
+        while (groups > 0) {
+          const uint16_t enc = *(st++);
+          int nch = *(st++);
+          const long ri = static_cast<long>(enc & 31) - 16;
+          const long rj = static_cast<long>((enc >> 5) & 31) - 16;
+          const long rk = static_cast<long>((enc >> 10) & 31) - 16;
+          const Cell& B = cells[c + ((rk * G[1]) + rj) * G[0] + ri];
+          --groups;
+          while (nch > 0) {
+            const unsigned pb = *(st++);
+            --nch;
+            const double drx = B.rx[pb] - A.rx[pa];
+            const double dry = B.ry[pb] - A.ry[pa];
+            const double drz = B.rz[pb] - A.rz[pa];
+            const double d2 = norm2(drx, dry, drz);
+            if (d2 > 0.0 && d2 <= rc2) {
+              if (B.type[pb] >= ntypes) { err |= 1; continue; }
+              const double mass_b = type_mass[B.type[pb]];
+              const double r = std::sqrt(d2);
+              const double inv_r = 1.0 / r;
+              const double e = -Gc * mass_a * mass_b * inv_r;
+              double de = Gc * mass_a * mass_b * inv_r * inv_r;
+              de *= 1.0 / r;
+              fx += de * drx;
+              fy += de * dry;
+              fz += de * drz;
+              e_sum += 0.5 * e;
+            }
+          }
+        }
+        A.fx[pa] = fx;
+        A.fy[pa] = fy;
+        A.fz[pa] = fz;
+        A.pe[pa] = e_sum;
+      }
+    }
+    return err ? -4 : 0;
+  }
+
+  /* type of each particle by id; ghost copies follow their owner */
+  int set_types(const uint64_t* ids, const uint8_t* types, int64_t n) {
+    std::vector<std::pair<uint64_t, uint8_t>> t(static_cast<size_t>(n));
+    for (int64_t q = 0; q < n; ++q) t[static_cast<size_t>(q)] = {ids[q], types[q]};
+    std::sort(t.begin(), t.end());
+    long matched = 0;
+    for (auto& cell : cells)
+      for (size_t q = 0; q < cell.size(); ++q) {
+        auto it = std::lower_bound(t.begin(), t.end(), std::make_pair(cell.id[q], static_cast<uint8_t>(0)));
+        if (it != t.end() && it->first == cell.id[q]) { cell.type[q] = it->second; ++matched; }
+      }
+    for (const GhostSend& gs : ghosts) {
+      const Cell& s = cells[gs.src_cell];
+      Cell& d = cells[gs.dst_cell];
+      for (size_t q = 0; q < gs.particle_i.size() && q < d.size(); ++q) d.type[q] = s.type[gs.particle_i[q]];
+    }
+    return static_cast<int>(matched > 0 ? 0 : -1);
   }
 
   /* PushVec3SecondOrderFunctor (defbox/include/exanb/defbox/push_vec3_2nd_order.h:29-38,
@@ -883,6 +970,14 @@ int xo_get_cell_stream(const xo_sys* s, int64_t ci, uint16_t* out) {
   const auto& v = s->streams[s->interior_to_grid(static_cast<long>(ci))];
   std::memcpy(out, v.data(), v.size() * sizeof(uint16_t));
   return 0;
+}
+
+int xo_set_types(xo_sys* s, const uint64_t* ids, const uint8_t* types, int64_t n) {
+  return s->set_types(ids, types, n);
+}
+
+int xo_gravitational_force(xo_sys* s, double G, const double* type_mass, int32_t ntypes, double rcut) {
+  return s->gravitational_forces(G, type_mass, ntypes, rcut);
 }
 
 int xo_energy(const xo_sys* s, double* ke, double* pe) {

@@ -84,6 +84,11 @@ int64_t xo_cell_stream_size(const xo_sys* s, int64_t interior_cell);
 int xo_get_cell_stream(const xo_sys* s, int64_t interior_cell, uint16_t* out);
 
 /* Kinetic (0.5 m v^2) and truncated-and-shifted LJ potential energy. */
+/* Particle types by id (field::type; 0 until set), ghost copies included. */
+int xo_set_types(xo_sys* s, const uint64_t* ids, const uint8_t* types, int64_t n);
+/* zero_particle_force + gravitational_force (contribs/pi/gravitational_force.cu:42-141)
+ * over the current streams with cutoff rcut (<= the neighbour distance); masses per type. */
+int xo_gravitational_force(xo_sys* s, double G, const double* type_mass, int32_t ntypes, double rcut);
 int xo_energy(const xo_sys* s, double* ke, double* pe);
 
 /* Count of particles over the displacement threshold right now (particle_displ_over). */
