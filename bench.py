@@ -79,10 +79,9 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from exanbody_gb300 import replicas
+
+    return replicas.dist_env()
 
 
 class Clocks:
@@ -259,9 +258,9 @@ def run_ours(args):
         e1.synchronize()
         ms = e0.elapsed_time(e1)
         if world > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+            from exanbody_gb300 import replicas
+
+            ms = replicas.max_over_ranks(ms, device=dev)  # the job's time is its slowest rank's
         return ms
 
     # Each precision is timed with both traversals (full lists: every pair from

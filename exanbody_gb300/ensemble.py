@@ -20,7 +20,7 @@ import time
 
 import numpy as np
 
-from . import workloads, xnb
+from . import replicas, workloads, xnb
 
 DEFAULTS = dict(stage_cap=640, force_block=128, skin=0.3, newton=False)
 
@@ -114,7 +114,16 @@ def main():
     args = ap.parse_args()
     import torch
 
-    specs = workloads.ensemble_specs(args.count, seed=args.seed)
+    rank, world, local = replicas.dist_env()
+    dev = None
+    if world > 1:
+        # replicas: each GPU advances every world-th system of the ensemble
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        torch.cuda.set_device(local)
+        dev = torch.device("cuda", local)
+    specs = replicas.shard(workloads.ensemble_specs(args.count, seed=args.seed), rank, world)
     systems = make_systems(specs)
     stream = torch.cuda.Stream()
     cfg = dict(DEFAULTS)
@@ -124,8 +133,9 @@ def main():
         sample = systems[: args.tune_sample]
         cfg, _, tune_log = autotune(sample, xnb.PREC_MIXED, tune_skin=args.tune_skin, stream=stream)
     tune_s = time.perf_counter() - t0
-    out = {"workload": "ensemble_%d_fcc_n4-25_rho0.70-1.00_T0.7-1.5" % args.count,
-           "atoms": int(sum(w["n_atoms"] for w in systems)), "systems": args.count, "steps": args.steps,
+    out = {"workload": "ensemble_%d_fcc_n4-25_rho0.70-1.00_T0.7-1.5" % args.count, "gpus": world,
+           "atoms": int(replicas.gather_values([sum(w["n_atoms"] for w in systems)], device=dev).sum()),
+           "systems": args.count, "steps": args.steps,
            "config": cfg, "autotune_seconds": tune_s}
     # the mixed path runs the tuned configuration; the FP64 path is timed with both
     # traversals (full lists, Newton half lists) and reported at its faster one
@@ -137,14 +147,19 @@ def main():
         secs, done = timed_steps(b, stream, args.steps, prec)
         rebuilds = sum(b.info(s).rebuilds for s in ids)
         b.close()
-        out[name] = {"atom_steps_per_s": n * done / secs, "seconds": secs, "steps": done,
+        # whole job: all ranks' atoms over the slowest rank's time
+        secs = replicas.max_over_ranks(secs, device=dev)
+        n_all = replicas.gather_values([n], device=dev).sum()
+        rebuilds = replicas.gather_values([rebuilds], device=dev).sum()
+        out[name] = {"atom_steps_per_s": float(n_all) * done / secs, "seconds": secs, "steps": done,
                      "rebuilds_total": int(rebuilds)}
     best = max(("fp64_full", "fp64_newton"), key=lambda k: out[k]["atom_steps_per_s"])
     out["fp64"] = dict(out[best], traversal=best)
     out["speedup_mixed_vs_fp64"] = out["mixed"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"]
     if tune_log is not None:
         out["autotune_trials"] = tune_log
-    print(json.dumps(out))
+    if rank == 0:
+        print(json.dumps(out))
 
 
 if __name__ == "__main__":

@@ -25,7 +25,7 @@ import time
 
 import numpy as np
 
-from . import workloads, xnb
+from . import replicas, workloads, xnb
 
 BYTES_LIST_PER_ATOM = 160.0  # neighbour slot entries per atom for admission (rho <= 1, x1.25 margin)
 
@@ -149,12 +149,17 @@ def serve_sequential(requests, prebuilt=None, precision=xnb.PREC_FP64, time_limi
     return records, time.perf_counter() - t0, atom_steps
 
 
-def summarize(records, wall, atom_steps):
+def summarize(records, wall, atom_steps, device=None):
+    """Completion-latency percentiles and throughput; under torchrun the latencies
+    of all ranks are gathered and the wall time is the slowest rank's."""
     lat = np.array([r["latency"] for r in records.values() if "latency" in r])
+    lat = replicas.gather_values(lat, device=device)
+    wall = replicas.max_over_ranks(wall, device=device)
+    atom_steps = replicas.gather_values([atom_steps], device=device).sum()
     return {"completed": int(len(lat)), "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
             "mean_s": float(lat.mean()) if len(lat) else None, "wall_s": wall,
-            "atom_steps_per_s": atom_steps / wall}
+            "atom_steps_per_s": float(atom_steps) / wall}
 
 
 def main():
@@ -168,8 +173,17 @@ def main():
     args = ap.parse_args()
     import torch
 
+    rank, world, local = replicas.dist_env()
+    dev = None
+    if world > 1:
+        # replicas: each GPU serves every world-th request of the one stream
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        torch.cuda.set_device(local)
+        dev = torch.device("cuda", local)
     torch.cuda.init()
-    reqs = workloads.serving_stream(args.requests, seed=args.seed, rate=1.0)
+    reqs = replicas.shard(workloads.serving_stream(args.requests, seed=args.seed, rate=1.0), rank, world)
     prebuilt = [request_system(r) for r in reqs]
     work = sum(w["n_atoms"] * r["steps"] for w, r in zip(prebuilt, reqs))
     rate = args.rate
@@ -181,7 +195,9 @@ def main():
         rec, wall, ast = srv.serve(probe, prebuilt[: len(probe)])
         srv.close()
         mean_work = work / len(reqs)
-        capacity = ast / wall / mean_work  # requests per second
+        capacity = ast / wall / mean_work  # requests per second of one GPU
+        # the whole stream arrives at 0.8 x the capacity of all GPUs (the slowest one's x world)
+        capacity = -replicas.max_over_ranks(-capacity, device=dev) * world
         rate = 0.8 * capacity
     # rescale the unit-rate arrival times of the seeded stream to the chosen rate
     for r in reqs:
@@ -191,13 +207,14 @@ def main():
     srv.close()
     out = {"workload": "serving_%d_requests_fcc_n5-40_steps200-2000" % args.requests,
            "arrival_rate_per_s": rate, "capacity_req_per_s": capacity, "budget_gb": args.budget_gb,
-           "chunk_steps": args.chunk, "total_atom_steps": work,
-           "batched_mixed": summarize(rec, wall, ast)}
+           "chunk_steps": args.chunk, "total_atom_steps": int(replicas.gather_values([work], device=dev).sum()),
+           "gpus": world, "batched_mixed": summarize(rec, wall, ast, dev)}
     if not args.no_baseline:
         # the plain FP64 path at its faster traversal on one system at a time (Newton half lists)
         rec, wall, ast = serve_sequential(reqs, prebuilt, precision=xnb.PREC_FP64 | xnb.PREC_NEWTON)
-        out["sequential_fp64"] = dict(summarize(rec, wall, ast), traversal="newton")
-    print(json.dumps(out))
+        out["sequential_fp64"] = dict(summarize(rec, wall, ast, dev), traversal="newton")
+    if rank == 0:
+        print(json.dumps(out))
 
 
 if __name__ == "__main__":
