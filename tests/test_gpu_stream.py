@@ -135,3 +135,28 @@ def test_stale_lists_are_refused():
     b.chunk_neighbors(s)
     buf, off = b.chunk_neighbors_stream(s, 1)
     assert len(buf) > 0
+
+
+def test_full_size_lists_are_the_fp64_neighbour_sets():
+    """The 4,000,000-atom benchmark system on the mixed path: at init and after
+    each rebuild of 40 steps, every list equals the exhaustive FP64 search of the
+    27-cell block (no missing or extra pair, no self, order and format kept)."""
+    w = workloads.lj_fcc_system(100, 0.8442, 1.44, 12345)
+    b = new_batch([w["n_atoms"]], [ncells(w["geom"])], list_per_atom=160.0)
+    s = b.add_system(xnb.lj_params(w["geom"]), w["r"], w["v"], w["id"], list_factor=1.2)
+    b.init_particles(s, xnb.PREC_MIXED)
+    checked = 0
+
+    def check():
+        buf, off = b.chunk_neighbors_stream(s, 2)
+        res = b.verify_chunk_neighbors(s, buf, off, 2)
+        assert all(v == 0 for v in res.values()), res
+
+    check()
+    for _ in range(40):
+        r0 = b.info(s).rebuilds
+        b.step(1, xnb.PREC_MIXED, xnb.STEP_HOST_SYNC)
+        if b.info(s).rebuilds != r0:
+            check()
+            checked += 1
+    assert checked >= 4
