@@ -845,11 +845,8 @@ int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const D
                      cudaStream_t stream) {
   if (ex.n_cells == 0) return 0;
   const size_t smem = static_cast<size_t>(cap) * sizeof(float4) + static_cast<size_t>(4) * 2 * lbuf * sizeof(uint32_t);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_neighbors, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    attr_set = true;
-  }
+  // a per-device attribute: set it on the current device every time (a host call, no GPU work)
+  cudaFuncSetAttribute(k_neighbors, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
   k_nbr_reset<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild);
   k_neighbors<<<warp_grid(ex.n_cells, 1, ex.sm_count), 128, smem, stream>>>(ex.n_cells, sys, st, a, cap, lbuf);
   return 2;
