@@ -995,6 +995,83 @@ int xnb_check_errors(xnb_batch* b, void* stream) {
   return XNB_OK;
 }
 
+int xnb_batch_set_tuning(xnb_batch* b, int32_t stage_cap, int32_t force_block) {
+  if (!b) return fail(XNB_ERR_ARG, "null batch");
+  if (stage_cap <= 0 || stage_cap > 1024) return fail(XNB_ERR_ARG, "stage_cap must be in 1..1024");
+  if (force_block <= 0 || force_block % 32 || force_block > 256)
+    return fail(XNB_ERR_ARG, "force_block must be a multiple of 32 and at most 256");
+  b->stage_cap = (stage_cap + 31) / 32 * 32;
+  b->force_block = force_block;
+  return XNB_OK;
+}
+
+int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* stream, xnb_tuning* out) {
+  if (!b || !out) return fail(XNB_ERR_ARG, "null argument");
+  if (trial_steps <= 0) return fail(XNB_ERR_ARG, "trial_steps must be positive");
+  if (precision != XNB_PREC_FP64 && precision != XNB_PREC_MIXED)
+    return fail(XNB_ERR_ARG, "autotune for XNB_PREC_FP64 or XNB_PREC_MIXED");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  XCK(cudaSetDevice(b->device));
+  uint64_t atoms = 0;
+  for (const SysHost& h : b->sys)
+    if (h.active) atoms += h.d.npart;
+  if (atoms == 0) return fail(XNB_ERR_ARG, "no resident particles");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  XCK(cudaEventCreate(&e0));
+  XCK(cudaEventCreate(&e1));
+  int trials = 0;
+  auto rate_of = [&](int sc, int fb, int nw, double* rate) -> int {
+    int rc = xnb_batch_set_tuning(b, sc, fb);
+    if (rc) return rc;
+    const int32_t prec = precision | (nw ? XNB_PREC_NEWTON : 0);
+    rc = xnb_step(b, 1, prec, 0, stream);
+    if (rc) return rc;
+    if (cudaEventRecord(e0, st) != cudaSuccess) return fail(XNB_ERR_CUDA, "event record");
+    rc = xnb_step(b, trial_steps, prec, 0, stream);
+    if (rc) return rc;
+    if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+      return fail(XNB_ERR_CUDA, "event sync");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ++trials;
+    *rate = static_cast<double>(atoms) * trial_steps / (static_cast<double>(ms) * 1e-3);
+    return xnb_check_errors(b, stream);
+  };
+  const int caps[3] = {384, 640, 1024}, blocks[2] = {128, 256};
+  int best_sc = b->stage_cap, best_fb = b->force_block, best_nw = 0;
+  double best = 0.0;
+  int rc = rate_of(best_sc, best_fb, best_nw, &best);
+  // coordinate search: one parameter at a time, the others at their best so far
+  for (int pass = 0; pass < 3 && rc == 0; ++pass) {
+    for (int v = 0; v < (pass == 0 ? 3 : (pass == 1 ? 2 : 2)) && rc == 0; ++v) {
+      int sc = best_sc, fb = best_fb, nw = best_nw;
+      if (pass == 0) sc = caps[v];
+      else if (pass == 1) fb = blocks[v];
+      else nw = v;
+      if (sc == best_sc && fb == best_fb && nw == best_nw) continue;
+      double r = 0.0;
+      rc = rate_of(sc, fb, nw, &r);
+      if (rc == 0 && r > best) {
+        best = r;
+        best_sc = sc;
+        best_fb = fb;
+        best_nw = nw;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  rc = xnb_batch_set_tuning(b, best_sc, best_fb);
+  if (rc) return rc;
+  out->stage_cap = best_sc;
+  out->force_block = best_fb;
+  out->newton = best_nw;
+  out->trials = trials;
+  out->atom_steps_per_s = best;
+  return XNB_OK;
+}
+
 int xnb_chunk_neighbors_stream(xnb_batch* b, int32_t s, int32_t offset_tables, uint16_t* stream, int64_t cap,
                                uint64_t* cell_offsets, int64_t* total_out, void* cuda_stream) {
   int rc = check_sys(b, s);

@@ -33,7 +33,7 @@ EXPORTED = [
     "xnb_ghost_update_r", "xnb_step", "xnb_step_graph_create", "xnb_graph_launch", "xnb_graph_destroy",
     "xnb_check_errors", "xnb_stats_kernel_launches", "xnb_chunk_neighbors_noalloc", "xnb_chunk_neighbors_stream",
     "xnb_verify_chunk_neighbors", "xnb_simulation_stats", "xnb_sample_particles", "xnb_system_set_types",
-    "xnb_gravitational_force",
+    "xnb_gravitational_force", "xnb_batch_set_tuning", "xnb_autotune",
 ]
 
 FORCE_ENERGY = 1
@@ -69,6 +69,16 @@ class SimStats(C.Structure):
         ("max_vel", C.c_double),
         ("min_acc", C.c_double),
         ("max_acc", C.c_double),
+    ]
+
+
+class Tuning(C.Structure):
+    _fields_ = [
+        ("stage_cap", C.c_int32),
+        ("force_block", C.c_int32),
+        ("newton", C.c_int32),
+        ("trials", C.c_int32),
+        ("atom_steps_per_s", C.c_double),
     ]
 
 
@@ -159,6 +169,8 @@ def load(build_if_missing=True):
     lib.xnb_sample_particles.argtypes = [vp, i32, P(u64), i64, P(d), P(i32), vp]
     lib.xnb_system_set_types.argtypes = [vp, i32, P(u64), P(C.c_uint8), i64, P(i64), vp]
     lib.xnb_gravitational_force.argtypes = [vp, i32, d, P(d), i32, d, i32, i32, vp]
+    lib.xnb_batch_set_tuning.argtypes = [vp, i32, i32]
+    lib.xnb_autotune.argtypes = [vp, i32, i32, vp, P(Tuning)]
     _LIB = lib
     return lib
 
@@ -376,6 +388,16 @@ class Batch:
         flags = (FORCE_ENERGY if energy else 0) | (FORCE_ACCUMULATE if accumulate else 0)
         _ck(self.lib.xnb_gravitational_force(self.h, s, float(G), masses.ctypes.data_as(C.POINTER(C.c_double)),
                                              len(masses), float(rcut), int(precision), flags, self.stream))
+
+    def set_tuning(self, stage_cap, force_block):
+        _ck(self.lib.xnb_batch_set_tuning(self.h, int(stage_cap), int(force_block)))
+
+    def autotune(self, trial_steps=20, precision=PREC_MIXED):
+        """Online autotuner (xnb_autotune): the batch advances while it is timed and is
+        left on the fastest configuration; returns it as a dict."""
+        t = Tuning()
+        _ck(self.lib.xnb_autotune(self.h, int(trial_steps), int(precision), self.stream, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in Tuning._fields_}
 
     def check_errors(self):
         _ck(self.lib.xnb_check_errors(self.h, self.stream))

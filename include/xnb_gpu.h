@@ -180,6 +180,27 @@ int xnb_check_errors(xnb_batch* b, void* stream);
  * the reference's equivalent bookkeeping lives in onika's profiling layer). */
 int64_t xnb_stats_kernel_launches(const xnb_batch* b);
 
+/* ---- tuning ---- */
+
+typedef struct xnb_tuning {
+  int32_t stage_cap;          /* neighbour-build candidates staged per cell round */
+  int32_t force_block;        /* threads per block of the full-list force traversal */
+  int32_t newton;             /* 1: XNB_PREC_NEWTON traversal */
+  int32_t trials;             /* configurations timed */
+  double atom_steps_per_s;    /* the chosen configuration's measured rate */
+} xnb_tuning;
+
+/* Changes the launch configuration of a live batch (same limits as at creation). */
+int xnb_batch_set_tuning(xnb_batch* b, int32_t stage_cap, int32_t force_block);
+/* Online autotuner: coordinate search over stage_cap {384, 640, 1024},
+ * force_block {128, 256} and the Newton traversal, each configuration timed
+ * (CUDA events on `stream`) over trial_steps of xnb_step without host sync
+ * after one untimed step. The trials are real MD steps: the batch advances
+ * (1 + trial_steps) x trials steps. The batch is left on the fastest
+ * configuration, which *out describes; precision is the base precision
+ * (XNB_PREC_FP64 or XNB_PREC_MIXED) the run will use. Synchronises. */
+int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* stream, xnb_tuning* out);
+
 /* ---- reference-format neighbour streams ---- */
 
 /* chunk_neighbors' own output layout (GridChunkNeighbors::m_cell_stream,

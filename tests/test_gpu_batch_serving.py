@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 from exanbody_gb300 import ensemble, serving, workloads, xnb
-from helpers import force_error, forces
+from helpers import force_error, forces, ncells, new_batch
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -50,3 +50,23 @@ def test_sequential_baseline_runs():
     rec, wall, ast = serving.serve_sequential(reqs, precision=xnb.PREC_FP64)
     summ = serving.summarize(rec, wall, ast)
     assert summ["completed"] == 3 and summ["p99_s"] >= summ["p50_s"] > 0
+
+
+def test_native_online_autotune():
+    """xnb_autotune: times real steps per configuration, leaves the batch on the
+    fastest one, and the batch keeps stepping normally afterwards."""
+    specs = workloads.ensemble_specs(12, seed=9, nmin=5, nmax=9)
+    systems = [workloads.lj_fcc_system(sp["n"], sp["rho"], sp["T"], sp["seed"]) for sp in specs]
+    b = new_batch([w["n_atoms"] for w in systems], [ncells(w["geom"]) for w in systems])
+    ids = [b.add_system(xnb.lj_params(w["geom"]), w["r"], w["v"], w["id"], list_factor=1.25) for w in systems]
+    b.init_particles(-1, xnb.PREC_MIXED)
+    r0 = sum(b.info(s).rebuilds for s in ids)
+    t = b.autotune(10, xnb.PREC_MIXED)
+    assert t["stage_cap"] in (384, 640, 1024) and t["force_block"] in (128, 256) and t["newton"] in (0, 1)
+    assert t["trials"] >= 4 and t["atom_steps_per_s"] > 0
+    assert sum(b.info(s).rebuilds for s in ids) > r0  # the trials were real steps
+    prec = xnb.PREC_MIXED | (xnb.PREC_NEWTON if t["newton"] else 0)
+    b.step(20, prec, 0)
+    b.check_errors()
+    with pytest.raises(xnb.XnbError):
+        b.set_tuning(2048, 128)
