@@ -308,6 +308,37 @@ struct BackupROp : OperatorNode {
 struct LennardJonesOp : OperatorNode {
   void execute(Context& ctx) override {
     if (!ctx.dry_run) ck(xnb_lennard_jones_force(ctx.batch, ctx.sys, ctx.precision, 1, nullptr), "lennard_jones_force");
+    ctx.forces_written = true;
+  }
+};
+
+// zero_particle_force (compute/zero_particle_force.cu:17-53): the force operators
+// that follow start from zero (lennard_jones_force zeroes the field itself).
+struct ZeroForceOp : OperatorNode {
+  void execute(Context& ctx) override { ctx.forces_written = false; }
+};
+
+// gravitational_force (contribs/pi/gravitational_force.cu:167-223): slots
+// config { G }, rcut; the species mass of particle_type_add_properties for every
+// particle (one species here). It adds onto the forces written earlier in the
+// step's force block (lennard_jones_force first when both are used), as chained
+// force operators add onto the zeroed field.
+struct GravityOp : OperatorNode {
+  void execute(Context& ctx) override {
+    const Node* cfg = local("config");
+    const Node* g = cfg ? cfg->find("G") : nullptr;
+    if (!g) throw Error("gravitational_force: config { G } required");
+    const double G = quantity(*g);
+    const Node* rc = local("rcut");
+    if (!rc) throw Error("gravitational_force: rcut required");
+    const double rcut = quantity(*rc);
+    if (ctx.dry_run) return;
+    const double mass = ctx.mass;
+    const int prec = ctx.precision == XNB_PREC_FP64_EXACT ? XNB_PREC_FP64_EXACT : XNB_PREC_FP64;
+    ck(xnb_gravitational_force(ctx.batch, ctx.sys, G, &mass, 1, rcut, prec,
+                               XNB_FORCE_ENERGY | (ctx.forces_written ? XNB_FORCE_ACCUMULATE : 0), nullptr),
+       "gravitational_force");
+    ctx.forces_written = true;
   }
 };
 
@@ -328,8 +359,6 @@ struct MessageOp : OperatorNode {
   }
 };
 
-// simulation_stats + print_simulation_stats (io/simulation_stats.cpp:60-124): kinetic
-// and potential energy of the system.
 // simulation_stats (debug/simulation_stats.cpp:60-124), reduced on the GPU; the
 // kinetic energy printed is 0.5 * m * sum |v|^2 with the species mass.
 struct StatsOp : OperatorNode {
@@ -422,9 +451,11 @@ void register_hot_path_operators() {
   reg<ChunkNeighborsOp>("chunk_neighbors");
   reg<BackupROp>("backup_r");
   reg<LennardJonesOp>("lennard_jones_force");
+  reg<GravityOp>("gravitational_force");
+  reg<ZeroForceOp>("zero_particle_force");
   // folded into move_particles / lennard_jones_force on the GPU, or single-rank no-ops
   for (const char* n : {"migrate_cell_particles", "rebuild_amr", "ghost_comm_scheme", "ghost_update_all",
-                        "ghost_update_r", "amr_grid_pairs", "resize_particle_locks", "zero_particle_force",
+                        "ghost_update_r", "amr_grid_pairs", "resize_particle_locks",
                         "update_force_from_ghost", "divide_force_by_type_scalar", "extend_domain",
                         "simple_cost_model", "load_balance_rcb", "nop", "init_cuda", "mpi_comm_world",
                         "print_grid", "grid_stats", "chunk_neighbors_stats", "dump_data", "final_dump",

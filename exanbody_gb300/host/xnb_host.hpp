@@ -66,6 +66,7 @@ struct Context {
   xnb_batch* batch = nullptr;
   int32_t sys = -1;
   int32_t precision = XNB_PREC_FP64_EXACT;
+  bool forces_written = false;  // a force operator of the current force block has written forces
   long timestep = 0;
   bool verbose = false;
   std::vector<std::string> trace;  // executed operator names (dry runs, tests)

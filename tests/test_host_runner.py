@@ -71,3 +71,24 @@ def test_ni_golden_deck_through_the_operator_runner():
             name = line.split()[1]
             vals[name] = float(line.split("=")[1].split("/")[0])
     assert vals["Position"] < 1e-9 and vals["Acceleration"] < 1e-6 and vals["Velocity"] < 1e-8
+
+
+def test_chained_force_operators(tmp_path):
+    """A force block in the reference's form: zero_particle_force, then
+    lennard_jones_force and gravitational_force (config { G }, rcut, with units)."""
+    deck = tmp_path / "g.msp"
+    deck.write_text(
+        "simulation: main\n"
+        "main:\n  - compute_all_forces_energy\n"
+        "compute_force:\n"
+        "  - lennard_jones_force\n"
+        "  - gravitational_force:\n"
+        "      config: { G: 6.67e-11 }\n"
+        "      rcut: 2.5 ang\n")
+    r = xnb_exec("--dry-run", str(deck))
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.splitlines()[:3] == ["zero_particle_force", "lennard_jones_force", "gravitational_force"]
+    bad = tmp_path / "b.msp"
+    bad.write_text("simulation: main\nmain:\n  - gravitational_force: { rcut: 2.5 }\n")
+    r = xnb_exec("--dry-run", str(bad))
+    assert r.returncode == 1 and "config { G }" in r.stderr
