@@ -2,7 +2,8 @@
 
 Each .cu under csrc/ is compiled in parallel with
     nvcc -gencode arch=compute_103a,code=sm_103a -lineinfo -O3
-and linked into exanbody_gb300/_build/libxnb_gpu.so (in-tree, git-ignored).
+(host-only .cpp files, the dump file codec, through the same driver) and linked
+into exanbody_gb300/_build/libxnb_gpu.so (in-tree, git-ignored).
 Host code is compiled with -ffp-contract=off so host-side geometry (bucketing,
 domain descriptors) rounds exactly like the reference on x86_64 and aarch64.
 """
@@ -33,7 +34,7 @@ def nvcc():
 
 
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def _stale(target, deps):
@@ -66,11 +67,11 @@ def build_host(verbose=False):
 def build(verbose=False, extra_flags=None):
     os.makedirs(OUT, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    headers.append(os.path.join(ROOT, "include", "xnb_gpu.h"))
+    headers += [os.path.join(ROOT, "include", f) for f in ("xnb_gpu.h", "xnb_dump.h")]
     flags = NVCC_FLAGS + (extra_flags or [])
     objs, procs = [], []
     for src in sources():
-        obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(OUT, os.path.splitext(os.path.basename(src))[0] + ".o")
         objs.append(obj)
         if _stale(obj, [src, __file__] + headers):
             cmd = [nvcc(), *ARCH, *flags, "-c", src, "-o", obj]
@@ -81,7 +82,7 @@ def build(verbose=False, extra_flags=None):
         if p.wait() != 0:
             raise RuntimeError("nvcc failed on %s" % src)
     if _stale(LIB, objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB + ".tmp", *objs]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-ldl", "-lpthread"]
         if verbose:
             print(" ".join(cmd), flush=True)
         if subprocess.call(cmd) != 0:

@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/xnb_dump.h"
 #include "../../include/xnb_gpu.h"
 #include "xnb_launch.cuh"
 
@@ -1322,4 +1323,58 @@ int xnb_chunk_neighbors_noalloc(const xnb_lj_params* p, int64_t n, const double*
   return XNB_OK;
 }
 
+int xnb_system_download_types(xnb_batch* b, int32_t s, uint8_t* type, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0 || !type) return fail(XNB_ERR_ARG, "download_types needs one system and an output array");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const SysHost& h = b->sys[s];
+  if (h.d.npart)
+    XCK(cudaMemcpyAsync(type, b->a.ptype + h.d.part_base, h.d.npart, cudaMemcpyDeviceToHost, st));
+  XCK(cudaStreamSynchronize(st));
+  return XNB_OK;
+}
+
+// write_dump (src/io/write_dump.cpp:35-44 over sim_dump_writer.h): the system's
+// particles in storage order -- interior cells in linear order, each cell's
+// particles in order -- as the writer walks the grid, chunks closed at cell
+// boundaries.
+int xnb_system_write_dump(xnb_batch* b, int32_t s, const char* filename, uint64_t timestep, double physical_time,
+                          int32_t compression_level, int64_t max_part_size, uint32_t extra_flags_clear,
+                          void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0) return fail(XNB_ERR_ARG, "write_dump needs one system");
+  const SysHost& h = b->sys[s];
+  const size_t n = h.d.npart;
+  std::vector<double> r[6];
+  for (auto& v : r) v.resize(n);
+  std::vector<uint64_t> id(n);
+  std::vector<int32_t> cell(n);
+  std::vector<uint8_t> type(n);
+  rc = xnb_system_download(b, s, r[0].data(), r[1].data(), r[2].data(), r[3].data(), r[4].data(), r[5].data(),
+                           nullptr, nullptr, nullptr, id.data(), cell.data(), nullptr, stream);
+  if (rc) return rc;
+  rc = xnb_system_download_types(b, s, type.data(), stream);
+  if (rc) return rc;
+  std::vector<int64_t> counts(h.d.ncells, 0);
+  for (size_t q = 0; q < n; ++q) {
+    if (cell[q] < 0 || static_cast<uint32_t>(cell[q]) >= h.d.ncells)
+      return fail(XNB_ERR_DEVICE, "write_dump: a particle has no cell (system in error)");
+    ++counts[static_cast<size_t>(cell[q])];
+  }
+  const int64_t dims[3] = {h.d.dims[0], h.d.dims[1], h.d.dims[2]};
+  xnb_dump_domain dom;
+  const uint32_t flags = (XNB_DOMAIN_PERIODIC_X | XNB_DOMAIN_PERIODIC_Y | XNB_DOMAIN_PERIODIC_Z |
+                          XNB_DOMAIN_EXPANDABLE) & ~extra_flags_clear;
+  xnb_dump_domain_init(&dom, h.d.origin, h.d.extent, dims, h.d.cell_size, flags);
+  return xnb_dump_write(filename, &dom, timestep, physical_time, static_cast<int64_t>(n), r[0].data(), r[1].data(),
+                        r[2].data(), r[3].data(), r[4].data(), r[5].data(), id.data(), type.data(), counts.data(),
+                        static_cast<int64_t>(counts.size()), compression_level, max_part_size, 0, 0);
+}
+
 }  // extern "C"
+
+namespace xnb {
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace xnb

@@ -92,6 +92,7 @@ struct DomainOp : OperatorNode {
           if (quantity(xf->seq.at(r).seq.at(c)) != (r == c ? 1.0 : 0.0))
             throw Error("domain: only the identity xform is supported");
     }
+    if (const Node* ex = local("expandable")) ctx.domain_expandable = to_bool(*ex);
     ctx.params.cell_size = quantity(*cs);
     for (int a = 0; a < 3; ++a) {
       ctx.params.dims[a] = static_cast<int32_t>(to_long(gd->seq.at(a)));
@@ -251,9 +252,17 @@ struct InitParticlesOp : OperatorNode {
       cfg.list_capacity = static_cast<int64_t>((2.0 * 4.18879 * nb * nb * nb * rho + 32.0) * static_cast<double>(n)) + 4096;
       ck(xnb_batch_create(&cfg, &ctx.batch), "xnb_batch_create");
     }
+    // per-cell input (lattice) or flat input placed by periodic location in
+    // input order (read_dump)
     ck(xnb_system_add(ctx.batch, &p, n, h.rx.data(), h.ry.data(), h.rz.data(), h.vx.data(), h.vy.data(),
-                      h.vz.data(), h.id.data(), h.cell_counts.data(), 1.3, nullptr, &ctx.sys),
+                      h.vz.data(), h.id.data(), h.cell_counts.empty() ? nullptr : h.cell_counts.data(), 1.3,
+                      nullptr, &ctx.sys),
        "xnb_system_add");
+    if (std::any_of(h.type.begin(), h.type.end(), [](uint8_t t) { return t != 0; })) {
+      int64_t matched = 0;
+      ck(xnb_system_set_types(ctx.batch, ctx.sys, h.id.data(), h.type.data(), n, &matched, nullptr),
+         "init_particles (types)");
+    }
     ck(xnb_update_particles_full(ctx.batch, ctx.sys, nullptr), "init_particles");
   }
 };
@@ -342,8 +351,13 @@ struct GravityOp : OperatorNode {
   }
 };
 
+// next_time_step: the time step counter and the physical time advance by one step
 struct NextTimeStepOp : OperatorNode {
-  void execute(Context& ctx) override { ++ctx.timestep; }
+  void execute(Context& ctx) override {
+    ++ctx.timestep;
+    ctx.physical_time += ctx.get_double("dt", 0.0);
+    ctx.set_double("physical_time", ctx.physical_time);
+  }
 };
 
 struct SimContinueOp : OperatorNode {
@@ -353,9 +367,105 @@ struct SimContinueOp : OperatorNode {
   }
 };
 
+// message: `message: text` or `message: { mesg: text, endl: bool }`; without a
+// text of its own it prints the `mesg` slot (rebound, e.g., to a file name).
 struct MessageOp : OperatorNode {
   void execute(Context& ctx) override {
-    if (ctx.verbose && m_local.is_scalar()) std::printf("%s\n", m_local.scalar.c_str());
+    if (!ctx.verbose) return;
+    std::string text;
+    bool endl = true;
+    if (m_local.is_scalar()) {
+      text = m_local.scalar;
+    } else {
+      if (const Node* m = local("mesg")) text = m->scalar;
+      else if (auto it = ctx.slots.find("mesg"); it != ctx.slots.end()) text = it->second.scalar;
+      if (const Node* e = local("endl")) endl = to_bool(*e);
+    }
+    std::printf("%s%s", text.c_str(), endl ? "\n" : "");
+  }
+};
+
+// timestep_file (logic/timestep_file_name.cpp:30-52): filename = format % timestep
+struct TimestepFileOp : OperatorNode {
+  void execute(Context& ctx) override {
+    const Node* f = m_local.is_scalar() ? &m_local : local("format");
+    if (!f) throw Error("timestep_file: format required");
+    const std::string& fmt = f->scalar;
+    char buf[4096];
+    const bool is_long = fmt.find("%l") != std::string::npos;
+    const int len = is_long ? std::snprintf(buf, sizeof(buf), fmt.c_str(), ctx.timestep)
+                            : std::snprintf(buf, sizeof(buf), fmt.c_str(), static_cast<int>(ctx.timestep));
+    if (len < 0 || len >= static_cast<int>(sizeof(buf))) throw Error("timestep_file: bad format '" + fmt + "'");
+    ctx.slots["filename"] = Node::make_scalar(buf);
+  }
+};
+
+// a string slot: the operator's own value, else the global slot, else dflt
+std::string slot_string(const Node* local_value, const Context& ctx, const std::string& k, const std::string& dflt) {
+  if (local_value) return local_value->scalar;
+  auto it = ctx.slots.find(k);
+  return (it == ctx.slots.end() || it->second.kind == Node::Null) ? dflt : it->second.scalar;
+}
+
+// write_dump (io/write_dump.cpp:35-44, sim_dump_writer.h:518-547): slots filename
+// ("output.dump"), compression_level (6), max_part_size (-1 = 128 GiB); the
+// time step and physical time of the run.
+struct WriteDumpOp : OperatorNode {
+  void execute(Context& ctx) override {
+    const std::string fn = slot_string(local("filename"), ctx, "filename", "output.dump");
+    const long level = local("compression_level") ? to_long(*local("compression_level"))
+                                                   : ctx.get_long("compression_level", 6);
+    const long mps = local("max_part_size") ? to_long(*local("max_part_size")) : ctx.get_long("max_part_size", -1);
+    if (ctx.dry_run || !gpu_ready(ctx)) return;
+    ck(xnb_system_write_dump(ctx.batch, ctx.sys, fn.c_str(), static_cast<uint64_t>(ctx.timestep), ctx.physical_time,
+                             static_cast<int32_t>(level), mps, ctx.domain_expandable ? 0u : XNB_DOMAIN_EXPANDABLE,
+                             nullptr),
+       "write_dump");
+    if (ctx.verbose) std::printf("write_dump: %s\n", fn.c_str());
+  }
+};
+
+// read_dump (io/read_dump.cpp:36-45, sim_dump_reader.h:430-456): the domain,
+// time step, physical time and particles of a .dump file; the particles go to
+// init_particles in file order and are placed in the cells of their periodic
+// locations (sim_dump_reader.h:293-352).
+struct ReadDumpOp : OperatorNode {
+  void execute(Context& ctx) override {
+    const std::string fn = slot_string(local("filename"), ctx, "filename", "");
+    if (fn.empty()) throw Error("read_dump: filename required");
+    xnb_dump_info info{};
+    if (xnb_dump_read_info(fn.c_str(), &info) != XNB_OK) throw Error(std::string("read_dump: ") + xnb_last_error_string());
+    const xnb_dump_domain& d = info.domain;
+    const uint32_t per = XNB_DOMAIN_PERIODIC_X | XNB_DOMAIN_PERIODIC_Y | XNB_DOMAIN_PERIODIC_Z;
+    if ((d.flags & per) != per) throw Error("read_dump: only fully periodic domains are supported");
+    if (!(d.flags & XNB_DOMAIN_XFORM_IDENTITY)) throw Error("read_dump: only the identity xform is supported");
+    for (int a = 0; a < 3; ++a) {
+      ctx.params.origin[a] = d.bmin[a];
+      ctx.params.extent[a] = d.bmax[a];
+      ctx.params.dims[a] = static_cast<int32_t>(d.grid_dims[a]);
+    }
+    ctx.params.cell_size = d.cell_size;
+    ctx.domain_set = true;
+    ctx.domain_expandable = (d.flags & XNB_DOMAIN_EXPANDABLE) != 0;
+    HostParticles& h = ctx.host;
+    h = HostParticles{};
+    const size_t n = static_cast<size_t>(info.n_particles);
+    h.rx.resize(n);
+    h.ry.resize(n);
+    h.rz.resize(n);
+    h.vx.resize(n);
+    h.vy.resize(n);
+    h.vz.resize(n);
+    h.id.resize(n);
+    h.type.resize(n);
+    int64_t got = 0;
+    if (xnb_dump_read(fn.c_str(), static_cast<int64_t>(n), h.rx.data(), h.ry.data(), h.rz.data(), h.vx.data(),
+                      h.vy.data(), h.vz.data(), h.id.data(), h.type.data(), &got, nullptr) != XNB_OK)
+      throw Error(std::string("read_dump: ") + xnb_last_error_string());
+    ctx.timestep = static_cast<long>(info.timestep);
+    ctx.physical_time = info.physical_time;
+    ctx.set_double("physical_time", ctx.physical_time);
+    if (ctx.verbose) std::printf("read_dump: %s, %lld particles, timestep %ld\n", fn.c_str(), static_cast<long long>(got), ctx.timestep);
   }
 };
 
@@ -458,12 +568,15 @@ void register_hot_path_operators() {
                         "ghost_update_r", "amr_grid_pairs", "resize_particle_locks",
                         "update_force_from_ghost", "divide_force_by_type_scalar", "extend_domain",
                         "simple_cost_model", "load_balance_rcb", "nop", "init_cuda", "mpi_comm_world",
-                        "print_grid", "grid_stats", "chunk_neighbors_stats", "dump_data", "final_dump",
+                        "print_grid", "grid_stats", "chunk_neighbors_stats", "dump_data",
                         "memory_stats", "print_log_if_triggered", "dump_data_if_triggered"})
     reg<NopOp>(n);
   reg<NextTimeStepOp>("next_time_step");
   reg<SimContinueOp>("sim_continue");
   reg<MessageOp>("message");
+  reg<TimestepFileOp>("timestep_file");
+  reg<WriteDumpOp>("write_dump");
+  reg<ReadDumpOp>("read_dump");
   reg<StatsOp>("simulation_stats");
   reg<NopOp>("print_simulation_stats");
   reg<CheckValuesOp>("check_values");

@@ -2,7 +2,7 @@
 //
 // The default operator graph below has the block names and order of the
 // reference's data/config decks (main-config.msp, compute-loop.msp,
-// numerical-scheme.msp, update-particles.msp), restated for the GPU operators
+// numerical-scheme.msp, update-particles.msp, dump-data.msp), restated for the GPU operators
 // of this library; a user deck overrides or extends blocks by name ('+name'
 // appends), sets slot defaults of an operator by a map under its name, and
 // chooses the block to run with `simulation:`.
@@ -32,7 +32,15 @@ default_simulation:
 global: {}
 input_data: nop
 simulation_epilog: nop
-final_dump: nop
+final_dump: dump_data_particles
+dump_data_particles:
+  - timestep_file: "particles_%09d.dump"
+  - message: { mesg: "Write " , endl: false }
+  - print_dump_file:
+      rebind: { mesg: filename }
+      body:
+        - message: { endl: true }
+  - write_dump
 first_iteration:
   - init_particles
   - print_grid
@@ -190,28 +198,7 @@ void Runner::run_named(const std::string& name, const Node* params) {
     } else if (blk.is_seq()) {
       for (const auto& item : blk.seq) run_item(item);
     } else if (is_flow_map(blk)) {
-      const Node* cond = blk.find("condition");
-      const Node* body = blk.find("body");
-      const Node* reb = blk.find("rebind");
-      const bool loop = blk.find("loop") && to_bool(*blk.find("loop"));
-      auto body_once = [&]() {
-        if (reb)
-          for (const auto& kv : reb->map)
-            if (m_ctx.slots.count(kv.second.scalar)) m_ctx.slots[kv.first] = m_ctx.slots[kv.second.scalar];
-        if (body && body->is_seq())
-          for (const auto& item : body->seq) run_item(item);
-        if (reb)
-          for (const auto& kv : reb->map)
-            if (m_ctx.slots.count(kv.first)) {
-              m_ctx.slots[kv.second.scalar] = m_ctx.slots[kv.first];
-              m_ctx.slots.erase(kv.first);
-            }
-      };
-      if (loop) {
-        while (!cond || condition_value(cond->scalar)) body_once();
-      } else if (!cond || condition_value(cond->scalar)) {
-        body_once();
-      }
+      run_flow(blk);
     } else if (blk.is_map()) {
       for (const auto& kv : blk.map) m_ctx.slots[kv.first] = kv.second;
     }
@@ -226,10 +213,40 @@ void Runner::run_named(const std::string& name, const Node* params) {
     op->set_local(local);
     m_ctx.trace.push_back(name);
     op->execute(m_ctx);
+  } else if (params && is_flow_map(*params)) {
+    // an inline batch: `name: { rebind: ..., body: [...] }` (e.g. print_dump_file
+    // in dump-data.msp:15-19)
+    m_ctx.trace.push_back(name);
+    run_flow(*params);
   } else {
     throw Error("unknown block or operator '" + name + "'");
   }
   --m_depth;
+}
+
+void Runner::run_flow(const Node& blk) {
+  const Node* cond = blk.find("condition");
+  const Node* body = blk.find("body");
+  const Node* reb = blk.find("rebind");
+  const bool loop = blk.find("loop") && to_bool(*blk.find("loop"));
+  auto body_once = [&]() {
+    if (reb)
+      for (const auto& kv : reb->map)
+        if (m_ctx.slots.count(kv.second.scalar)) m_ctx.slots[kv.first] = m_ctx.slots[kv.second.scalar];
+    if (body && body->is_seq())
+      for (const auto& item : body->seq) run_item(item);
+    if (reb)
+      for (const auto& kv : reb->map)
+        if (m_ctx.slots.count(kv.first)) {
+          m_ctx.slots[kv.second.scalar] = m_ctx.slots[kv.first];
+          m_ctx.slots.erase(kv.first);
+        }
+  };
+  if (loop) {
+    while (!cond || condition_value(cond->scalar)) body_once();
+  } else if (!cond || condition_value(cond->scalar)) {
+    body_once();
+  }
 }
 
 void Runner::run_item(const Node& item) {

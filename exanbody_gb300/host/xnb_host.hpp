@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "xnb_dump.h"
 #include "xnb_gpu.h"
 
 namespace xnbhost {
@@ -54,12 +55,14 @@ struct HostParticles {
   std::vector<int64_t> cell_counts;
   std::vector<double> rx, ry, rz, vx, vy, vz;
   std::vector<uint64_t> id;
+  std::vector<uint8_t> type;  // empty: all type 0
 };
 
 struct Context {
   std::map<std::string, Node> slots;  // global slot values (YAML scalars / maps)
   xnb_lj_params params{};
   bool domain_set = false;
+  bool domain_expandable = true;  // Domain() starts expandable (core/include/exanb/core/domain.h:104)
   double mass = 1.0;
   bool divide_by_mass = false;
   HostParticles host;
@@ -68,6 +71,7 @@ struct Context {
   int32_t precision = XNB_PREC_FP64_EXACT;
   bool forces_written = false;  // a force operator of the current force block has written forces
   long timestep = 0;
+  double physical_time = 0.0;
   bool verbose = false;
   std::vector<std::string> trace;  // executed operator names (dry runs, tests)
   bool dry_run = false;
@@ -136,6 +140,7 @@ class Runner {
 
  private:
   void run_named(const std::string& name, const Node* params);
+  void run_flow(const Node& blk);
   bool condition_value(const std::string& name);
   Context& m_ctx;
   std::map<std::string, Node> m_blocks;

@@ -1,12 +1,13 @@
 """The C-ABI library builds for sm_103a, loads, and exports every entry point
-declared in include/xnb_gpu.h (no compute calls: no GPU needed)."""
+declared in include/xnb_gpu.h and include/xnb_dump.h (no compute calls: no GPU
+needed)."""
 import ctypes
 import os
 import re
 
 import pytest
 
-from exanbody_gb300 import build, xnb
+from exanbody_gb300 import build, dump, xnb
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -29,6 +30,14 @@ def test_library_builds_and_exports_header_symbols():
 
 def test_binding_covers_header():
     assert set(declared("xnb_gpu.h")) == set(xnb.EXPORTED)
+
+
+def test_dump_header_symbols_exported_and_bound():
+    lib = ctypes.CDLL(build.build())
+    names = declared("xnb_dump.h")
+    assert set(names) == set(dump.EXPORTED)
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
 
 
 def test_version_and_error_string_without_gpu():

@@ -3,6 +3,7 @@ structure and step order, and the error behaviour (no GPU needed: --dry-run)."""
 import os
 import subprocess
 
+import numpy as np
 import pytest
 
 from exanbody_gb300 import build
@@ -11,12 +12,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 DECK = os.path.join(HERE, "decks", "lj_ni_golden.msp")
 
 
-def xnb_exec(*args):
+def xnb_exec(*args, cwd=None):
     exe = build.build_host() if os.path.exists(build.LIB) else None
     if exe is None:
         build.build()
         exe = build.EXEC
-    return subprocess.run([exe, *args], capture_output=True, text=True, timeout=120)
+    return subprocess.run([exe, *args], capture_output=True, text=True, timeout=300, cwd=cwd)
 
 
 def test_dry_run_follows_the_numerical_scheme():
@@ -36,7 +37,9 @@ def test_dry_run_follows_the_numerical_scheme():
                     "lennard_jones_force", "update_force_from_ghost", "divide_force_by_type_scalar", "push_f_v",
                     "next_time_step", "sim_continue"]
     assert ops.count("push_f_v_r") == 100
-    assert ops[-1] == "check_values"
+    # simulation_epilog, then final_dump = dump_data_particles (dump-data.msp:31-43)
+    assert ops[ops.index("check_values"):] == ["check_values", "timestep_file", "message", "print_dump_file",
+                                               "message", "write_dump"]
     assert "done, 100 steps" in r.stdout
 
 
@@ -61,9 +64,10 @@ def test_units_and_overrides(tmp_path):
 
 
 @pytest.mark.gpu
-def test_ni_golden_deck_through_the_operator_runner():
-    """The reference-style regression deck passes its check_values on the GPU."""
-    r = xnb_exec(DECK)
+def test_ni_golden_deck_through_the_operator_runner(tmp_path):
+    """The reference-style regression deck passes its check_values on the GPU
+    (and leaves its final dump in the working directory)."""
+    r = xnb_exec(DECK, cwd=tmp_path)
     assert r.returncode == 0, r.stdout + r.stderr
     vals = {}
     for line in r.stdout.splitlines():
@@ -92,3 +96,48 @@ def test_chained_force_operators(tmp_path):
     bad.write_text("simulation: main\nmain:\n  - gravitational_force: { rcut: 2.5 }\n")
     r = xnb_exec("--dry-run", str(bad))
     assert r.returncode == 1 and "config { G }" in r.stderr
+
+
+def _deck_body(end, epilog="nop"):
+    """The Ni deck without its golden check, ending at `end`."""
+    text = open(DECK).read().split("simulation_epilog:")[0]
+    return text.replace("simulation_end_iteration: 100", "simulation_end_iteration: %d" % end) + \
+        "simulation_epilog: %s\n" % epilog
+
+
+@pytest.mark.gpu
+def test_restart_from_final_dump_through_read_dump(tmp_path):
+    """final_dump writes particles_%09d.dump; a deck whose input_data is
+    read_dump continues from it. 30 + 30 steps agree with 60 steps in one run to
+    rounding (the restart re-bins particles, so pair orders may differ)."""
+    from exanbody_gb300 import dump
+
+    a, c = tmp_path / "a", tmp_path / "c"
+    a.mkdir()
+    c.mkdir()
+    (a / "a.msp").write_text(_deck_body(30))
+    r = xnb_exec(str(a / "a.msp"), cwd=a)
+    assert r.returncode == 0, r.stdout + r.stderr
+    first = a / "particles_000000031.dump"
+    info = dump.read_info(first)
+    assert info["timestep"] == 31 and info["n_particles"] == 16384
+    ni_input = ("input_data:\n  - particle_types\n  - particle_type_add_properties:\n      Ni: { mass: 58.693 Da }\n"
+                "  - read_dump: { filename: %s }\n" % first)
+    body = _deck_body(61)
+    body = body.replace(body[body.index("input_data:"): body.index("replicate_domain:")], ni_input + "\n")
+    (a / "b.msp").write_text(body)
+    r = xnb_exec(str(a / "b.msp"), cwd=a)
+    assert r.returncode == 0, r.stdout + r.stderr
+    (c / "c.msp").write_text(_deck_body(60))
+    r = xnb_exec(str(c / "c.msp"), cwd=c)
+    assert r.returncode == 0, r.stdout + r.stderr
+    restarted = dump.read(a / "particles_000000062.dump")
+    straight = dump.read(c / "particles_000000061.dump")
+    assert restarted["info"]["physical_time"] == pytest.approx(straight["info"]["physical_time"] + 2e-3, rel=1e-12)
+    o1, o2 = np.argsort(restarted["id"]), np.argsort(straight["id"])
+    assert np.array_equal(restarted["id"][o1], straight["id"][o2])
+    L = np.array(straight["info"]["domain"]["extent"]) - np.array(straight["info"]["domain"]["origin"])
+    dr = restarted["r"][o1] - straight["r"][o2]
+    dr -= L * np.round(dr / L)
+    assert np.max(np.abs(dr)) < 1e-9
+    assert np.max(np.abs(restarted["v"][o1] - straight["v"][o2])) < 1e-9
