@@ -10,6 +10,7 @@
 #include "../../include/xnb_dump.h"
 #include "../../include/xnb_gpu.h"
 #include "xnb_launch.cuh"
+#include "xnb_snap.cuh"
 
 using namespace xnb;
 
@@ -1292,6 +1293,69 @@ int xnb_gravitational_force(xnb_batch* b, int32_t s, double G, const double* typ
 }
 
 int64_t xnb_stats_kernel_launches(const xnb_batch* b) { return b ? static_cast<int64_t>(b->launches) : -1; }
+
+}  // extern "C"
+
+struct xnb_snap {
+  int device = 0;
+  SnapArgs t{};
+  std::vector<void*> allocs;
+};
+
+extern "C" {
+
+int xnb_snap_create(const xnb_snap_params* p, int32_t device, xnb_snap** out) {
+  if (!p || !out) return fail(XNB_ERR_ARG, "xnb_snap_create: params and out required");
+  *out = nullptr;
+  auto* s = new xnb_snap();
+  s->device = device;
+  std::string err;
+  const int rc = snap_build(*p, device, s->t, s->allocs, err);
+  if (rc != XNB_OK) {
+    for (void* q : s->allocs) cudaFree(q);
+    delete s;
+    return fail(rc, "xnb_snap_create: " + err);
+  }
+  *out = s;
+  return XNB_OK;
+}
+
+int xnb_snap_destroy(xnb_snap* s) {
+  if (!s) return XNB_OK;
+  cudaSetDevice(s->device);
+  for (void* q : s->allocs) cudaFree(q);
+  delete s;
+  return XNB_OK;
+}
+
+int xnb_snap_force(xnb_batch* b, int32_t s, const xnb_snap* snap, int32_t flags, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (!snap) return fail(XNB_ERR_ARG, "xnb_snap_force: no potential");
+  if (snap->device != b->device) return fail(XNB_ERR_ARG, "xnb_snap_force: potential built on another device");
+  if (flags & ~(XNB_FORCE_ENERGY | XNB_FORCE_ACCUMULATE)) return fail(XNB_ERR_ARG, "bad flags");
+  double rad_max = 0.0;
+  for (int k = 0; k < snap->t.ntypes; ++k) rad_max = std::max(rad_max, snap->t.radelem[k]);
+  const double cut_max = 2.0 * rad_max * snap->t.rcutfac;
+  for (size_t q = 0; q < b->sys.size(); ++q) {
+    const SysHost& h = b->sys[q];
+    if (!h.active || (s >= 0 && static_cast<int32_t>(q) != s)) continue;
+    if (cut_max > std::sqrt(h.d.nbh2) * (1.0 + 1e-15))
+      return fail(XNB_ERR_ARG, "SNAP cutoff above the neighbour distance of the lists");
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  XCK(cudaSetDevice(b->device));
+  XCK(cudaMemsetAsync(b->d_flag, 0, sizeof(unsigned int), st));
+  const Extent ex = b->extent();
+  b->launches += launch_snap(ex, b->d_sys, b->d_st, b->a, snap->t, s, (flags & XNB_FORCE_ENERGY) != 0,
+                             (flags & XNB_FORCE_ACCUMULATE) != 0, b->d_flag, st);
+  unsigned int flag = 0;
+  XCK(cudaMemcpyAsync(&flag, b->d_flag, sizeof(flag), cudaMemcpyDeviceToHost, st));
+  XCK(cudaStreamSynchronize(st));
+  if (flag & 1u) return fail(XNB_ERR_ARG, "a particle type has no SNAP coefficients");
+  if (flag & 2u) return fail(XNB_ERR_ARG, "a SNAP environment exceeds 128 neighbours");
+  return check_launch();
+}
 
 // chunk_neighbors for callers that cannot allocate device memory: only the
 // caller's buffers and the library's static scratch array are touched.

@@ -1,0 +1,643 @@
+// snap_force_generic (contribs/md/snap/include/md/snap/snap_force.h:134-372,
+// snap_force_op_coop.hxx:170-405): linear SNAP forces over the per-particle
+// neighbour lists, one CTA of kSnapWarps warps per atom.
+//
+// For atom i (type ti) the environment is the list entries at squared distance
+// in (1e-20, ((rad_ti + rad_tj) rcutfac)^2), in list order (snap_force_op_coop.hxx:
+// 215-226). Then, in FP64:
+//   U_tot = self term (1 on every diagonal) + sum_j wj sfac(r) U(r_ij), where U
+//     is built level by level with the recursion of the Wigner U-functions in
+//     the Cayley-Klein parameters of r_ij (snap_compute_ui.h:95-150). Only the
+//     unique half of each level is computed (rows 2mb < j and the first half
+//     of an even j's middle row); the rest follows from
+//     U[j-mb][j-ma] = (-1)^(ma+mb) conj(U[mb][ma]). Each warp sums its
+//     neighbours into its own partial, and the partials are added in warp order.
+//   Y (unique half) = sum over the Z elements of beta_j Z (snap_compute_yi.h:
+//     96-160), accumulated in shared memory; the per-atom energy
+//     E_i = beta_0 + sum_k beta_k (B_k - bzero_k), B from the same Z elements
+//     (snap_compute_bi.h:28-75).
+//   For each neighbour j, U and dU/dr_ij are rebuilt level by level and
+//     fij = 2 sum_unique w Re(conj(wj (dsfac U u + sfac dU)) Y) (w = 1/2 on an
+//     even j's centre, snap_compute_deidrj.h:28-75); f_i += fij, f_j -= fij
+//     (snap_force_op_coop.hxx:331-356), the reactions by FP64 atomics.
+// Forces are scaled by the energy unit, divided by the mass when the system's
+// force chain ends with divide_force_by_type_scalar. The order of the Y and
+// reaction additions varies from run to run, so results agree to rounding.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "../../include/xnb_gpu.h"
+#include "xnb_snap.cuh"
+
+namespace xnb {
+
+namespace {
+
+constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+
+__host__ __device__ inline int nunique(int j) { return (j & 1) ? ((j + 1) / 2) * (j + 1) : (j / 2) * (j + 1) + j / 2 + 1; }
+
+struct C2 {
+  double r, i;
+};
+__device__ __forceinline__ C2 cmulc(C2 a, C2 b) {  // conj(a) * b
+  return C2{fma(a.r, b.r, a.i * b.i), fma(a.r, b.i, -(a.i * b.r))};
+}
+__device__ __forceinline__ C2 cmul(C2 a, C2 b) { return C2{fma(a.r, b.r, -(a.i * b.i)), fma(a.r, b.i, a.i * b.r)}; }
+
+// element (r, c) of level L from its unique-half buffer (stride `st` doubles
+// per element, complex at offset `off`)
+__device__ __forceinline__ C2 level_get(const double* buf, int st, int off, int L, int r, int c) {
+  const int idx = r * (L + 1) + c;
+  if (idx < nunique(L)) return C2{buf[idx * st + off], buf[idx * st + off + 1]};
+  const int k = (L - r) * (L + 1) + (L - c);
+  const double s = ((r + c) & 1) ? -1.0 : 1.0;
+  return C2{s * buf[k * st + off], -s * buf[k * st + off + 1]};
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Cayley-Klein parameters of r_ij and their derivatives (snap_compute_duidrj.h:75-120).
+struct Geo {
+  C2 a, b, da[3], db[3];
+  double u[3], sfac, dsfac;
+};
+
+__device__ __forceinline__ Geo geometry(double x, double y, double z, double rcut, const SnapArgs& t, bool deriv) {
+  Geo g;
+  const double rsq = fma(x, x, fma(y, y, z * z));
+  const double r = sqrt(rsq);
+  const double rscale0 = t.rfac0 * M_PI / (rcut - t.rmin0);
+  const double theta0 = (r - t.rmin0) * rscale0;
+  double sn, cs;
+  sincos(theta0, &sn, &cs);
+  const double z0 = r * cs / sn;
+  const double r0inv = 1.0 / sqrt(fma(r, r, z0 * z0));
+  g.a = C2{r0inv * z0, -r0inv * z};
+  g.b = C2{r0inv * y, -r0inv * x};
+  g.sfac = 1.0;
+  g.dsfac = 0.0;
+  if (t.switchflag && r > t.rmin0) {
+    const double f = M_PI / (rcut - t.rmin0);
+    double ss, cc;
+    sincos((r - t.rmin0) * f, &ss, &cc);
+    g.sfac = 0.5 * (cc + 1.0);
+    g.dsfac = -0.5 * ss * f;
+  }
+  if (deriv) {
+    const double rinv = 1.0 / r;
+    g.u[0] = x * rinv;
+    g.u[1] = y * rinv;
+    g.u[2] = z * rinv;
+    const double dz0dr = z0 / r - (r * rscale0) * (rsq + z0 * z0) / rsq;
+    const double dr0invdr = -(r0inv * r0inv * r0inv) * (r + z0 * dz0dr);
+    for (int k = 0; k < 3; ++k) {
+      const double dr0 = dr0invdr * g.u[k];
+      g.da[k] = C2{dz0dr * g.u[k] * r0inv + z0 * dr0, -z * dr0};
+      g.db[k] = C2{y * dr0, -x * dr0};
+    }
+    g.da[2].i += -r0inv;
+    g.db[0].i += -r0inv;
+    g.db[1].r += r0inv;
+  }
+  return g;
+}
+
+__global__ void k_snap_zero(uint32_t n_part, const SysDesc* __restrict__ sys, const SysState* __restrict__ st,
+                            DevArrays a, int sys_only, bool zero_f, bool zero_pe) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_part) return;
+  const uint32_t c = a.pcell[i];
+  if (c == kInvalid) return;
+  const uint32_t s = a.cell_sys[c];
+  if (sys_only >= 0 && s != static_cast<uint32_t>(sys_only)) return;
+  if (st[s].error) return;
+  if (zero_f) {
+    a.fx[i] = 0.0;
+    a.fy[i] = 0.0;
+    a.fz[i] = 0.0;
+  }
+  if (zero_pe) a.pe[i] = 0.0;
+}
+
+__global__ void __launch_bounds__(kSnapWarps * 32)
+    k_snap(uint32_t n_part, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a,
+           SnapArgs t, int sys_only, bool with_pe, unsigned int* flags) {
+  extern __shared__ double sm[];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int J = t.twojmax;
+  const int lvl_max = nunique(J);
+  // shared layout (doubles)
+  double* nx = sm;
+  double* ny = nx + kSnapMaxNbr;
+  double* nz = ny + kSnapMaxNbr;
+  uint32_t* nj = reinterpret_cast<uint32_t*>(nz + kSnapMaxNbr);          // kSnapMaxNbr u32
+  uint8_t* nt = reinterpret_cast<uint8_t*>(nj + kSnapMaxNbr);            // kSnapMaxNbr u8
+  double* utot = nz + kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8;   // 2 * nu_full
+  double* yv = utot + 2 * t.nu_full;                                      // 2 * nu_unique
+  double* upart = yv + 2 * t.nu_unique;                                   // warps x 2 * nu_unique
+  double* lvl = upart + kSnapWarps * 2 * t.nu_unique;                     // warps x 2 x lvl_max x 8
+  double* red = lvl + kSnapWarps * 2 * lvl_max * 8;                      // 8 doubles
+  int* icnt = reinterpret_cast<int*>(red + 8);                            // 8 ints
+  double* my_up = upart + w * 2 * t.nu_unique;
+  double* my_lvl = lvl + w * 2 * lvl_max * 8;
+
+  for (uint32_t i = blockIdx.x; i < n_part; i += gridDim.x) {
+    const uint32_t c = a.pcell[i];
+    if (c == kInvalid) continue;
+    const uint32_t s = a.cell_sys[c];
+    if (sys_only >= 0 && s != static_cast<uint32_t>(sys_only)) continue;
+    if (st[s].error) continue;
+    const SysDesc& S = sys[s];
+    const uint32_t ti = a.ptype[i];
+    if (ti >= static_cast<uint32_t>(t.ntypes)) {
+      if (tid == 0) atomicOr(flags, 1u);
+      continue;
+    }
+    const double xa = a.rx[i], ya = a.ry[i], za = a.rz[i];
+    const uint32_t* __restrict__ L = a.nbr + S.list_base + a.nbr_start[i];
+    const uint32_t n = a.nbr_cnt[i];
+    const uint32_t pbase = S.part_base;
+    const double radi = t.radelem[ti];
+    const double fscale = S.divide_by_mass ? t.energy_unit / S.mass : t.energy_unit;
+
+    // ---- environment, in list order ----
+    if (tid == 0) icnt[4] = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < n; base += kSnapWarps * 32) {
+      const uint32_t k = base + tid;
+      bool keep = false;
+      double dx = 0, dy = 0, dz = 0;
+      uint32_t j = 0, tj = 0;
+      if (k < n) {
+        const uint32_t e = __ldg(L + k);
+        j = pbase + (e >> 5);
+        const uint32_t code = e & 31u;
+        double xb = __ldg(a.rx + j), yb = __ldg(a.ry + j), zb = __ldg(a.rz + j);
+        if (code != static_cast<uint32_t>(kImageCenter)) {
+          xb = image_coord(xb, S.period[0], static_cast<int>(code % 3u));
+          yb = image_coord(yb, S.period[1], static_cast<int>((code / 3u) % 3u));
+          zb = image_coord(zb, S.period[2], static_cast<int>(code / 9u));
+        }
+        dx = xb - xa;
+        dy = yb - ya;
+        dz = zb - za;
+        const double d2 = norm2_rn(dx, dy, dz);
+        tj = a.ptype[j];
+        if (tj >= static_cast<uint32_t>(t.ntypes)) {
+          atomicOr(flags, 1u);
+        } else {
+          const double cij = (radi + t.radelem[tj]) * t.rcutfac;
+          keep = d2 < cij * cij && d2 > 1e-20;
+        }
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, keep);
+      if (lane == 0) icnt[w] = __popc(bal);
+      __syncthreads();
+      int off = icnt[4];
+      for (int q = 0; q < w; ++q) off += icnt[q];
+      off += __popc(bal & ((1u << lane) - 1u));
+      if (keep && off < kSnapMaxNbr) {
+        nx[off] = dx;
+        ny[off] = dy;
+        nz[off] = dz;
+        nj[off] = j;
+        nt[off] = static_cast<uint8_t>(tj);
+      }
+      __syncthreads();
+      if (tid == 0) icnt[4] += icnt[0] + icnt[1] + icnt[2] + icnt[3];
+      __syncthreads();
+    }
+    const int nn = icnt[4];
+    if (nn > kSnapMaxNbr) {
+      if (tid == 0) atomicOr(flags, 2u);
+      __syncthreads();
+      continue;
+    }
+
+    // ---- U_tot: per-warp partial sums over the unique half ----
+    for (int e = lane; e < 2 * t.nu_unique; e += 32) my_up[e] = 0.0;
+    __syncwarp();
+    for (int q = w; q < nn; q += kSnapWarps) {
+      const double rcut = (radi + t.radelem[nt[q]]) * t.rcutfac;
+      const Geo g = geometry(nx[q], ny[q], nz[q], rcut, t, false);
+      const double sw = t.wj[nt[q]] * g.sfac;
+      double* prev = my_lvl;
+      double* cur = my_lvl + lvl_max * 8;
+      if (lane == 0) {
+        prev[0] = 1.0;
+        prev[1] = 0.0;
+        my_up[0] += sw;
+      }
+      __syncwarp();
+      for (int j = 1; j <= J; ++j) {
+        const int nuj = nunique(j);
+        for (int e = lane; e < nuj; e += 32) {
+          const int mb = e / (j + 1), ma = e % (j + 1);
+          C2 u{0.0, 0.0};
+          if (ma < j) {
+            const C2 up = level_get(prev, 8, 0, j - 1, mb, ma);
+            const double rp = t.rootpq[(j - ma) * (J + 1) + (j - mb)];
+            const C2 v = cmulc(g.a, up);
+            u.r += rp * v.r;
+            u.i += rp * v.i;
+          }
+          if (ma > 0) {
+            const C2 up = level_get(prev, 8, 0, j - 1, mb, ma - 1);
+            const double rp = t.rootpq[ma * (J + 1) + (j - mb)];
+            const C2 v = cmulc(g.b, up);
+            u.r -= rp * v.r;
+            u.i -= rp * v.i;
+          }
+          cur[e * 8] = u.r;
+          cur[e * 8 + 1] = u.i;
+          my_up[2 * (t.ublk[j] + e)] += sw * u.r;
+          my_up[2 * (t.ublk[j] + e) + 1] += sw * u.i;
+        }
+        __syncwarp();
+        double* tmp = prev;
+        prev = cur;
+        cur = tmp;
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    // ---- combine the partials, add the self term, expand to the full matrices ----
+    for (int e = tid; e < t.nu_unique; e += kSnapWarps * 32) {
+      int j = 0;
+      while (j < J && e >= t.ublk[j + 1]) ++j;
+      const int le = e - t.ublk[j];
+      const int mb = le / (j + 1), ma = le % (j + 1);
+      double re = (mb == ma) ? 1.0 : 0.0, im = 0.0;
+      for (int q = 0; q < kSnapWarps; ++q) {
+        re += upart[q * 2 * t.nu_unique + 2 * e];
+        im += upart[q * 2 * t.nu_unique + 2 * e + 1];
+      }
+      const int f = t.fblk[j] + mb * (j + 1) + ma;
+      utot[2 * f] = re;
+      utot[2 * f + 1] = im;
+      if (!(2 * mb == j && ma == mb)) {
+        const int g2 = t.fblk[j] + (j - mb) * (j + 1) + (j - ma);
+        const double sg = ((ma + mb) & 1) ? -1.0 : 1.0;
+        utot[2 * g2] = sg * re;
+        utot[2 * g2 + 1] = -sg * im;
+      }
+      yv[2 * e] = 0.0;
+      yv[2 * e + 1] = 0.0;
+    }
+    __syncthreads();
+    // ---- Y = sum beta_j Z, and the energy ----
+    double eloc = 0.0;
+    const double* zb = t.zbeta + static_cast<size_t>(ti) * t.nz;
+    const double* ze = t.zener + static_cast<size_t>(ti) * t.nz;
+    for (int e = tid; e < t.nz; e += kSnapWarps * 32) {
+      const SnapZ z = t.z[e];
+      const double* cgb = t.cg + z.cg;
+      const int j1 = z.j1, j2 = z.j2;
+      int jju1 = t.fblk[j1] + (j1 + 1) * z.mb1min;
+      int jju2 = t.fblk[j2] + (j2 + 1) * z.mb2max;
+      int icgb = z.mb1min * (j2 + 1) + z.mb2max;
+      C2 zt{0.0, 0.0};
+      for (int ib = 0; ib < z.nb; ++ib) {
+        C2 sa{0.0, 0.0};
+        int ma1 = z.ma1min, ma2 = z.ma2max;
+        int icga = z.ma1min * (j2 + 1) + z.ma2max;
+        for (int ia = 0; ia < z.na; ++ia) {
+          const C2 p = cmul(C2{utot[2 * (jju1 + ma1)], utot[2 * (jju1 + ma1) + 1]},
+                            C2{utot[2 * (jju2 + ma2)], utot[2 * (jju2 + ma2) + 1]});
+          sa.r = fma(cgb[icga], p.r, sa.r);
+          sa.i = fma(cgb[icga], p.i, sa.i);
+          ++ma1;
+          --ma2;
+          icga += j2;
+        }
+        zt.r = fma(cgb[icgb], sa.r, zt.r);
+        zt.i = fma(cgb[icgb], sa.i, zt.i);
+        jju1 += j1 + 1;
+        jju2 -= j2 + 1;
+        icgb += j2;
+      }
+      atomicAdd(&yv[2 * z.y], zb[e] * zt.r);
+      atomicAdd(&yv[2 * z.y + 1], zb[e] * zt.i);
+      if (with_pe && ze[e] != 0.0) {
+        const C2 u{utot[2 * z.uf], utot[2 * z.uf + 1]};
+        eloc += ze[e] * cmulc(u, zt).r;
+      }
+    }
+    if (with_pe) {
+      eloc = warp_sum(eloc);
+      if (lane == 0) red[w] = eloc;
+    }
+    __syncthreads();
+    if (with_pe && tid == 0) {
+      double es = t.e0[ti];
+      for (int q = 0; q < kSnapWarps; ++q) es += red[q];
+      a.pe[i] = es * t.energy_unit;
+    }
+    // ---- forces: U and dU per neighbour, contracted with Y ----
+    double fi0 = 0.0, fi1 = 0.0, fi2 = 0.0;
+    for (int q = w; q < nn; q += kSnapWarps) {
+      const double rcut = (radi + t.radelem[nt[q]]) * t.rcutfac;
+      const Geo g = geometry(nx[q], ny[q], nz[q], rcut, t, true);
+      const double wjq = t.wj[nt[q]];
+      const double sw = wjq * g.sfac, dsw = wjq * g.dsfac;
+      double* prev = my_lvl;
+      double* cur = my_lvl + lvl_max * 8;
+      double f0 = 0.0, f1 = 0.0, f2 = 0.0;
+      if (lane == 0) {
+        prev[0] = 1.0;
+        prev[1] = 0.0;
+        for (int k = 2; k < 8; ++k) prev[k] = 0.0;
+        // level 0 (centre, weight 1/2): dU_tot = dsfac * 1 * u
+        f0 += 0.5 * dsw * g.u[0] * yv[0];
+        f1 += 0.5 * dsw * g.u[1] * yv[0];
+        f2 += 0.5 * dsw * g.u[2] * yv[0];
+      }
+      __syncwarp();
+      for (int j = 1; j <= J; ++j) {
+        const int nuj = nunique(j);
+        const bool even = (j & 1) == 0;
+        for (int e = lane; e < nuj; e += 32) {
+          const int mb = e / (j + 1), ma = e % (j + 1);
+          C2 u{0.0, 0.0}, du[3] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+          if (ma < j) {
+            const double rp = t.rootpq[(j - ma) * (J + 1) + (j - mb)];
+            const C2 up = level_get(prev, 8, 0, j - 1, mb, ma);
+            C2 v = cmulc(g.a, up);
+            u.r += rp * v.r;
+            u.i += rp * v.i;
+            for (int k = 0; k < 3; ++k) {
+              const C2 dup = level_get(prev, 8, 2 + 2 * k, j - 1, mb, ma);
+              const C2 v1 = cmulc(g.da[k], up), v2 = cmulc(g.a, dup);
+              du[k].r += rp * (v1.r + v2.r);
+              du[k].i += rp * (v1.i + v2.i);
+            }
+          }
+          if (ma > 0) {
+            const double rp = t.rootpq[ma * (J + 1) + (j - mb)];
+            const C2 up = level_get(prev, 8, 0, j - 1, mb, ma - 1);
+            C2 v = cmulc(g.b, up);
+            u.r -= rp * v.r;
+            u.i -= rp * v.i;
+            for (int k = 0; k < 3; ++k) {
+              const C2 dup = level_get(prev, 8, 2 + 2 * k, j - 1, mb, ma - 1);
+              const C2 v1 = cmulc(g.db[k], up), v2 = cmulc(g.b, dup);
+              du[k].r -= rp * (v1.r + v2.r);
+              du[k].i -= rp * (v1.i + v2.i);
+            }
+          }
+          double* o = cur + e * 8;
+          o[0] = u.r;
+          o[1] = u.i;
+          for (int k = 0; k < 3; ++k) {
+            o[2 + 2 * k] = du[k].r;
+            o[3 + 2 * k] = du[k].i;
+          }
+          const double wgt = (even && e == nuj - 1) ? 0.5 : 1.0;
+          const double yr = yv[2 * (t.ublk[j] + e)], yi = yv[2 * (t.ublk[j] + e) + 1];
+          const double dtr0 = dsw * u.r * g.u[0] + sw * du[0].r, dti0 = dsw * u.i * g.u[0] + sw * du[0].i;
+          const double dtr1 = dsw * u.r * g.u[1] + sw * du[1].r, dti1 = dsw * u.i * g.u[1] + sw * du[1].i;
+          const double dtr2 = dsw * u.r * g.u[2] + sw * du[2].r, dti2 = dsw * u.i * g.u[2] + sw * du[2].i;
+          f0 += wgt * fma(dtr0, yr, dti0 * yi);
+          f1 += wgt * fma(dtr1, yr, dti1 * yi);
+          f2 += wgt * fma(dtr2, yr, dti2 * yi);
+        }
+        __syncwarp();
+        double* tmp = prev;
+        prev = cur;
+        cur = tmp;
+      }
+      f0 = warp_sum(f0) * 2.0 * fscale;
+      f1 = warp_sum(f1) * 2.0 * fscale;
+      f2 = warp_sum(f2) * 2.0 * fscale;
+      if (lane == 0) {
+        const uint32_t j = nj[q];
+        atomicAdd(a.fx + j, -f0);
+        atomicAdd(a.fy + j, -f1);
+        atomicAdd(a.fz + j, -f2);
+        fi0 += f0;
+        fi1 += f1;
+        fi2 += f2;
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      atomicAdd(a.fx + i, fi0);
+      atomicAdd(a.fy + i, fi1);
+      atomicAdd(a.fz + i, fi2);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host tables. Clebsch-Gordan coefficients by Racah's closed formula with
+// exact integer factorials in long double.
+long double lfact(int n) {
+  long double r = 1.0L;
+  for (int k = 2; k <= n; ++k) r *= k;
+  return r;
+}
+
+double clebsch(int j1, int j2, int j, int m1, int m2) {
+  const int a2 = 2 * m1 - j1, b2 = 2 * m2 - j2, c2 = a2 + b2;
+  if (c2 < -j || c2 > j) return 0.0;
+  const long double tri =
+      lfact((j1 + j2 - j) / 2) * lfact((j1 - j2 + j) / 2) * lfact((-j1 + j2 + j) / 2) / lfact((j1 + j2 + j) / 2 + 1);
+  const long double pre = sqrtl((j + 1) * tri * lfact((j1 + a2) / 2) * lfact((j1 - a2) / 2) * lfact((j2 + b2) / 2) *
+                                lfact((j2 - b2) / 2) * lfact((j + c2) / 2) * lfact((j - c2) / 2));
+  long double sum = 0.0L;
+  const int kmin = std::max(0, std::max(-(j - j2 + a2) / 2, -(j - j1 - b2) / 2));
+  const int kmax = std::min((j1 + j2 - j) / 2, std::min((j1 - a2) / 2, (j2 + b2) / 2));
+  for (int k = kmin; k <= kmax; ++k) {
+    const long double den = lfact(k) * lfact((j1 + j2 - j) / 2 - k) * lfact((j1 - a2) / 2 - k) *
+                            lfact((j2 + b2) / 2 - k) * lfact((j - j2 + a2) / 2 + k) * lfact((j - j1 - b2) / 2 + k);
+    sum += ((k & 1) ? -1.0L : 1.0L) / den;
+  }
+  return static_cast<double>(pre * sum);
+}
+
+}  // namespace
+
+int snap_build(const xnb_snap_params& p, int device, SnapArgs& t, std::vector<void*>& allocs, std::string& err) {
+  const int J = p.twojmax;
+  if (J < 0 || J > kSnapMaxTwoJ) {
+    err = "twojmax must be in [0, 10]";
+    return XNB_ERR_ARG;
+  }
+  if (p.chemflag || p.bnormflag || p.quadraticflag || p.switchinnerflag) {
+    err = "only linear SNAP with chemflag, bnormflag, quadraticflag and switchinnerflag off is supported";
+    return XNB_ERR_ARG;
+  }
+  if (p.ntypes < 1 || p.ntypes > kSnapMaxTypes || !p.coeff) {
+    err = "1 to 16 particle types with coefficients";
+    return XNB_ERR_ARG;
+  }
+  std::memset(&t, 0, sizeof(t));
+  t.twojmax = J;
+  t.ntypes = p.ntypes;
+  t.switchflag = p.switchflag != 0;
+  t.rcutfac = p.rcutfac;
+  t.rfac0 = p.rfac0;
+  t.rmin0 = p.rmin0;
+  t.energy_unit = p.energy_unit;
+  for (int k = 0; k < p.ntypes; ++k) {
+    t.radelem[k] = p.radelem[k];
+    t.wj[k] = p.wj[k];
+  }
+  int nu = 0, nf = 0;
+  for (int j = 0; j <= J; ++j) {
+    t.ublk[j] = nu;
+    t.fblk[j] = nf;
+    nu += nunique(j);
+    nf += (j + 1) * (j + 1);
+  }
+  t.ublk[J + 1] = nu;
+  t.fblk[J + 1] = nf;
+  t.nu_unique = nu;
+  t.nu_full = nf;
+  // coefficient order (sna.cpp:236-259) and Clebsch-Gordan blocks (sna.cpp:194-205)
+  struct Tri {
+    int j1, j2, j;
+  };
+  std::vector<Tri> bl;
+  std::vector<double> cg;
+  std::vector<int> cgoff;  // by (j1, j2, j)
+  cgoff.assign((J + 1) * (J + 1) * (J + 1), -1);
+  for (int j1 = 0; j1 <= J; ++j1)
+    for (int j2 = 0; j2 <= j1; ++j2)
+      for (int j = j1 - j2; j <= std::min(J, j1 + j2); j += 2) {
+        if (j >= j1) bl.push_back({j1, j2, j});
+        cgoff[(j1 * (J + 1) + j2) * (J + 1) + j] = static_cast<int>(cg.size());
+        for (int m1 = 0; m1 <= j1; ++m1)
+          for (int m2 = 0; m2 <= j2; ++m2) cg.push_back(clebsch(j1, j2, j, m1, m2));
+      }
+  const int ncoeff = static_cast<int>(bl.size());
+  if (p.ncoeffall != ncoeff + 1) {
+    err = "coefficient count " + std::to_string(p.ncoeffall) + " does not match twojmax (expected " +
+          std::to_string(ncoeff + 1) + ")";
+    return XNB_ERR_ARG;
+  }
+  auto bindex = [&](int a, int b, int c) {
+    for (int k = 0; k < ncoeff; ++k)
+      if (bl[k].j1 == a && bl[k].j2 == b && bl[k].j == c) return k;
+    return -1;
+  };
+  // Z elements of the unique half, with the beta multipliers (snap_compute_yi.h:133-158)
+  std::vector<SnapZ> zs;
+  std::vector<double> mult;  // multiplicity * (j1+1)/(j+1)
+  std::vector<int> kb;       // coefficient of the multiplier
+  std::vector<int> ecoef;    // coefficient for the energy (canonical entries) or -1
+  std::vector<double> ew;    // 2 w of the energy sum
+  for (int j1 = 0; j1 <= J; ++j1)
+    for (int j2 = 0; j2 <= j1; ++j2)
+      for (int j = j1 - j2; j <= std::min(J, j1 + j2); j += 2)
+        for (int mb = 0; 2 * mb <= j; ++mb)
+          for (int ma = 0; ma <= j; ++ma) {
+            if (2 * mb == j && ma > mb) continue;
+            SnapZ z{};
+            z.j1 = static_cast<uint8_t>(j1);
+            z.j2 = static_cast<uint8_t>(j2);
+            z.j = static_cast<uint8_t>(j);
+            const int ma1min = std::max(0, (2 * ma - j - j2 + j1) / 2);
+            const int ma2max = (2 * ma - j - (2 * ma1min - j1) + j2) / 2;
+            const int na = std::min(j1, (2 * ma - j + j2 + j1) / 2) - ma1min + 1;
+            const int mb1min = std::max(0, (2 * mb - j - j2 + j1) / 2);
+            const int mb2max = (2 * mb - j - (2 * mb1min - j1) + j2) / 2;
+            const int nb = std::min(j1, (2 * mb - j + j2 + j1) / 2) - mb1min + 1;
+            z.ma1min = static_cast<uint8_t>(ma1min);
+            z.ma2max = static_cast<uint8_t>(ma2max);
+            z.na = static_cast<uint8_t>(std::max(0, na));
+            z.mb1min = static_cast<uint8_t>(mb1min);
+            z.mb2max = static_cast<uint8_t>(mb2max);
+            z.nb = static_cast<uint8_t>(std::max(0, nb));
+            z.y = static_cast<uint16_t>(t.ublk[j] + mb * (j + 1) + ma);
+            z.uf = static_cast<uint16_t>(t.fblk[j] + mb * (j + 1) + ma);
+            z.cg = static_cast<uint32_t>(cgoff[(j1 * (J + 1) + j2) * (J + 1) + j]);
+            double m;
+            int k;
+            if (j >= j1) {
+              k = bindex(j1, j2, j);
+              m = (j1 == j) ? ((j2 == j) ? 3.0 : 2.0) : 1.0;
+            } else if (j >= j2) {
+              k = bindex(j, j2, j1);
+              m = (j2 == j) ? 2.0 : 1.0;
+            } else {
+              k = bindex(j2, j, j1);
+              m = 1.0;
+            }
+            if (j1 > j) m *= (j1 + 1) / (j + 1.0);
+            zs.push_back(z);
+            mult.push_back(m);
+            kb.push_back(k);
+            ecoef.push_back(j >= j1 ? bindex(j1, j2, j) : -1);
+            ew.push_back((2 * mb == j && ma == mb) ? 1.0 : 2.0);
+          }
+  t.nz = static_cast<int>(zs.size());
+  std::vector<double> zbeta(static_cast<size_t>(p.ntypes) * t.nz), zener(zbeta.size());
+  for (int ty = 0; ty < p.ntypes; ++ty) {
+    const double* c = p.coeff + static_cast<size_t>(ty) * p.ncoeffall;
+    double e0 = c[0];
+    if (p.bzeroflag)
+      for (int k = 0; k < ncoeff; ++k) e0 -= c[1 + k] * (bl[k].j + 1);  // bzero_j = wself^3 (j+1)
+    t.e0[ty] = e0;
+    for (int e = 0; e < t.nz; ++e) {
+      zbeta[static_cast<size_t>(ty) * t.nz + e] = mult[e] * c[1 + kb[e]];
+      zener[static_cast<size_t>(ty) * t.nz + e] = ecoef[e] >= 0 ? ew[e] * c[1 + ecoef[e]] : 0.0;
+    }
+  }
+  std::vector<double> rootpq((J + 1) * (J + 1), 0.0);
+  for (int a = 1; a <= J; ++a)
+    for (int b = 1; b <= J; ++b) rootpq[a * (J + 1) + b] = std::sqrt(static_cast<double>(a) / b);
+  // upload
+  if (cudaSetDevice(device) != cudaSuccess) {
+    err = "cudaSetDevice failed";
+    return XNB_ERR_CUDA;
+  }
+  auto up = [&](const void* src, size_t bytes, const void** dst) -> bool {
+    void* d = nullptr;
+    if (cudaMalloc(&d, std::max<size_t>(bytes, 16)) != cudaSuccess) return false;
+    allocs.push_back(d);
+    if (bytes && cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return false;
+    *dst = d;
+    return true;
+  };
+  if (!up(rootpq.data(), rootpq.size() * 8, reinterpret_cast<const void**>(&t.rootpq)) ||
+      !up(cg.data(), cg.size() * 8, reinterpret_cast<const void**>(&t.cg)) ||
+      !up(zs.data(), zs.size() * sizeof(SnapZ), reinterpret_cast<const void**>(&t.z)) ||
+      !up(zbeta.data(), zbeta.size() * 8, reinterpret_cast<const void**>(&t.zbeta)) ||
+      !up(zener.data(), zener.size() * 8, reinterpret_cast<const void**>(&t.zener))) {
+    err = "device memory for the SNAP tables";
+    return XNB_ERR_NOMEM;
+  }
+  const int lvl_max = nunique(J);
+  const size_t doubles = 3 * kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8 + 2 * t.nu_full + 2 * t.nu_unique +
+                         kSnapWarps * 2 * t.nu_unique + kSnapWarps * 2 * lvl_max * 8 + 8 + 4;
+  t.smem_bytes = doubles * sizeof(double);
+  return XNB_OK;
+}
+
+int launch_snap(const Extent& ex, const SysDesc* sys, const SysState* st, const DevArrays& a, const SnapArgs& t,
+                int sys_only, bool with_pe, bool accumulate, unsigned int* flags, cudaStream_t stream) {
+  if (ex.n_part == 0) return 0;
+  int launches = 0;
+  if (!accumulate || with_pe) {
+    const int g = static_cast<int>((static_cast<long long>(ex.n_part) + 255) / 256);
+    k_snap_zero<<<g, 256, 0, stream>>>(ex.n_part, sys, st, a, sys_only, !accumulate, with_pe);
+    ++launches;
+  }
+  cudaFuncSetAttribute(k_snap, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(t.smem_bytes));
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_snap, kSnapWarps * 32, t.smem_bytes);
+  long long g = static_cast<long long>(ex.sm_count) * std::max(1, per_sm) * 4;
+  if (g > static_cast<long long>(ex.n_part)) g = ex.n_part;
+  k_snap<<<static_cast<int>(std::max(1LL, g)), kSnapWarps * 32, t.smem_bytes, stream>>>(ex.n_part, sys, st, a, t,
+                                                                                      sys_only, with_pe, flags);
+  return launches + 1;
+}
+
+}  // namespace xnb

@@ -4,13 +4,17 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <fstream>
+#include <map>
 #include <random>
+#include <sstream>
 
 #include "xnb_host.hpp"
 
 namespace xnbhost {
 
 Context::~Context() {
+  if (snap) xnb_snap_destroy(snap);
   if (batch) xnb_batch_destroy(batch);
 }
 
@@ -124,11 +128,17 @@ struct LatticeOp : OperatorNode {
   void execute(Context& ctx) override {
     if (!ctx.domain_set) throw Error("lattice: domain must come first");
     const Node* st = local("structure");
-    if (!st || st->scalar != "FCC") throw Error("lattice: only structure FCC is supported");
+    // unit-cell bases of lattice_generator.h:140-170
+    static const double sc[1][3] = {{.5, .5, .5}};
+    static const double bcc[2][3] = {{.0, .0, .0}, {.5, .5, .5}};
+    static const double fcc[4][3] = {{.0, .0, .0}, {.0, .5, .5}, {.5, .0, .5}, {.5, .5, .0}};
+    if (!st || (st->scalar != "FCC" && st->scalar != "BCC" && st->scalar != "SC"))
+      throw Error("lattice: structure SC, BCC or FCC");
+    const double(*basis)[3] = st->scalar == "SC" ? sc : st->scalar == "BCC" ? bcc : fcc;
+    const int nbasis = st->scalar == "SC" ? 1 : st->scalar == "BCC" ? 2 : 4;
     const Node* sz = local("size");
     if (!sz || !sz->is_seq()) throw Error("lattice: size [a, a, a] required");
     const double a[3] = {quantity(sz->seq.at(0)), quantity(sz->seq.at(1)), quantity(sz->seq.at(2))};
-    const double basis[4][3] = {{.0, .0, .0}, {.0, .5, .5}, {.5, .0, .5}, {.5, .5, .0}};
     const auto& p = ctx.params;
     const long D[3] = {p.dims[0], p.dims[1], p.dims[2]};
     const long ncell = D[0] * D[1] * D[2];
@@ -141,7 +151,7 @@ struct LatticeOp : OperatorNode {
     for (long k = lo[2]; k <= hi[2]; ++k)
       for (long j = lo[1]; j <= hi[1]; ++j)
         for (long i = lo[0]; i <= hi[0]; ++i)
-          for (int l = 0; l < 4; ++l) {
+          for (int l = 0; l < nbasis; ++l) {
             const double x = (static_cast<double>(i) + basis[l][0]) * a[0];
             const double y = (static_cast<double>(j) + basis[l][1]) * a[1];
             const double z = (static_cast<double>(k) + basis[l][2]) * a[2];
@@ -352,6 +362,103 @@ struct GravityOp : OperatorNode {
 };
 
 // next_time_step: the time step counter and the physical time advance by one step
+// snap_force_generic (contribs/md/snap/include/md/snap/snap_force.h:52-372):
+// slot parameters { param, coef, nt } naming LAMMPS files (read as
+// lib/snap_read_lammps.cpp:30-132 does: `key value` lines over the SnapConfig
+// defaults, then `n_materials coefs_per_material`, per material `name radelem
+// weight` and one coefficient per line), conv_coef_units (false: coefficients
+// stay in eV and forces are converted). Relative file names are taken from the
+// deck's directory. Adds onto the forces written earlier in the force block.
+struct SnapOp : OperatorNode {
+  static std::string resolve(Context& ctx, const std::string& f) {
+    return (!f.empty() && f[0] != '/') ? ctx.slots["deck_dir"].scalar + "/" + f : f;
+  }
+  static void read(const std::string& param, const std::string& coef, xnb_snap_params& p,
+                   std::vector<double>& coeffs) {
+    std::map<std::string, double> v = {{"rfac0", 0.99363}, {"rmin0", 0.0},      {"rcutfac", 0.0},
+                                       {"twojmax", 6.0},    {"nelements", 1.0},  {"bzeroflag", 1.0},
+                                       {"switchflag", 1.0}, {"chemflag", 0.0},   {"bnormflag", 0.0},
+                                       {"wselfallflag", 0.0}, {"switchinnerflag", 0.0}, {"quadraticflag", 0.0}};
+    std::ifstream in(param);
+    if (!in.good()) throw Error("snap_force_generic: can't open file '" + param + "'");
+    std::string line;
+    while (std::getline(in, line)) {
+      if (line.empty() || line[0] == '#') continue;
+      std::istringstream ls(line);
+      std::string key;
+      double value = 0.0;
+      if (ls >> key >> value && v.count(key)) v[key] = value;
+    }
+    std::ifstream cf(coef);
+    if (!cf.good()) throw Error("snap_force_generic: cannot read file '" + coef + "'");
+    int skipped = 0;
+    std::getline(cf, line);
+    while (cf.good() && (line.empty() || line[0] == '#') && skipped < 100) {
+      std::getline(cf, line);
+      ++skipped;
+    }
+    size_t nmat = 0, ncoef = 0;
+    std::istringstream(line) >> nmat >> ncoef;
+    if (nmat == 0 || nmat > 16 || ncoef == 0) throw Error("snap_force_generic: bad coefficient file '" + coef + "'");
+    p = xnb_snap_params{};
+    p.twojmax = static_cast<int32_t>(v["twojmax"]);
+    p.rcutfac = v["rcutfac"];
+    p.rfac0 = v["rfac0"];
+    p.rmin0 = v["rmin0"];
+    p.switchflag = static_cast<int32_t>(v["switchflag"]);
+    p.bzeroflag = static_cast<int32_t>(v["bzeroflag"]);
+    p.chemflag = static_cast<int32_t>(v["chemflag"]);
+    p.bnormflag = static_cast<int32_t>(v["bnormflag"]);
+    p.quadraticflag = static_cast<int32_t>(v["quadraticflag"]);
+    p.switchinnerflag = static_cast<int32_t>(v["switchinnerflag"]);
+    p.ntypes = static_cast<int32_t>(nmat);
+    p.ncoeffall = static_cast<int32_t>(ncoef);
+    coeffs.clear();
+    for (size_t m = 0; m < nmat; ++m) {
+      std::getline(cf, line);
+      std::string name;
+      double rad = 0.0, w = 1.0;
+      std::istringstream(line) >> name >> rad >> w;
+      p.radelem[m] = rad;
+      p.wj[m] = w;
+      for (size_t k = 0; k < ncoef; ++k) {
+        std::getline(cf, line);
+        double c = 0.0;
+        std::istringstream(line) >> c;
+        coeffs.push_back(c);
+      }
+    }
+    if (!cf) throw Error("snap_force_generic: coefficient file '" + coef + "' is short");
+  }
+  void execute(Context& ctx) override {
+    const Node* prm = local("parameters");
+    const Node* pf = prm ? prm->find("param") : nullptr;
+    const Node* cf = prm ? prm->find("coef") : nullptr;
+    if (!pf || !cf) throw Error("snap_force_generic: parameters { param, coef } required");
+    const bool conv = local("conv_coef_units") && to_bool(*local("conv_coef_units"));
+    if (!ctx.snap) {
+      xnb_snap_params p{};
+      std::vector<double> coeffs;
+      read(resolve(ctx, pf->scalar), resolve(ctx, cf->scalar), p, coeffs);
+      if (conv) {
+        for (double& c : coeffs) c *= quantity("1 eV");
+        p.energy_unit = 1.0;
+      } else {
+        p.energy_unit = quantity("1 eV");
+      }
+      p.coeff = coeffs.data();
+      if (ctx.dry_run) return;
+      if (xnb_snap_create(&p, 0, &ctx.snap) != XNB_OK)
+        throw Error(std::string("snap_force_generic: ") + xnb_last_error_string());
+    }
+    if (ctx.dry_run || !gpu_ready(ctx)) return;
+    ck(xnb_snap_force(ctx.batch, ctx.sys, ctx.snap, XNB_FORCE_ENERGY | (ctx.forces_written ? XNB_FORCE_ACCUMULATE : 0),
+                      nullptr),
+       "snap_force_generic");
+    ctx.forces_written = true;
+  }
+};
+
 struct NextTimeStepOp : OperatorNode {
   void execute(Context& ctx) override {
     ++ctx.timestep;
@@ -563,6 +670,7 @@ void register_hot_path_operators() {
   reg<LennardJonesOp>("lennard_jones_force");
   reg<GravityOp>("gravitational_force");
   reg<ZeroForceOp>("zero_particle_force");
+  reg<SnapOp>("snap_force_generic");
   // folded into move_particles / lennard_jones_force on the GPU, or single-rank no-ops
   for (const char* n : {"migrate_cell_particles", "rebuild_amr", "ghost_comm_scheme", "ghost_update_all",
                         "ghost_update_r", "amr_grid_pairs", "resize_particle_locks",

@@ -70,6 +70,7 @@ struct Context {
   int32_t sys = -1;
   int32_t precision = XNB_PREC_FP64_EXACT;
   bool forces_written = false;  // a force operator of the current force block has written forces
+  xnb_snap* snap = nullptr;     // snap_force_generic's potential, built at its first call
   long timestep = 0;
   double physical_time = 0.0;
   bool verbose = false;

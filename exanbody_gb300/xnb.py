@@ -33,7 +33,8 @@ EXPORTED = [
     "xnb_ghost_update_r", "xnb_step", "xnb_step_graph_create", "xnb_graph_launch", "xnb_graph_destroy",
     "xnb_check_errors", "xnb_stats_kernel_launches", "xnb_chunk_neighbors_noalloc", "xnb_chunk_neighbors_stream",
     "xnb_verify_chunk_neighbors", "xnb_simulation_stats", "xnb_sample_particles", "xnb_system_set_types",
-    "xnb_gravitational_force", "xnb_batch_set_tuning", "xnb_autotune",
+    "xnb_gravitational_force", "xnb_batch_set_tuning", "xnb_autotune", "xnb_snap_create", "xnb_snap_destroy",
+    "xnb_snap_force",
 ]
 
 FORCE_ENERGY = 1
@@ -108,6 +109,14 @@ class SystemInfo(C.Structure):
     ]
 
 
+class SnapParams(C.Structure):
+    _fields_ = [("twojmax", C.c_int32), ("rcutfac", C.c_double), ("rfac0", C.c_double), ("rmin0", C.c_double),
+                ("switchflag", C.c_int32), ("bzeroflag", C.c_int32), ("chemflag", C.c_int32),
+                ("bnormflag", C.c_int32), ("quadraticflag", C.c_int32), ("switchinnerflag", C.c_int32),
+                ("ntypes", C.c_int32), ("radelem", C.c_double * 16), ("wj", C.c_double * 16),
+                ("ncoeffall", C.c_int32), ("coeff", C.POINTER(C.c_double)), ("energy_unit", C.c_double)]
+
+
 class XnbError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("xnb error %d: %s" % (code, msg))
@@ -171,6 +180,9 @@ def load(build_if_missing=True):
     lib.xnb_gravitational_force.argtypes = [vp, i32, d, P(d), i32, d, i32, i32, vp]
     lib.xnb_batch_set_tuning.argtypes = [vp, i32, i32]
     lib.xnb_autotune.argtypes = [vp, i32, i32, vp, P(Tuning)]
+    lib.xnb_snap_create.argtypes = [P(SnapParams), i32, P(vp)]
+    lib.xnb_snap_destroy.argtypes = [vp]
+    lib.xnb_snap_force.argtypes = [vp, i32, vp, i32, vp]
     _LIB = lib
     return lib
 

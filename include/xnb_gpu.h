@@ -303,6 +303,48 @@ int xnb_chunk_neighbors_noalloc(const xnb_lj_params* p, int64_t n, const double*
                                 uint32_t* nbr, int64_t nbr_capacity, uint32_t* nbr_start, uint32_t* nbr_count,
                                 int64_t* total_out, void* stream);
 
+/* ---- SNAP (snap_force_generic, contribs/md/snap/include/md/snap/snap_force.h:
+ *      134-372) ---- */
+/* A linear SNAP potential as the reference reads it from LAMMPS files
+ * (lib/snap_read_lammps.cpp:30-132): rcutfac, rfac0, rmin0, twojmax (<= 10),
+ * switchflag, bzeroflag; per particle type radelem, the weight wj and
+ * ncoeffall coefficients (constant term first, bispectrum order of
+ * sna.cpp:236-259). chemflag, bnormflag, quadraticflag, switchinnerflag must be
+ * 0 and wselfallflag is irrelevant for one element set. Forces and energies are
+ * multiplied by energy_unit (1 eV in the system's units when the coefficients
+ * are in eV, as the reference does without conv_coef_units). */
+typedef struct xnb_snap_params {
+  int32_t twojmax;
+  double rcutfac;
+  double rfac0;
+  double rmin0;
+  int32_t switchflag;
+  int32_t bzeroflag;
+  int32_t chemflag;
+  int32_t bnormflag;
+  int32_t quadraticflag;
+  int32_t switchinnerflag;
+  int32_t ntypes; /* <= 16 */
+  double radelem[16];
+  double wj[16];
+  int32_t ncoeffall;
+  const double* coeff; /* ntypes x ncoeffall */
+  double energy_unit;
+} xnb_snap_params;
+typedef struct xnb_snap xnb_snap;
+/* Builds the potential's tables (Clebsch-Gordan blocks, index lists, the
+ * coefficient multipliers of the adjoint) on `device`. */
+int xnb_snap_create(const xnb_snap_params* p, int32_t device, xnb_snap** out);
+int xnb_snap_destroy(xnb_snap* s);
+/* zero_particle_force + snap_force_generic + update_force_from_ghost (+ the
+ * division by mass of systems whose force chain ends with it) over the current
+ * lists, FP64. The SNAP cutoff (rad_a + rad_b) rcutfac must not exceed the
+ * lists' rcut + rcut_inc. flags: XNB_FORCE_ENERGY writes the per-particle SNAP
+ * energy to pe; XNB_FORCE_ACCUMULATE adds onto the current forces. An
+ * environment of more than 128 neighbours or a particle type without
+ * coefficients returns XNB_ERR_ARG. Synchronises `stream`. */
+int xnb_snap_force(xnb_batch* b, int32_t sys, const xnb_snap* snap, int32_t flags, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,7 +27,8 @@ def build(verbose=False):
     for name, flags in jobs:
         dst = os.path.join(OUT, name)
         if os.path.exists(dst) and os.path.getmtime(dst) >= max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "xnb_oracle.h"))
+            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "xnb_oracle.h")),
+            os.path.getmtime(os.path.join(HERE, "xnb_snap_oracle.h"))
         ):
             continue
         cmd = ["g++", "-std=c++17", "-shared", "-fPIC", *flags, src, "-o", dst + ".tmp"]

@@ -45,6 +45,8 @@ def _lib(kind="parity"):
     lib.xo_load_flat.argtypes = [C.c_void_p, i64] + [P(d)] * 6 + [P(u64)]
     lib.xo_load_cells.argtypes = [C.c_void_p, P(i64)] + [P(d)] * 6 + [P(u64)]
     lib.xo_load_lattice_noise_fcc.argtypes = [C.c_void_p, d, d]
+    lib.xo_load_lattice_noise.argtypes = [C.c_void_p, i32, d, d]
+    lib.xo_set_snap.argtypes = [C.c_void_p, i32, d, d, d, i32, i32, i32, P(d), P(d), i32, P(d), d, i32]
     lib.xo_init.argtypes = [C.c_void_p]
     lib.xo_step.argtypes = [C.c_void_p]
     for f in ("xo_num_particles", "xo_rebuild_count", "xo_num_cells", "xo_pair_count", "xo_displ_over_count"):
@@ -108,6 +110,24 @@ class OracleSystem:
 
     def load_lattice_noise_fcc(self, a, sigma):
         assert self.lib.xo_load_lattice_noise_fcc(self.h, a, sigma) == 0
+
+    def load_lattice_noise(self, structure, a, sigma):
+        """structure: "SC", "BCC" or "FCC" (the reference's lattice generator basis)."""
+        code = {"SC": 0, "BCC": 1, "FCC": 2}[structure]
+        assert self.lib.xo_load_lattice_noise(self.h, code, a, sigma) == 0
+
+    def set_snap(self, cfg, energy_unit, with_energy=False):
+        """Force chain = snap_force_generic with a read_lammps() configuration."""
+        els = cfg["elements"]
+        rad = np.ascontiguousarray([e["radelem"] for e in els], np.float64)
+        wj = np.ascontiguousarray([e["weight"] for e in els], np.float64)
+        coeff = np.ascontiguousarray([c for e in els for c in e["coeffs"]], np.float64)
+        rc = self.lib.xo_set_snap(self.h, int(cfg["twojmax"]), float(cfg["rcutfac"]), float(cfg["rfac0"]),
+                                  float(cfg["rmin0"]), int(cfg["switchflag"]), int(cfg["bzeroflag"]), len(els),
+                                  _ptr(rad, C.c_double), _ptr(wj, C.c_double), int(cfg["ncoeffall"]),
+                                  _ptr(coeff, C.c_double), float(energy_unit), int(bool(with_energy)))
+        if rc != 0:
+            raise RuntimeError("oracle set_snap failed: %d" % rc)
 
     def init(self):
         rc = self.lib.xo_init(self.h)

@@ -13,8 +13,11 @@
  *   IJK * double promotes each index to double, then multiplies.
  */
 #include "xnb_oracle.h"
+#include "xnb_snap_oracle.h"
 
 #include <algorithm>
+#include <array>
+#include <memory>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -141,6 +144,8 @@ struct xo_sys {
   std::vector<GhostSend> ghosts;
   int64_t rebuilds = 0;
   bool ready = false;
+  std::unique_ptr<xo_snap::Calc> snap;  // set: the force chain is snap_force_generic
+  bool snap_energy = false;
 
   long gidx(long i, long j, long k) const { return (k * G[1] + j) * G[0] + i; }
   L3 gloc(long c) const { return L3{c % G[0], (c / G[0]) % G[1], c / (G[0] * G[1])}; }
@@ -482,6 +487,7 @@ struct xo_sys {
    * buffer, then LennardJonesForceFunctor (lennard_jones.cu:67-102). The potential
    * energy (discarded by the reference) is 0.5*(e - e(rc)) per stream entry. */
   int compute_forces() {
+    if (snap) return snap_forces();
     int err = 0;
 #pragma omp parallel for schedule(dynamic) reduction(| : err)
     for (long c = 0; c < static_cast<long>(cells.size()); ++c) {
@@ -554,6 +560,115 @@ struct xo_sys {
         }
       }
     }
+    return err ? -4 : 0;
+  }
+
+  /* zero_particle_force { ghost: true } + snap_force_generic + update_force_from_ghost
+   * (+ divide_force_by_type_scalar): SnapForceRealT over the per-particle compute
+   * buffer (contribs/md/snap/include/md/snap/snap_force.h:290-372): for particle i,
+   * the stream entries inside the traversal cutoff whose squared distance lies in
+   * (1e-20, ((rad_i + rad_j) rcutfac)^2) (snap_force_op_coop.hxx:215-226) are its
+   * environment; f_i += sum fij and f_j -= fij for each (snap_force_op_coop.hxx:
+   * 331-356), fij = dE_i/dr_ij. Reactions are applied after all environments, in
+   * cell, particle and stream order; ghost particles' forces then go to the
+   * particles they copy (update_force_from_ghost). */
+  int snap_forces() {
+    for (Cell& C : cells)
+      for (size_t q = 0; q < C.size(); ++q) { C.fx[q] = 0.0; C.fy[q] = 0.0; C.fz[q] = 0.0; C.pe[q] = 0.0; }
+    struct Reac { long cb; uint32_t pb; std::array<double, 3> f; };
+    struct AtomOut { double e; std::array<double, 3> f; std::vector<Reac> reac; };
+    std::vector<std::vector<AtomOut>> out(cells.size());
+    int err = 0;
+#pragma omp parallel for schedule(dynamic) reduction(| : err)
+    for (long c = 0; c < static_cast<long>(cells.size()); ++c) {
+      const L3 la = gloc(c);
+      if (is_ghost(la)) continue;
+      const Cell& A = cells[c];
+      const size_t na = A.size();
+      if (na == 0) continue;
+      out[c].resize(na);
+      const uint16_t* base = streams[c].data();
+      const int ntab = base[0];
+      const int tab = ntab >= 1 ? static_cast<int>((na * ntab + 1) * 2) : 0;
+      const uint16_t* stream_base = base + tab;
+      const uint32_t* offset = reinterpret_cast<const uint32_t*>(base);
+      std::vector<std::array<double, 3>> dr, fij;
+      std::vector<int> tj;
+      std::vector<Reac> who;
+      for (size_t pa = 0; pa < na; ++pa) {
+        const uint16_t* st = stream_base + offset[pa] - ntab;
+        int groups = *(st++);
+        dr.clear(); tj.clear(); who.clear();
+        const int ti = A.type[pa];
+        while (groups-- > 0) {
+          const uint16_t enc = *(st++);
+          int nch = *(st++);
+          const long ri = static_cast<long>(enc & 31) - 16;
+          const long rj = static_cast<long>((enc >> 5) & 31) - 16;
+          const long rk = static_cast<long>((enc >> 10) & 31) - 16;
+          const long cb = c + ((rk * G[1]) + rj) * G[0] + ri;
+          const Cell& B = cells[cb];
+          while (nch-- > 0) {
+            const unsigned pb = *(st++);
+            const double drx = B.rx[pb] - A.rx[pa];
+            const double dry = B.ry[pb] - A.ry[pa];
+            const double drz = B.rz[pb] - A.rz[pa];
+            const double d2 = norm2(drx, dry, drz);
+            if (!(d2 > 0.0 && d2 <= rcut2)) continue;
+            const double cij = snap->cut(ti, B.type[pb]);
+            if (!(d2 < cij * cij && d2 > 1e-20)) continue;
+            dr.push_back({drx, dry, drz});
+            tj.push_back(B.type[pb]);
+            who.push_back({cb, pb, {0.0, 0.0, 0.0}});
+          }
+        }
+        if (dr.size() >= 256) err |= 1;
+        AtomOut& o = out[c][pa];
+        o.e = snap->atom(ti, dr, tj, snap_energy, fij);
+        o.f = {0.0, 0.0, 0.0};
+        for (size_t q = 0; q < fij.size(); ++q) {
+          for (int k = 0; k < 3; ++k) o.f[k] += fij[q][k];
+          who[q].f = fij[q];
+        }
+        o.reac = who;
+      }
+    }
+    for (long c = 0; c < static_cast<long>(cells.size()); ++c) {
+      Cell& A = cells[c];
+      for (size_t pa = 0; pa < out[c].size(); ++pa) {
+        const AtomOut& o = out[c][pa];
+        A.fx[pa] += o.f[0];
+        A.fy[pa] += o.f[1];
+        A.fz[pa] += o.f[2];
+        A.pe[pa] = o.e;
+        for (const Reac& r : o.reac) {
+          Cell& B = cells[r.cb];
+          B.fx[r.pb] -= r.f[0];
+          B.fy[r.pb] -= r.f[1];
+          B.fz[r.pb] -= r.f[2];
+        }
+      }
+    }
+    for (const GhostSend& gs : ghosts) {
+      Cell& owner = cells[gs.src_cell];
+      const Cell& g = cells[gs.dst_cell];
+      for (size_t q = 0; q < gs.particle_i.size() && q < g.size(); ++q) {
+        const uint32_t pi = gs.particle_i[q];
+        owner.fx[pi] += g.fx[q];
+        owner.fy[pi] += g.fy[q];
+        owner.fz[pi] += g.fz[q];
+      }
+    }
+    if (p.divide_by_mass)
+      for (long c = 0; c < static_cast<long>(cells.size()); ++c) {
+        if (is_ghost(gloc(c))) continue;
+        Cell& A = cells[c];
+        for (size_t q = 0; q < A.size(); ++q) {
+          A.fx[q] /= p.mass;
+          A.fy[q] /= p.mass;
+          A.fz[q] /= p.mass;
+        }
+      }
     return err ? -4 : 0;
   }
 
@@ -781,14 +896,20 @@ int xo_load_cells(xo_sys* s, const int64_t* cell_counts, const double* rx, const
   return 0;
 }
 
+int xo_load_lattice_noise_fcc(xo_sys* s, double a, double sigma) { return xo_load_lattice_noise(s, 2, a, sigma); }
+
 /* generate_particle_lattice (grid_cell_particles/include/exanb/grid_cell_particles/
- * generate_particle_lattice.h:247-388) with deterministic_noise, FCC basis
- * (lattice_generator.h:162-170), then GaussianNoise on rx,ry,rz
+ * generate_particle_lattice.h:247-388) with deterministic_noise, SC / BCC / FCC
+ * basis (lattice_generator.h:140-170), then GaussianNoise on rx,ry,rz
  * (compute/include/exanb/compute/gaussian_noise.h:62-80,150-161). */
-int xo_load_lattice_noise_fcc(xo_sys* s, double a, double sigma) {
-  if (!s) return -1;
+int xo_load_lattice_noise(xo_sys* s, int32_t structure, double a, double sigma) {
+  if (!s || structure < 0 || structure > 2) return -1;
   for (auto& c : s->cells) c.clear();
-  const double basis[4][3] = {{.0, .0, .0}, {.0, .5, .5}, {.5, .0, .5}, {.5, .5, .0}};
+  static const double sc[1][3] = {{.5, .5, .5}};
+  static const double bcc[2][3] = {{.0, .0, .0}, {.5, .5, .5}};
+  static const double fcc[4][3] = {{.0, .0, .0}, {.0, .5, .5}, {.5, .0, .5}, {.5, .5, .0}};
+  const double(*basis)[3] = structure == 0 ? sc : structure == 1 ? bcc : fcc;
+  const int nbasis = structure == 0 ? 1 : structure == 1 ? 2 : 4;
   const double lo[3] = {s->p.origin[0], s->p.origin[1], s->p.origin[2]};
   const double hi[3] = {s->p.extent[0], s->p.extent[1], s->p.extent[2]};
   const long ist = static_cast<long>(std::floor(lo[0] / a)) - 1, iend = static_cast<long>(std::ceil(hi[0] / a)) + 1;
@@ -805,7 +926,7 @@ int xo_load_lattice_noise_fcc(xo_sys* s, double a, double sigma) {
   for (long k = kst; k <= kend; ++k)
     for (long j = jst; j <= jend; ++j)
       for (long i = ist; i <= iend; ++i)
-        for (int l = 0; l < 4; ++l) {
+        for (int l = 0; l < nbasis; ++l) {
           const double x = (static_cast<double>(i) + basis[l][0]) * a;
           const double y = (static_cast<double>(j) + basis[l][1]) * a;
           const double z = (static_cast<double>(k) + basis[l][2]) * a;
@@ -974,6 +1095,30 @@ int xo_get_cell_stream(const xo_sys* s, int64_t ci, uint16_t* out) {
 
 int xo_set_types(xo_sys* s, const uint64_t* ids, const uint8_t* types, int64_t n) {
   return s->set_types(ids, types, n);
+}
+
+int xo_set_snap(xo_sys* s, int32_t twojmax, double rcutfac, double rfac0, double rmin0, int32_t switchflag,
+                int32_t bzeroflag, int32_t ntypes, const double* radelem, const double* wj, int32_t ncoeffall,
+                const double* coeff, double energy_unit, int32_t with_energy) {
+  if (!s || twojmax < 0 || twojmax > 16 || ntypes < 1 || !radelem || !wj || !coeff) return -1;
+  xo_snap::Spec sp;
+  sp.twojmax = twojmax;
+  sp.rcutfac = rcutfac;
+  sp.rfac0 = rfac0;
+  sp.rmin0 = rmin0;
+  sp.switchflag = switchflag != 0;
+  sp.bzeroflag = bzeroflag != 0;
+  sp.ntypes = ntypes;
+  sp.radelem.assign(radelem, radelem + ntypes);
+  sp.wj.assign(wj, wj + ntypes);
+  sp.ncoeffall = ncoeffall;
+  sp.coeff.assign(coeff, coeff + static_cast<size_t>(ntypes) * ncoeffall);
+  sp.energy_unit = energy_unit;
+  auto calc = std::make_unique<xo_snap::Calc>(sp);
+  if (calc->ncoeff() + 1 != ncoeffall) return -2;
+  s->snap = std::move(calc);
+  s->snap_energy = with_energy != 0;
+  return 0;
 }
 
 int xo_gravitational_force(xo_sys* s, double G, const double* type_mass, int32_t ntypes, double rcut) {

@@ -55,6 +55,8 @@ int xo_load_cells(xo_sys* s, const int64_t* cell_counts, const double* rx, const
 /* Reference Ni golden-deck initial state: FCC lattice (generate_particle_lattice.h)
  * with deterministic gaussian position noise (gaussian_noise.h). Loads cells. */
 int xo_load_lattice_noise_fcc(xo_sys* s, double lattice_a, double noise_sigma);
+/* The same generator for structure 0 = SC, 1 = BCC, 2 = FCC. */
+int xo_load_lattice_noise(xo_sys* s, int32_t structure, double lattice_a, double noise_sigma);
 
 /* init_particles (update-particles.msp:31-36) followed by compute_all_forces_energy. */
 int xo_init(xo_sys* s);
@@ -89,6 +91,15 @@ int xo_set_types(xo_sys* s, const uint64_t* ids, const uint8_t* types, int64_t n
 /* zero_particle_force + gravitational_force (contribs/pi/gravitational_force.cu:42-141)
  * over the current streams with cutoff rcut (<= the neighbour distance); masses per type. */
 int xo_gravitational_force(xo_sys* s, double G, const double* type_mass, int32_t ntypes, double rcut);
+/* From now on the force chain is snap_force_generic (linear SNAP, one element
+ * set: chemflag, bnormflag, quadraticflag, switchinnerflag off), followed by
+ * update_force_from_ghost and, when the system divides by mass, the division.
+ * coeff: ntypes x ncoeffall (constant term first); forces and energies are
+ * multiplied by energy_unit. with_energy: per-particle energies in pe.
+ * Returns -2 when ncoeffall does not match twojmax. */
+int xo_set_snap(xo_sys* s, int32_t twojmax, double rcutfac, double rfac0, double rmin0, int32_t switchflag,
+                int32_t bzeroflag, int32_t ntypes, const double* radelem, const double* wj, int32_t ncoeffall,
+                const double* coeff, double energy_unit, int32_t with_energy);
 int xo_energy(const xo_sys* s, double* ke, double* pe);
 
 /* Count of particles over the displacement threshold right now (particle_displ_over). */
