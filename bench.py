@@ -75,6 +75,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--force-block", type=int, default=0, help="threads per block of the force kernel (0: library default)")
     ap.add_argument("--stage-cap", type=int, default=0, help="neighbour-build staging candidates (0: library default)")
+    ap.add_argument("--workload", default="lj", choices=["lj", "snap_ni", "snap_mo"],
+                    help="lj: the 4M-atom LJ headline; snap_*: the reference's SNAP benchmark decks")
     return ap.parse_args()
 
 
@@ -441,8 +443,197 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# SNAP workloads: the systems of the reference's benchmark_lj_snap SNAP decks
+# (input_snap_{Ni,Mo}.msp: FCC Ni 16^3 / BCC Mo 16^3 with Gaussian noise, 4^3
+# cells, rcut_inc 2 A, dt 2 fs, mass division), started at rest, one bench step =
+# one velocity-Verlet step with snap_force_generic.
+SNAP_DECKS = {
+    "snap_ni": dict(el="Ni", structure="FCC", n=16, a=3.48, sigma=0.05, mass=58.693, cells=4),
+    "snap_mo": dict(el="Mo", structure="BCC", n=16, a=3.15, sigma=0.1, mass=95.96, cells=4),
+}
+
+
+def snap_setup(name):
+    from exanbody_gb300 import snap
+
+    d = SNAP_DECKS[name]
+    g = os.path.join(ROOT, "tests", "golden", "snap")
+    cfg = snap.read_lammps(os.path.join(g, "%s_Zuo_JPCA2020.snapparam" % d["el"]),
+                           os.path.join(g, "%s_Zuo_JPCA2020.snapcoeff" % d["el"]))
+    r = snap.lattice(d["structure"], d["n"], d["a"], d["sigma"], 2024)
+    L = d["n"] * d["a"]
+    geom = {"origin": (0.0, 0.0, 0.0), "extent": (L, L, L), "dims": (d["cells"],) * 3, "cell_size": L / d["cells"]}
+    return d, cfg, r, geom
+
+
+def snap_flop64_per_atom(cfg, nn):
+    """FP64 flop (FMA = 2) of one atom's SNAP force in this implementation's
+    formulation: per neighbour and unique U element, 20 (U recursion) + 4 (its
+    weighted sum into U_tot) + 4 (F) + 16 (dF/da, dF/db) + 20 (adjoint gather);
+    per Z element 10 per Clebsch-Gordan product term, 4 per row and 4 for its Y
+    contribution."""
+    J = int(cfg["twojmax"])
+    nu = sum(((j + 1) // 2) * (j + 1) if j % 2 else (j // 2) * (j + 1) + j // 2 + 1 for j in range(J + 1))
+    z = 0
+    for j1 in range(J + 1):
+        for j2 in range(j1 + 1):
+            for j in range(j1 - j2, min(J, j1 + j2) + 1, 2):
+                for mb in range(j // 2 + 1):
+                    for ma in range(j + 1):
+                        if 2 * mb == j and ma > mb:
+                            continue
+                        ma1 = max(0, (2 * ma - j - j2 + j1) // 2)
+                        na = min(j1, (2 * ma - j + j2 + j1) // 2) - ma1 + 1
+                        mb1 = max(0, (2 * mb - j - j2 + j1) // 2)
+                        nb = min(j1, (2 * mb - j + j2 + j1) // 2) - mb1 + 1
+                        z += nb * (10 * na + 4) + 4
+    return nn * nu * (20 + 4 + 4 + 16 + 20) + z
+
+
+def run_snap(args):
+    import torch
+
+    from exanbody_gb300 import snap, xnb
+
+    rank, world, local = dist_env()
+    name = args.workload
+    d, cfg, r, geom = snap_setup(name)
+    N = len(r)
+    L = geom["extent"][0]
+    nbh = cfg["rcutfac"] + 2.0
+    params = xnb.lj_params(geom, rcut=cfg["rcutfac"], rcut_inc=2.0, dt=2e-3, mass=d["mass"], divide_by_mass=True)
+    ids = np.arange(1, N + 1, dtype=np.uint64)
+    v0 = np.zeros_like(r)
+    metric = "atom-steps/s, SNAP MD step (%s %s %d^3, %d atoms, twojmax %d, FP64)" % (
+        d["structure"], d["el"], d["n"], N, cfg["twojmax"])
+    conf = {"workload": "%s_%s%d^3_snap_twojmax%d" % (name, d["structure"], d["n"], cfg["twojmax"]), "atoms": N,
+            "rcut": cfg["rcutfac"], "skin": 2.0, "dt_ps": 2e-3, "deck": "input_%s.msp" % name.replace("snap_", "snap_"),
+            "flush": "none: the SNAP kernel is FP64-bound; its state (%.1f MB) stays in L2" % (N * 900 / 1e6)}
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        from oracle.oracle import OracleSystem
+
+        s = OracleSystem((0, 0, 0), (L, L, L), geom["dims"], geom["cell_size"], cfg["rcutfac"], 2.0, 1.0, 1.0, 2e-3,
+                         mass=d["mass"], divide_by_mass=True, kind="omp")
+        used = s.set_threads(os.cpu_count() or 1)
+        s.set_snap(cfg, snap.energy_unit())
+        s.load_flat(r, v0, ids)
+        s.init()
+        for _ in range(args.warmup):
+            s.step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s.step()
+        dt = time.perf_counter() - t0
+        v = N * args.steps / dt
+        print(json.dumps({"impl": "reference", "metric": metric, "value": v, "unit": "atom-steps/s", "n_gpus": args.gpus,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic", "config": conf,
+                          "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": used, "kind": "port",
+                                           "sample": "%d SNAP MD steps, oracle/xnb_snap_oracle.h OpenMP" % args.steps},
+                          "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return 0
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    b = xnb.Batch(N + 64, geom["dims"][0] ** 3 + 64, N * 200 + 4096, max_systems=1, device=local)
+    s = b.add_system(params, r, v0, ids)
+    b.init_particles(s, xnb.PREC_FP64)
+    pot = snap.Potential(cfg, device=local)
+    pot.force(b, s)
+    snap.md_steps(b, s, pot, max(3, args.warmup))
+    steps = args.steps
+    reb0 = b.info(s).rebuilds
+    l0 = b.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as ck:
+        torch.cuda.synchronize()
+        e0.record()
+        snap.md_steps(b, s, pot, steps)
+        e1.record()
+        e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = b.kernel_launches() - l0
+    rebuilds = b.info(s).rebuilds - reb0
+    # the force kernel alone
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    f0.record()
+    for _ in range(5):
+        pot.force(b, s)
+    f1.record()
+    f1.synchronize()
+    ms_force = f0.elapsed_time(f1) / 5
+    # neighbours inside the SNAP cutoff (for the operation count)
+    P = b.download(s)
+    try:
+        from scipy.spatial import cKDTree
+
+        pts = np.stack([P["rx"], P["ry"], P["rz"]], 1) % L
+        tree = cKDTree(pts, boxsize=L)
+        nn = float(np.mean([len(x) - 1 for x in tree.query_ball_point(pts[:2000], cfg["rcutfac"])]))
+    except ImportError:
+        nn = 18.0 if d["structure"] == "FCC" else 14.0
+    flop = snap_flop64_per_atom(cfg, nn)
+    peak64 = fp64_peak_tflops(torch, dev)
+    achieved = flop * N / (ms_force * 1e-3) / 1e12
+    b.check_errors()
+    b.close()
+    e2e = None
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        bb = xnb.Batch(N + 64, geom["dims"][0] ** 3 + 64, N * 200 + 4096, max_systems=1, device=local)
+        ss = bb.add_system(params, r, v0, ids)
+        bb.init_particles(ss, xnb.PREC_FP64)
+        pot.force(bb, ss)
+        snap.md_steps(bb, ss, pot, steps)
+        out = bb.download(ss)
+        dt = time.perf_counter() - t0
+        bb.close()
+        e2e = {"value": N * steps / dt, "unit": "atom-steps/s", "h2d_bytes_per_step": N * 56 / steps,
+               "d2h_bytes_per_step": N * 92 / steps,
+               "run": "host arrays -> xnb_system_add -> init + xnb_snap_force -> %d SNAP MD steps -> download"
+                      % steps}
+        del out
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle.oracle import OracleSystem
+
+        so = OracleSystem((0, 0, 0), (L, L, L), geom["dims"], geom["cell_size"], cfg["rcutfac"], 2.0, 1.0, 1.0,
+                          2e-3, mass=d["mass"], divide_by_mass=True, kind="omp")
+        used = so.set_threads(os.cpu_count() or 1)
+        so.set_snap(cfg, snap.energy_unit())
+        so.load_flat(r, v0, ids)
+        so.init()
+        sample = 3
+        t0 = time.perf_counter()
+        for _ in range(sample):
+            so.step()
+        dt = time.perf_counter() - t0
+        cpu = {"value": N * sample / dt, "unit": "atom-steps/s", "cores": used, "kind": "port",
+               "sample": "%d SNAP MD steps of the same system, oracle OpenMP build" % sample}
+    if rank == 0:
+        print(json.dumps({
+            "metric": metric, "value": world * N * steps / (ms * 1e-3), "unit": "atom-steps/s", "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(conf, rebuilds_in_timed_steps=rebuilds, neighbours_in_cutoff=nn),
+            "clocks": ck.summary(), "e2e": e2e, "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "kernel": "k_snap", "achieved": achieved, "peak": peak64,
+                         "unit": "TFLOP/s", "frac": achieved / peak64,
+                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                         "flop_per_atom": flop, "ms_per_launch": ms_force, "traffic": None},
+            "cpu_baseline": cpu}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload != "lj":
+        return run_snap(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

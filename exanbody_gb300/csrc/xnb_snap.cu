@@ -124,27 +124,69 @@ __global__ void k_snap_zero(uint32_t n_part, const SysDesc* __restrict__ sys, co
   if (zero_pe) a.pe[i] = 0.0;
 }
 
-__global__ void __launch_bounds__(kSnapWarps * 32)
+__device__ __forceinline__ bool uq(int j, int r, int c) {
+  return r >= 0 && c >= 0 && c <= j && r * (j + 1) + c < nunique(j);
+}
+
+// Forward U levels 1..J of one neighbour into its unique-half buffer u (level j
+// at ublk[j]); level 0 is set by the caller. Threads slot, slot + lpn, ... of the
+// neighbour take the elements of each level; the CTA synchronises between levels.
+__device__ __forceinline__ void forward_levels(double* u, bool active, int slot, int lpn, C2 a, C2 b,
+                                               const SnapArgs& t) {
+  const int J = t.twojmax;
+  for (int j = 1; j <= J; ++j) {
+    if (active) {
+      const int nuj = nunique(j);
+      const double* prev = u + 2 * t.ublk[j - 1];
+      double* cur = u + 2 * t.ublk[j];
+      for (int e = slot; e < nuj; e += lpn) {
+        const int mb = e / (j + 1), ma = e % (j + 1);
+        C2 v{0.0, 0.0};
+        if (ma < j) {
+          const C2 p = level_get(prev, 2, 0, j - 1, mb, ma);
+          const double rp = t.rootpq[(j - ma) * (J + 1) + (j - mb)];
+          const C2 q = cmulc(a, p);
+          v.r = rp * q.r;
+          v.i = rp * q.i;
+        }
+        if (ma > 0) {
+          const C2 p = level_get(prev, 2, 0, j - 1, mb, ma - 1);
+          const double rp = t.rootpq[ma * (J + 1) + (j - mb)];
+          const C2 q = cmulc(b, p);
+          v.r = fma(-rp, q.r, v.r);
+          v.i = fma(-rp, q.i, v.i);
+        }
+        cur[2 * e] = v.r;
+        cur[2 * e + 1] = v.i;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kSnapThreads)
     k_snap(uint32_t n_part, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a,
            SnapArgs t, int sys_only, bool with_pe, unsigned int* flags) {
   extern __shared__ double sm[];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int J = t.twojmax;
   const int lvl_max = nunique(J);
+  const int nu = t.nu_unique;
   // shared layout (doubles)
   double* nx = sm;
   double* ny = nx + kSnapMaxNbr;
   double* nz = ny + kSnapMaxNbr;
-  uint32_t* nj = reinterpret_cast<uint32_t*>(nz + kSnapMaxNbr);          // kSnapMaxNbr u32
-  uint8_t* nt = reinterpret_cast<uint8_t*>(nj + kSnapMaxNbr);            // kSnapMaxNbr u8
-  double* utot = nz + kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8;   // 2 * nu_full
-  double* yv = utot + 2 * t.nu_full;                                      // 2 * nu_unique
-  double* upart = yv + 2 * t.nu_unique;                                   // warps x 2 * nu_unique
-  double* lvl = upart + kSnapWarps * 2 * t.nu_unique;                     // warps x 2 x lvl_max x 8
-  double* red = lvl + kSnapWarps * 2 * lvl_max * 8;                      // 8 doubles
-  int* icnt = reinterpret_cast<int*>(red + 8);                            // 8 ints
-  double* my_up = upart + w * 2 * t.nu_unique;
-  double* my_lvl = lvl + w * 2 * lvl_max * 8;
+  double* nsw = nz + kSnapMaxNbr;                                          // wj sfac per neighbour
+  uint32_t* nj = reinterpret_cast<uint32_t*>(nsw + kSnapMaxNbr);           // kSnapMaxNbr u32
+  uint8_t* nt = reinterpret_cast<uint8_t*>(nj + kSnapMaxNbr);              // kSnapMaxNbr u8
+  double* utot = nsw + kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8;    // 2 nu_full
+  double* yv = utot + 2 * t.nu_full;                                        // 2 nu
+  double* uacc = yv + 2 * nu;                                               // 2 nu
+  double* red = uacc + 2 * nu;                                              // kSnapThreads x 5
+  double* misc = red + kSnapThreads * 5;                                    // 8 doubles: fsum[3], wsum[4]
+  int* icnt = reinterpret_cast<int*>(misc + 8);                             // 8 ints
+  double* uall = misc + 12;                                                 // group x 2 nu
+  double* adj = uall + static_cast<size_t>(t.group) * 2 * nu;               // group x 2 x 2 lvl_max
 
   for (uint32_t i = blockIdx.x; i < n_part; i += gridDim.x) {
     const uint32_t c = a.pcell[i];
@@ -166,9 +208,12 @@ __global__ void __launch_bounds__(kSnapWarps * 32)
     const double fscale = S.divide_by_mass ? t.energy_unit / S.mass : t.energy_unit;
 
     // ---- environment, in list order ----
-    if (tid == 0) icnt[4] = 0;
+    if (tid == 0) {
+      icnt[4] = 0;
+      misc[0] = misc[1] = misc[2] = 0.0;
+    }
     __syncthreads();
-    for (uint32_t base = 0; base < n; base += kSnapWarps * 32) {
+    for (uint32_t base = 0; base < n; base += kSnapThreads) {
       const uint32_t k = base + tid;
       bool keep = false;
       double dx = 0, dy = 0, dz = 0;
@@ -219,64 +264,48 @@ __global__ void __launch_bounds__(kSnapWarps * 32)
       continue;
     }
 
-    // ---- U_tot: per-warp partial sums over the unique half ----
-    for (int e = lane; e < 2 * t.nu_unique; e += 32) my_up[e] = 0.0;
-    __syncwarp();
-    for (int q = w; q < nn; q += kSnapWarps) {
-      const double rcut = (radi + t.radelem[nt[q]]) * t.rcutfac;
-      const Geo g = geometry(nx[q], ny[q], nz[q], rcut, t, false);
-      const double sw = t.wj[nt[q]] * g.sfac;
-      double* prev = my_lvl;
-      double* cur = my_lvl + lvl_max * 8;
-      if (lane == 0) {
-        prev[0] = 1.0;
-        prev[1] = 0.0;
-        my_up[0] += sw;
-      }
-      __syncwarp();
-      for (int j = 1; j <= J; ++j) {
-        const int nuj = nunique(j);
-        for (int e = lane; e < nuj; e += 32) {
-          const int mb = e / (j + 1), ma = e % (j + 1);
-          C2 u{0.0, 0.0};
-          if (ma < j) {
-            const C2 up = level_get(prev, 8, 0, j - 1, mb, ma);
-            const double rp = t.rootpq[(j - ma) * (J + 1) + (j - mb)];
-            const C2 v = cmulc(g.a, up);
-            u.r += rp * v.r;
-            u.i += rp * v.i;
-          }
-          if (ma > 0) {
-            const C2 up = level_get(prev, 8, 0, j - 1, mb, ma - 1);
-            const double rp = t.rootpq[ma * (J + 1) + (j - mb)];
-            const C2 v = cmulc(g.b, up);
-            u.r -= rp * v.r;
-            u.i -= rp * v.i;
-          }
-          cur[e * 8] = u.r;
-          cur[e * 8 + 1] = u.i;
-          my_up[2 * (t.ublk[j] + e)] += sw * u.r;
-          my_up[2 * (t.ublk[j] + e) + 1] += sw * u.i;
+    // ---- U_tot = self + sum_j wj sfac U_j, neighbours in rounds of `group` ----
+    for (int e = tid; e < 2 * nu; e += kSnapThreads) uacc[e] = 0.0;
+    for (int q0 = 0; q0 < nn; q0 += t.group) {
+      const int gr = min(t.group, nn - q0);
+      const int lpn = kSnapThreads / gr;
+      const int g = tid / lpn, slot = tid % lpn;
+      const bool active = g < gr;
+      double* ug = uall + static_cast<size_t>(active ? g : 0) * 2 * nu;
+      C2 ca{0.0, 0.0}, cb{0.0, 0.0};
+      if (active) {
+        const int q = q0 + g;
+        const double rcut = (radi + t.radelem[nt[q]]) * t.rcutfac;
+        const Geo geo = geometry(nx[q], ny[q], nz[q], rcut, t, false);
+        ca = geo.a;
+        cb = geo.b;
+        if (slot == 0) {
+          nsw[q] = t.wj[nt[q]] * geo.sfac;
+          ug[0] = 1.0;
+          ug[1] = 0.0;
         }
-        __syncwarp();
-        double* tmp = prev;
-        prev = cur;
-        cur = tmp;
       }
-      __syncwarp();
+      __syncthreads();
+      forward_levels(ug, active, slot, lpn, ca, cb, t);
+      for (int e = tid; e < nu; e += kSnapThreads) {
+        double re = 0.0, im = 0.0;
+        for (int q = 0; q < gr; ++q) {
+          const double sw = nsw[q0 + q];
+          re = fma(sw, uall[static_cast<size_t>(q) * 2 * nu + 2 * e], re);
+          im = fma(sw, uall[static_cast<size_t>(q) * 2 * nu + 2 * e + 1], im);
+        }
+        uacc[2 * e] += re;
+        uacc[2 * e + 1] += im;
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    // ---- combine the partials, add the self term, expand to the full matrices ----
-    for (int e = tid; e < t.nu_unique; e += kSnapWarps * 32) {
+    // ---- self term, full matrices ----
+    for (int e = tid; e < nu; e += kSnapThreads) {
       int j = 0;
       while (j < J && e >= t.ublk[j + 1]) ++j;
       const int le = e - t.ublk[j];
       const int mb = le / (j + 1), ma = le % (j + 1);
-      double re = (mb == ma) ? 1.0 : 0.0, im = 0.0;
-      for (int q = 0; q < kSnapWarps; ++q) {
-        re += upart[q * 2 * t.nu_unique + 2 * e];
-        im += upart[q * 2 * t.nu_unique + 2 * e + 1];
-      }
+      const double re = uacc[2 * e] + ((mb == ma) ? 1.0 : 0.0), im = uacc[2 * e + 1];
       const int f = t.fblk[j] + mb * (j + 1) + ma;
       utot[2 * f] = re;
       utot[2 * f + 1] = im;
@@ -294,7 +323,7 @@ __global__ void __launch_bounds__(kSnapWarps * 32)
     double eloc = 0.0;
     const double* zb = t.zbeta + static_cast<size_t>(ti) * t.nz;
     const double* ze = t.zener + static_cast<size_t>(ti) * t.nz;
-    for (int e = tid; e < t.nz; e += kSnapWarps * 32) {
+    for (int e = tid; e < t.nz; e += kSnapThreads) {
       const SnapZ z = t.z[e];
       const double* cgb = t.cg + z.cg;
       const int j1 = z.j1, j2 = z.j2;
@@ -330,105 +359,164 @@ __global__ void __launch_bounds__(kSnapWarps * 32)
     }
     if (with_pe) {
       eloc = warp_sum(eloc);
-      if (lane == 0) red[w] = eloc;
+      if (lane == 0) misc[4 + w] = eloc;
     }
     __syncthreads();
     if (with_pe && tid == 0) {
       double es = t.e0[ti];
-      for (int q = 0; q < kSnapWarps; ++q) es += red[q];
+      for (int q = 0; q < kSnapWarps; ++q) es += misc[4 + q];
       a.pe[i] = es * t.energy_unit;
     }
-    // ---- forces: U and dU per neighbour, contracted with Y ----
-    double fi0 = 0.0, fi1 = 0.0, fi2 = 0.0;
-    for (int q = w; q < nn; q += kSnapWarps) {
-      const double rcut = (radi + t.radelem[nt[q]]) * t.rcutfac;
-      const Geo g = geometry(nx[q], ny[q], nz[q], rcut, t, true);
-      const double wjq = t.wj[nt[q]];
-      const double sw = wjq * g.sfac, dsw = wjq * g.dsfac;
-      double* prev = my_lvl;
-      double* cur = my_lvl + lvl_max * 8;
-      double f0 = 0.0, f1 = 0.0, f2 = 0.0;
-      if (lane == 0) {
-        prev[0] = 1.0;
-        prev[1] = 0.0;
-        for (int k = 2; k < 8; ++k) prev[k] = 0.0;
-        // level 0 (centre, weight 1/2): dU_tot = dsfac * 1 * u
-        f0 += 0.5 * dsw * g.u[0] * yv[0];
-        f1 += 0.5 * dsw * g.u[1] * yv[0];
-        f2 += 0.5 * dsw * g.u[2] * yv[0];
-      }
-      __syncwarp();
-      for (int j = 1; j <= J; ++j) {
-        const int nuj = nunique(j);
-        const bool even = (j & 1) == 0;
-        for (int e = lane; e < nuj; e += 32) {
-          const int mb = e / (j + 1), ma = e % (j + 1);
-          C2 u{0.0, 0.0}, du[3] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
-          if (ma < j) {
-            const double rp = t.rootpq[(j - ma) * (J + 1) + (j - mb)];
-            const C2 up = level_get(prev, 8, 0, j - 1, mb, ma);
-            C2 v = cmulc(g.a, up);
-            u.r += rp * v.r;
-            u.i += rp * v.i;
-            for (int k = 0; k < 3; ++k) {
-              const C2 dup = level_get(prev, 8, 2 + 2 * k, j - 1, mb, ma);
-              const C2 v1 = cmulc(g.da[k], up), v2 = cmulc(g.a, dup);
-              du[k].r += rp * (v1.r + v2.r);
-              du[k].i += rp * (v1.i + v2.i);
-            }
-          }
-          if (ma > 0) {
-            const double rp = t.rootpq[ma * (J + 1) + (j - mb)];
-            const C2 up = level_get(prev, 8, 0, j - 1, mb, ma - 1);
-            C2 v = cmulc(g.b, up);
-            u.r -= rp * v.r;
-            u.i -= rp * v.i;
-            for (int k = 0; k < 3; ++k) {
-              const C2 dup = level_get(prev, 8, 2 + 2 * k, j - 1, mb, ma - 1);
-              const C2 v1 = cmulc(g.db[k], up), v2 = cmulc(g.b, dup);
-              du[k].r -= rp * (v1.r + v2.r);
-              du[k].i -= rp * (v1.i + v2.i);
-            }
-          }
-          double* o = cur + e * 8;
-          o[0] = u.r;
-          o[1] = u.i;
-          for (int k = 0; k < 3; ++k) {
-            o[2 + 2 * k] = du[k].r;
-            o[3 + 2 * k] = du[k].i;
-          }
-          const double wgt = (even && e == nuj - 1) ? 0.5 : 1.0;
-          const double yr = yv[2 * (t.ublk[j] + e)], yi = yv[2 * (t.ublk[j] + e) + 1];
-          const double dtr0 = dsw * u.r * g.u[0] + sw * du[0].r, dti0 = dsw * u.i * g.u[0] + sw * du[0].i;
-          const double dtr1 = dsw * u.r * g.u[1] + sw * du[1].r, dti1 = dsw * u.i * g.u[1] + sw * du[1].i;
-          const double dtr2 = dsw * u.r * g.u[2] + sw * du[2].r, dti2 = dsw * u.i * g.u[2] + sw * du[2].i;
-          f0 += wgt * fma(dtr0, yr, dti0 * yi);
-          f1 += wgt * fma(dtr1, yr, dti1 * yi);
-          f2 += wgt * fma(dtr2, yr, dti2 * yi);
+
+    // ---- forces by reverse mode: F = sum_e w Re(conj(U_e) Y_e) per neighbour,
+    //      dF/da and dF/db from the adjoint w Y propagated down the levels ----
+    for (int q0 = 0; q0 < nn; q0 += t.group) {
+      const int gr = min(t.group, nn - q0);
+      const int lpn = kSnapThreads / gr;
+      const int g = tid / lpn, slot = tid % lpn;
+      const bool active = g < gr;
+      double* ug = uall + static_cast<size_t>(active ? g : 0) * 2 * nu;
+      double* adj0 = adj + static_cast<size_t>(active ? g : 0) * 4 * lvl_max;
+      double* adj1 = adj0 + 2 * lvl_max;
+      C2 ca{0.0, 0.0}, cb{0.0, 0.0};
+      if (active) {
+        const int q = q0 + g;
+        const double rcut = (radi + t.radelem[nt[q]]) * t.rcutfac;
+        const Geo geo = geometry(nx[q], ny[q], nz[q], rcut, t, false);
+        ca = geo.a;
+        cb = geo.b;
+        if (nn > t.group && slot == 0) {  // U of this round's neighbours was overwritten
+          ug[0] = 1.0;
+          ug[1] = 0.0;
         }
-        __syncwarp();
-        double* tmp = prev;
-        prev = cur;
-        cur = tmp;
       }
-      f0 = warp_sum(f0) * 2.0 * fscale;
-      f1 = warp_sum(f1) * 2.0 * fscale;
-      f2 = warp_sum(f2) * 2.0 * fscale;
-      if (lane == 0) {
+      if (nn > t.group) {
+        __syncthreads();
+        forward_levels(ug, active, slot, lpn, ca, cb, t);
+      }
+      double F = 0.0, gar = 0.0, gai = 0.0, gbr = 0.0, gbi = 0.0;
+      // seed the top level
+      if (active) {
+        const int nuJ = nunique(J);
+        for (int e = slot; e < nuJ; e += lpn) {
+          const double wgt = ((J & 1) == 0 && e == nuJ - 1) ? 0.5 : 1.0;
+          adj0[2 * e] = wgt * yv[2 * (t.ublk[J] + e)];
+          adj0[2 * e + 1] = wgt * yv[2 * (t.ublk[J] + e) + 1];
+        }
+      }
+      __syncthreads();
+      double* A = adj0;
+      double* Nx = adj1;
+      for (int j = J; j >= 1; --j) {
+        const int Lv = j - 1;
+        if (active) {
+          const int nuj = nunique(j);
+          const double* uj = ug + 2 * t.ublk[j];
+          const double* ul = ug + 2 * t.ublk[Lv];
+          const double* yj = yv + 2 * t.ublk[j];
+          for (int e = slot; e < nuj; e += lpn) {
+            const int mb = e / (j + 1), ma = e % (j + 1);
+            const double wgt = ((j & 1) == 0 && e == nuj - 1) ? 0.5 : 1.0;
+            F = fma(wgt, fma(uj[2 * e], yj[2 * e], uj[2 * e + 1] * yj[2 * e + 1]), F);
+            const double Gr = A[2 * e], Gi = A[2 * e + 1];
+            if (ma < j) {
+              const C2 p = level_get(ul, 2, 0, Lv, mb, ma);
+              const double rp = t.rootpq[(j - ma) * (J + 1) + (j - mb)];
+              gar = fma(rp, fma(Gr, p.r, Gi * p.i), gar);
+              gai = fma(rp, fma(Gr, p.i, -(Gi * p.r)), gai);
+            }
+            if (ma > 0) {
+              const C2 p = level_get(ul, 2, 0, Lv, mb, ma - 1);
+              const double rp = t.rootpq[ma * (J + 1) + (j - mb)];
+              gbr = fma(-rp, fma(Gr, p.r, Gi * p.i), gbr);
+              gbi = fma(-rp, fma(Gr, p.i, -(Gi * p.r)), gbi);
+            }
+          }
+          // adjoint of level j-1 by gathering its readers in level j
+          const int nul = nunique(Lv);
+          const double* yl = yv + 2 * t.ublk[Lv];
+          for (int u = slot; u < nul; u += lpn) {
+            const int r = u / (Lv + 1), cc = u % (Lv + 1);
+            const double wgt = ((Lv & 1) == 0 && u == nul - 1) ? 0.5 : 1.0;
+            double accr = wgt * yl[2 * u], acci = wgt * yl[2 * u + 1];
+            if (uq(j, r, cc)) {
+              const int k = r * (j + 1) + cc;
+              const double rp = t.rootpq[(j - cc) * (J + 1) + (j - r)];
+              const C2 m = cmul(ca, C2{A[2 * k], A[2 * k + 1]});
+              accr = fma(rp, m.r, accr);
+              acci = fma(rp, m.i, acci);
+            }
+            if (cc + 1 <= j && uq(j, r, cc + 1)) {
+              const int k = r * (j + 1) + cc + 1;
+              const double rp = t.rootpq[(cc + 1) * (J + 1) + (j - r)];
+              const C2 m = cmul(cb, C2{A[2 * k], A[2 * k + 1]});
+              accr = fma(-rp, m.r, accr);
+              acci = fma(-rp, m.i, acci);
+            }
+            const int r2 = Lv - r, c2 = Lv - cc;
+            if (!(r2 == r && c2 == cc) && !uq(Lv, r2, c2)) {
+              double tr = 0.0, tim = 0.0;
+              if (uq(j, r2, c2)) {
+                const int k = r2 * (j + 1) + c2;
+                const double rp = t.rootpq[(j - c2) * (J + 1) + (j - r2)];
+                const C2 m = cmul(ca, C2{A[2 * k], A[2 * k + 1]});
+                tr = rp * m.r;
+                tim = rp * m.i;
+              }
+              if (c2 + 1 <= j && uq(j, r2, c2 + 1)) {
+                const int k = r2 * (j + 1) + c2 + 1;
+                const double rp = t.rootpq[(c2 + 1) * (J + 1) + (j - r2)];
+                const C2 m = cmul(cb, C2{A[2 * k], A[2 * k + 1]});
+                tr = fma(-rp, m.r, tr);
+                tim = fma(-rp, m.i, tim);
+              }
+              const double sg = ((r2 + c2) & 1) ? -1.0 : 1.0;
+              accr = fma(sg, tr, accr);
+              acci = fma(-sg, tim, acci);
+            }
+            Nx[2 * u] = accr;
+            Nx[2 * u + 1] = acci;
+          }
+        }
+        __syncthreads();
+        double* tmp = A;
+        A = Nx;
+        Nx = tmp;
+      }
+      if (active && slot == 0) F += 0.5 * yv[0];  // level 0: U = 1, centre weight 1/2
+      red[tid * 5 + 0] = active ? F : 0.0;
+      red[tid * 5 + 1] = gar;
+      red[tid * 5 + 2] = gai;
+      red[tid * 5 + 3] = gbr;
+      red[tid * 5 + 4] = gbi;
+      __syncthreads();
+      if (tid < gr) {
+        const int q = q0 + tid;
+        double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int sl = 0; sl < lpn; ++sl)
+          for (int k = 0; k < 5; ++k) v[k] += red[(tid * lpn + sl) * 5 + k];
+        const double rcut = (radi + t.radelem[nt[q]]) * t.rcutfac;
+        const Geo geo = geometry(nx[q], ny[q], nz[q], rcut, t, true);
+        const double wjq = t.wj[nt[q]];
+        double f[3];
+        for (int k = 0; k < 3; ++k) {
+          const double dF = v[1] * geo.da[k].r + v[2] * geo.da[k].i + v[3] * geo.db[k].r + v[4] * geo.db[k].i;
+          f[k] = 2.0 * fscale * wjq * (geo.dsfac * geo.u[k] * v[0] + geo.sfac * dF);
+        }
         const uint32_t j = nj[q];
-        atomicAdd(a.fx + j, -f0);
-        atomicAdd(a.fy + j, -f1);
-        atomicAdd(a.fz + j, -f2);
-        fi0 += f0;
-        fi1 += f1;
-        fi2 += f2;
+        atomicAdd(a.fx + j, -f[0]);
+        atomicAdd(a.fy + j, -f[1]);
+        atomicAdd(a.fz + j, -f[2]);
+        atomicAdd(&misc[0], f[0]);
+        atomicAdd(&misc[1], f[1]);
+        atomicAdd(&misc[2], f[2]);
       }
-      __syncwarp();
+      __syncthreads();
     }
-    if (lane == 0) {
-      atomicAdd(a.fx + i, fi0);
-      atomicAdd(a.fy + i, fi1);
-      atomicAdd(a.fz + i, fi2);
+    if (tid == 0) {
+      atomicAdd(a.fx + i, misc[0]);
+      atomicAdd(a.fy + i, misc[1]);
+      atomicAdd(a.fz + i, misc[2]);
     }
     __syncthreads();
   }
@@ -577,6 +665,29 @@ int snap_build(const xnb_snap_params& p, int device, SnapArgs& t, std::vector<vo
             ecoef.push_back(j >= j1 ? bindex(j1, j2, j) : -1);
             ew.push_back((2 * mb == j && ma == mb) ? 1.0 : 2.0);
           }
+  // order the Z elements by their work (na x nb terms), largest first: the
+  // threads of a warp then run loops of similar length
+  {
+    std::vector<int> perm(zs.size());
+    for (size_t e = 0; e < perm.size(); ++e) perm[e] = static_cast<int>(e);
+    std::stable_sort(perm.begin(), perm.end(),
+                     [&](int x, int y) { return zs[x].na * zs[x].nb > zs[y].na * zs[y].nb; });
+    std::vector<SnapZ> zs2(zs.size());
+    std::vector<double> mult2(zs.size()), ew2(zs.size());
+    std::vector<int> kb2(zs.size()), ec2(zs.size());
+    for (size_t e = 0; e < perm.size(); ++e) {
+      zs2[e] = zs[perm[e]];
+      mult2[e] = mult[perm[e]];
+      kb2[e] = kb[perm[e]];
+      ec2[e] = ecoef[perm[e]];
+      ew2[e] = ew[perm[e]];
+    }
+    zs.swap(zs2);
+    mult.swap(mult2);
+    kb.swap(kb2);
+    ecoef.swap(ec2);
+    ew.swap(ew2);
+  }
   t.nz = static_cast<int>(zs.size());
   std::vector<double> zbeta(static_cast<size_t>(p.ntypes) * t.nz), zener(zbeta.size());
   for (int ty = 0; ty < p.ntypes; ++ty) {
@@ -614,10 +725,18 @@ int snap_build(const xnb_snap_params& p, int device, SnapArgs& t, std::vector<vo
     err = "device memory for the SNAP tables";
     return XNB_ERR_NOMEM;
   }
+  // shared memory: fixed part plus, per neighbour of a round, its forward U
+  // (unique half of every level) and two adjoint levels; the round size is the
+  // largest that keeps a CTA within ~100 KB (two CTAs per SM)
   const int lvl_max = nunique(J);
-  const size_t doubles = 3 * kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8 + 2 * t.nu_full + 2 * t.nu_unique +
-                         kSnapWarps * 2 * t.nu_unique + kSnapWarps * 2 * lvl_max * 8 + 8 + 4;
-  t.smem_bytes = doubles * sizeof(double);
+  const size_t fixed = 4 * kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8 + 2 * t.nu_full + 4 * t.nu_unique +
+                       kSnapThreads * 5 + 12;
+  const size_t per = 2 * t.nu_unique + 4 * lvl_max;
+  const size_t budget = 100 * 1024 / sizeof(double);
+  long long grp = budget > fixed ? static_cast<long long>((budget - fixed) / per) : 1;
+  grp = std::max(1LL, std::min<long long>(grp, kSnapMaxGroup));
+  t.group = static_cast<int>(grp);
+  t.smem_bytes = (fixed + per * t.group) * sizeof(double);
   return XNB_OK;
 }
 
@@ -632,11 +751,11 @@ int launch_snap(const Extent& ex, const SysDesc* sys, const SysState* st, const 
   }
   cudaFuncSetAttribute(k_snap, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(t.smem_bytes));
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_snap, kSnapWarps * 32, t.smem_bytes);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_snap, kSnapThreads, t.smem_bytes);
   long long g = static_cast<long long>(ex.sm_count) * std::max(1, per_sm) * 4;
   if (g > static_cast<long long>(ex.n_part)) g = ex.n_part;
-  k_snap<<<static_cast<int>(std::max(1LL, g)), kSnapWarps * 32, t.smem_bytes, stream>>>(ex.n_part, sys, st, a, t,
-                                                                                      sys_only, with_pe, flags);
+  k_snap<<<static_cast<int>(std::max(1LL, g)), kSnapThreads, t.smem_bytes, stream>>>(ex.n_part, sys, st, a, t,
+                                                                                   sys_only, with_pe, flags);
   return launches + 1;
 }
 

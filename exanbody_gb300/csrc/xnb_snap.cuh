@@ -15,6 +15,8 @@ constexpr int kSnapMaxTwoJ = 10;
 constexpr int kSnapMaxTypes = 16;
 constexpr int kSnapMaxNbr = 128;  // environment size per atom
 constexpr int kSnapWarps = 4;     // warps per atom (one CTA)
+constexpr int kSnapThreads = kSnapWarps * 32;
+constexpr int kSnapMaxGroup = 32; // neighbours whose U levels are held at once
 
 // One element Z^j_{j1 j2}[mb][ma] on the unique half of U^j (rows 2 mb < j, and
 // the first j/2 + 1 elements of an even j's middle row), with the index ranges
@@ -30,6 +32,7 @@ struct SnapZ {
 
 struct SnapArgs {
   int twojmax, nz, nu_unique, nu_full, ntypes, switchflag;
+  int group;                   // neighbours per round (shared-memory budget)
   int ublk[kSnapMaxTwoJ + 2];  // first unique-layout index of level j
   int fblk[kSnapMaxTwoJ + 2];  // first full-layout index of level j
   double rcutfac, rfac0, rmin0;

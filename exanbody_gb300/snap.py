@@ -103,3 +103,30 @@ class Potential:
     @property
     def cutoff(self):
         return 2.0 * max(e["radelem"] for e in self.cfg["elements"]) * float(self.cfg["rcutfac"])
+
+
+def md_steps(batch, s, pot, nsteps, energy=False):
+    """Velocity-Verlet steps of system s with snap_force_generic as the force
+    chain (numerical-scheme.msp:13-25 with update-particles.msp): push_f_v_r,
+    push_f_v, particle_displ_over and, when triggered, move_particles +
+    chunk_neighbors, then the SNAP forces and push_f_v."""
+    for _ in range(nsteps):
+        batch.push_f_v_r(1.0, s)
+        batch.push_f_v(0.5, s)
+        if batch.particle_displ_over(s) > 0:
+            batch.update_particles_full(s)
+        pot.force(batch, s, energy=energy)
+        batch.push_f_v(0.5, s)
+
+
+def lattice(structure, n, a, sigma, seed):
+    """Sites of an n^3 block of unit cells (SC, BCC or FCC basis of the
+    reference's lattice generator, lattice_generator.h:140-170) with Gaussian
+    noise of sigma (seeded), wrapped into the [0, n a) box."""
+    basis = {"SC": np.array([[0.5, 0.5, 0.5]]), "BCC": np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.5]]),
+             "FCC": np.array([[0.0, 0.0, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0]])}[structure]
+    k, j, i = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    cells = np.stack([i.ravel(), j.ravel(), k.ravel()], axis=1).astype(np.float64)
+    r = (cells[:, None, :] + basis[None]).reshape(-1, 3) * a
+    r += np.random.default_rng(seed).normal(0.0, sigma, r.shape)
+    return r % (n * a)
