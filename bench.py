@@ -546,27 +546,48 @@ def run_snap(args):
     pot.force(b, s)
     snap.md_steps(b, s, pot, max(3, args.warmup))
     steps = args.steps
-    reb0 = b.info(s).rebuilds
-    l0 = b.kernel_launches()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with Clocks(local) as ck:
+
+    def timed_steps(mixed):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record()
-        snap.md_steps(b, s, pot, steps)
+        snap.md_steps(b, s, pot, steps, mixed=mixed)
         e1.record()
         e1.synchronize()
-    ms = e0.elapsed_time(e1)
+        return e0.elapsed_time(e1)
+
+    def timed_force(mixed, reps=5):
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        f0.record()
+        for _ in range(reps):
+            pot.force(b, s, mixed=mixed)
+        f1.record()
+        f1.synchronize()
+        return f0.elapsed_time(f1) / reps
+
+    # headline: the mixed path (FP32 U/Z/Y/adjoint arithmetic, FP64 geometry and sums)
+    snap.md_steps(b, s, pot, 2, mixed=True)
+    reb0 = b.info(s).rebuilds
+    l0 = b.kernel_launches()
+    with Clocks(local) as ck:
+        ms = timed_steps(True)
     launches = b.kernel_launches() - l0
     rebuilds = b.info(s).rebuilds - reb0
-    # the force kernel alone
-    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    f0.record()
-    for _ in range(5):
-        pot.force(b, s)
-    f1.record()
-    f1.synchronize()
-    ms_force = f0.elapsed_time(f1) / 5
+    ms64 = timed_steps(False)
+    ms_force = timed_force(True)
+    ms_force64 = timed_force(False)
+    # force error of the mixed path against FP64 on one state
+    pot.force(b, s)
+    P = b.download(s)
+    f64 = np.stack([P["fx"], P["fy"], P["fz"]], 1)
+    pot.force(b, s, mixed=True)
+    P = b.download(s)
+    fmx = np.stack([P["fx"], P["fy"], P["fz"]], 1)
+    mag = np.linalg.norm(f64, axis=1)
+    frms = float(np.sqrt((mag ** 2).mean()))
+    rel = np.linalg.norm(fmx - f64, axis=1) / np.maximum(mag, frms)
+    err_max, err_rms = float(rel.max()), float(np.sqrt((rel ** 2).mean()))
     # neighbours inside the SNAP cutoff (for the operation count)
     P = b.download(s)
     try:
@@ -579,7 +600,7 @@ def run_snap(args):
         nn = 18.0 if d["structure"] == "FCC" else 14.0
     flop = snap_flop64_per_atom(cfg, nn)
     peak64 = fp64_peak_tflops(torch, dev)
-    achieved = flop * N / (ms_force * 1e-3) / 1e12
+    achieved = flop * N / (ms_force64 * 1e-3) / 1e12
     b.check_errors()
     b.close()
     e2e = None
@@ -588,8 +609,8 @@ def run_snap(args):
         bb = xnb.Batch(N + 64, geom["dims"][0] ** 3 + 64, N * 200 + 4096, max_systems=1, device=local)
         ss = bb.add_system(params, r, v0, ids)
         bb.init_particles(ss, xnb.PREC_FP64)
-        pot.force(bb, ss)
-        snap.md_steps(bb, ss, pot, steps)
+        pot.force(bb, ss, mixed=True)
+        snap.md_steps(bb, ss, pot, steps, mixed=True)
         out = bb.download(ss)
         dt = time.perf_counter() - t0
         bb.close()
@@ -617,15 +638,20 @@ def run_snap(args):
                "sample": "%d SNAP MD steps of the same system, oracle OpenMP build" % sample}
     if rank == 0:
         print(json.dumps({
-            "metric": metric, "value": world * N * steps / (ms * 1e-3), "unit": "atom-steps/s", "n_gpus": world,
+            "metric": metric.replace("FP64)", "mixed precision; FP64 beside it)"),
+            "value": world * N * steps / (ms * 1e-3), "unit": "atom-steps/s", "n_gpus": world,
             "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(conf, rebuilds_in_timed_steps=rebuilds, neighbours_in_cutoff=nn),
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+            "config": dict(conf, rebuilds_in_timed_steps=rebuilds, neighbours_in_cutoff=nn, precision="mixed"),
+            "fp64": {"value": N * steps / (ms64 * 1e-3), "unit": "atom-steps/s", "ms_per_step": ms64 / steps,
+                     "speedup_mixed_vs_fp64": ms64 / ms},
+            "force_error_mixed_vs_fp64": {"max": err_max, "rms": err_rms, "tolerance": 1e-5},
             "clocks": ck.summary(), "e2e": e2e, "gpu_launches": launches,
-            "roofline": {"bound": "fp64", "kernel": "k_snap", "achieved": achieved, "peak": peak64,
-                         "unit": "TFLOP/s", "frac": achieved / peak64,
+            "roofline": {"bound": "fp64", "kernel": "k_snap<double> (the FP64 path)", "achieved": achieved,
+                         "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
                          "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
-                         "flop_per_atom": flop, "ms_per_launch": ms_force, "traffic": None},
+                         "flop_per_atom": flop, "ms_per_launch": ms_force64, "ms_per_launch_mixed": ms_force,
+                         "traffic": None},
             "cpu_baseline": cpu}), flush=True)
     return 0
 

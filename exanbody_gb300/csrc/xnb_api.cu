@@ -1333,7 +1333,7 @@ int xnb_snap_force(xnb_batch* b, int32_t s, const xnb_snap* snap, int32_t flags,
   if (rc) return rc;
   if (!snap) return fail(XNB_ERR_ARG, "xnb_snap_force: no potential");
   if (snap->device != b->device) return fail(XNB_ERR_ARG, "xnb_snap_force: potential built on another device");
-  if (flags & ~(XNB_FORCE_ENERGY | XNB_FORCE_ACCUMULATE)) return fail(XNB_ERR_ARG, "bad flags");
+  if (flags & ~(XNB_FORCE_ENERGY | XNB_FORCE_ACCUMULATE | XNB_FORCE_MIXED)) return fail(XNB_ERR_ARG, "bad flags");
   double rad_max = 0.0;
   for (int k = 0; k < snap->t.ntypes; ++k) rad_max = std::max(rad_max, snap->t.radelem[k]);
   const double cut_max = 2.0 * rad_max * snap->t.rcutfac;
@@ -1348,7 +1348,7 @@ int xnb_snap_force(xnb_batch* b, int32_t s, const xnb_snap* snap, int32_t flags,
   XCK(cudaMemsetAsync(b->d_flag, 0, sizeof(unsigned int), st));
   const Extent ex = b->extent();
   b->launches += launch_snap(ex, b->d_sys, b->d_st, b->a, snap->t, s, (flags & XNB_FORCE_ENERGY) != 0,
-                             (flags & XNB_FORCE_ACCUMULATE) != 0, b->d_flag, st);
+                             (flags & XNB_FORCE_ACCUMULATE) != 0, (flags & XNB_FORCE_MIXED) != 0, b->d_flag, st);
   unsigned int flag = 0;
   XCK(cudaMemcpyAsync(&flag, b->d_flag, sizeof(flag), cudaMemcpyDeviceToHost, st));
   XCK(cudaStreamSynchronize(st));

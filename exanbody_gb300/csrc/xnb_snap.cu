@@ -38,22 +38,45 @@ constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 
 __host__ __device__ inline int nunique(int j) { return (j & 1) ? ((j + 1) / 2) * (j + 1) : (j / 2) * (j + 1) + j / 2 + 1; }
 
-struct C2 {
-  double r, i;
+template <class R>
+struct CX {
+  R r, i;
 };
-__device__ __forceinline__ C2 cmulc(C2 a, C2 b) {  // conj(a) * b
-  return C2{fma(a.r, b.r, a.i * b.i), fma(a.r, b.i, -(a.i * b.r))};
+using C2 = CX<double>;
+template <class R>
+__device__ __forceinline__ CX<R> cmulc(CX<R> a, CX<R> b) {  // conj(a) * b
+  return CX<R>{fma(a.r, b.r, a.i * b.i), fma(a.r, b.i, -(a.i * b.r))};
 }
-__device__ __forceinline__ C2 cmul(C2 a, C2 b) { return C2{fma(a.r, b.r, -(a.i * b.i)), fma(a.r, b.i, a.i * b.r)}; }
+template <class R>
+__device__ __forceinline__ CX<R> cmul(CX<R> a, CX<R> b) {
+  return CX<R>{fma(a.r, b.r, -(a.i * b.i)), fma(a.r, b.i, a.i * b.r)};
+}
 
-// element (r, c) of level L from its unique-half buffer (stride `st` doubles
+// element (r, c) of level L from its unique-half buffer (stride `st` values
 // per element, complex at offset `off`)
-__device__ __forceinline__ C2 level_get(const double* buf, int st, int off, int L, int r, int c) {
+template <class R>
+__device__ __forceinline__ CX<R> level_get(const R* buf, int st, int off, int L, int r, int c) {
   const int idx = r * (L + 1) + c;
-  if (idx < nunique(L)) return C2{buf[idx * st + off], buf[idx * st + off + 1]};
+  if (idx < nunique(L)) return CX<R>{buf[idx * st + off], buf[idx * st + off + 1]};
   const int k = (L - r) * (L + 1) + (L - c);
-  const double s = ((r + c) & 1) ? -1.0 : 1.0;
-  return C2{s * buf[k * st + off], -s * buf[k * st + off + 1]};
+  const R s = ((r + c) & 1) ? R(-1) : R(1);
+  return CX<R>{s * buf[k * st + off], -s * buf[k * st + off + 1]};
+}
+
+// the potential's tables in the compute type
+template <class R>
+struct Tabs {
+  const R *rootpq, *cg, *zbeta, *zener;
+};
+template <class R>
+__device__ __forceinline__ Tabs<R> tabs(const SnapArgs& t);
+template <>
+__device__ __forceinline__ Tabs<double> tabs<double>(const SnapArgs& t) {
+  return Tabs<double>{t.rootpq, t.cg, t.zbeta, t.zener};
+}
+template <>
+__device__ __forceinline__ Tabs<float> tabs<float>(const SnapArgs& t) {
+  return Tabs<float>{t.rootpq_f, t.cg_f, t.zbeta_f, t.zener_f};
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -131,28 +154,29 @@ __device__ __forceinline__ bool uq(int j, int r, int c) {
 // Forward U levels 1..J of one neighbour into its unique-half buffer u (level j
 // at ublk[j]); level 0 is set by the caller. Threads slot, slot + lpn, ... of the
 // neighbour take the elements of each level; the CTA synchronises between levels.
-__device__ __forceinline__ void forward_levels(double* u, bool active, int slot, int lpn, C2 a, C2 b,
-                                               const SnapArgs& t) {
+template <class R>
+__device__ __forceinline__ void forward_levels(R* u, bool active, int slot, int lpn, CX<R> a, CX<R> b,
+                                               const SnapArgs& t, const R* rootpq) {
   const int J = t.twojmax;
   for (int j = 1; j <= J; ++j) {
     if (active) {
       const int nuj = nunique(j);
-      const double* prev = u + 2 * t.ublk[j - 1];
-      double* cur = u + 2 * t.ublk[j];
+      const R* prev = u + 2 * t.ublk[j - 1];
+      R* cur = u + 2 * t.ublk[j];
       for (int e = slot; e < nuj; e += lpn) {
         const int mb = e / (j + 1), ma = e % (j + 1);
-        C2 v{0.0, 0.0};
+        CX<R> v{R(0), R(0)};
         if (ma < j) {
-          const C2 p = level_get(prev, 2, 0, j - 1, mb, ma);
-          const double rp = t.rootpq[(j - ma) * (J + 1) + (j - mb)];
-          const C2 q = cmulc(a, p);
+          const CX<R> p = level_get(prev, 2, 0, j - 1, mb, ma);
+          const R rp = rootpq[(j - ma) * (J + 1) + (j - mb)];
+          const CX<R> q = cmulc(a, p);
           v.r = rp * q.r;
           v.i = rp * q.i;
         }
         if (ma > 0) {
-          const C2 p = level_get(prev, 2, 0, j - 1, mb, ma - 1);
-          const double rp = t.rootpq[ma * (J + 1) + (j - mb)];
-          const C2 q = cmulc(b, p);
+          const CX<R> p = level_get(prev, 2, 0, j - 1, mb, ma - 1);
+          const R rp = rootpq[ma * (J + 1) + (j - mb)];
+          const CX<R> q = cmulc(b, p);
           v.r = fma(-rp, q.r, v.r);
           v.i = fma(-rp, q.i, v.i);
         }
@@ -164,29 +188,33 @@ __device__ __forceinline__ void forward_levels(double* u, bool active, int slot,
   }
 }
 
+// R: the type of the U, Z, Y and adjoint arithmetic (double, or float for the
+// mixed path); geometry, switching and the force sums stay in double.
+template <class R>
 __global__ void __launch_bounds__(kSnapThreads)
     k_snap(uint32_t n_part, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a,
-           SnapArgs t, int sys_only, bool with_pe, unsigned int* flags) {
+           SnapArgs t, int group, int sys_only, bool with_pe, unsigned int* flags) {
   extern __shared__ double sm[];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int J = t.twojmax;
   const int lvl_max = nunique(J);
   const int nu = t.nu_unique;
-  // shared layout (doubles)
+  const Tabs<R> T = tabs<R>(t);
+  // shared layout: double part, then the compute-type part
   double* nx = sm;
   double* ny = nx + kSnapMaxNbr;
   double* nz = ny + kSnapMaxNbr;
   double* nsw = nz + kSnapMaxNbr;                                          // wj sfac per neighbour
   uint32_t* nj = reinterpret_cast<uint32_t*>(nsw + kSnapMaxNbr);           // kSnapMaxNbr u32
   uint8_t* nt = reinterpret_cast<uint8_t*>(nj + kSnapMaxNbr);              // kSnapMaxNbr u8
-  double* utot = nsw + kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8;    // 2 nu_full
-  double* yv = utot + 2 * t.nu_full;                                        // 2 nu
-  double* uacc = yv + 2 * nu;                                               // 2 nu
-  double* red = uacc + 2 * nu;                                              // kSnapThreads x 5
+  double* red = nsw + kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8;     // kSnapThreads x 5
   double* misc = red + kSnapThreads * 5;                                    // 8 doubles: fsum[3], wsum[4]
   int* icnt = reinterpret_cast<int*>(misc + 8);                             // 8 ints
-  double* uall = misc + 12;                                                 // group x 2 nu
-  double* adj = uall + static_cast<size_t>(t.group) * 2 * nu;               // group x 2 x 2 lvl_max
+  R* utot = reinterpret_cast<R*>(misc + 12);                               // 2 nu_full
+  R* yv = utot + 2 * t.nu_full;                                             // 2 nu
+  R* uacc = yv + 2 * nu;                                                    // 2 nu
+  R* uall = uacc + 2 * nu;                                                  // group x 2 nu
+  R* adj = uall + static_cast<size_t>(group) * 2 * nu;                      // group x 2 x 2 lvl_max
 
   for (uint32_t i = blockIdx.x; i < n_part; i += gridDim.x) {
     const uint32_t c = a.pcell[i];
@@ -265,32 +293,32 @@ __global__ void __launch_bounds__(kSnapThreads)
     }
 
     // ---- U_tot = self + sum_j wj sfac U_j, neighbours in rounds of `group` ----
-    for (int e = tid; e < 2 * nu; e += kSnapThreads) uacc[e] = 0.0;
-    for (int q0 = 0; q0 < nn; q0 += t.group) {
-      const int gr = min(t.group, nn - q0);
+    for (int e = tid; e < 2 * nu; e += kSnapThreads) uacc[e] = R(0);
+    for (int q0 = 0; q0 < nn; q0 += group) {
+      const int gr = min(group, nn - q0);
       const int lpn = kSnapThreads / gr;
       const int g = tid / lpn, slot = tid % lpn;
       const bool active = g < gr;
-      double* ug = uall + static_cast<size_t>(active ? g : 0) * 2 * nu;
-      C2 ca{0.0, 0.0}, cb{0.0, 0.0};
+      R* ug = uall + static_cast<size_t>(active ? g : 0) * 2 * nu;
+      CX<R> ca{R(0), R(0)}, cb{R(0), R(0)};
       if (active) {
         const int q = q0 + g;
         const double rcut = (radi + t.radelem[nt[q]]) * t.rcutfac;
         const Geo geo = geometry(nx[q], ny[q], nz[q], rcut, t, false);
-        ca = geo.a;
-        cb = geo.b;
+        ca = CX<R>{R(geo.a.r), R(geo.a.i)};
+        cb = CX<R>{R(geo.b.r), R(geo.b.i)};
         if (slot == 0) {
           nsw[q] = t.wj[nt[q]] * geo.sfac;
-          ug[0] = 1.0;
-          ug[1] = 0.0;
+          ug[0] = R(1);
+          ug[1] = R(0);
         }
       }
       __syncthreads();
-      forward_levels(ug, active, slot, lpn, ca, cb, t);
+      forward_levels(ug, active, slot, lpn, ca, cb, t, T.rootpq);
       for (int e = tid; e < nu; e += kSnapThreads) {
-        double re = 0.0, im = 0.0;
+        R re = R(0), im = R(0);
         for (int q = 0; q < gr; ++q) {
-          const double sw = nsw[q0 + q];
+          const R sw = R(nsw[q0 + q]);
           re = fma(sw, uall[static_cast<size_t>(q) * 2 * nu + 2 * e], re);
           im = fma(sw, uall[static_cast<size_t>(q) * 2 * nu + 2 * e + 1], im);
         }
@@ -305,39 +333,39 @@ __global__ void __launch_bounds__(kSnapThreads)
       while (j < J && e >= t.ublk[j + 1]) ++j;
       const int le = e - t.ublk[j];
       const int mb = le / (j + 1), ma = le % (j + 1);
-      const double re = uacc[2 * e] + ((mb == ma) ? 1.0 : 0.0), im = uacc[2 * e + 1];
+      const R re = uacc[2 * e] + ((mb == ma) ? R(1) : R(0)), im = uacc[2 * e + 1];
       const int f = t.fblk[j] + mb * (j + 1) + ma;
       utot[2 * f] = re;
       utot[2 * f + 1] = im;
       if (!(2 * mb == j && ma == mb)) {
         const int g2 = t.fblk[j] + (j - mb) * (j + 1) + (j - ma);
-        const double sg = ((ma + mb) & 1) ? -1.0 : 1.0;
+        const R sg = ((ma + mb) & 1) ? R(-1) : R(1);
         utot[2 * g2] = sg * re;
         utot[2 * g2 + 1] = -sg * im;
       }
-      yv[2 * e] = 0.0;
-      yv[2 * e + 1] = 0.0;
+      yv[2 * e] = R(0);
+      yv[2 * e + 1] = R(0);
     }
     __syncthreads();
     // ---- Y = sum beta_j Z, and the energy ----
     double eloc = 0.0;
-    const double* zb = t.zbeta + static_cast<size_t>(ti) * t.nz;
-    const double* ze = t.zener + static_cast<size_t>(ti) * t.nz;
+    const R* zb = T.zbeta + static_cast<size_t>(ti) * t.nz;
+    const R* ze = T.zener + static_cast<size_t>(ti) * t.nz;
     for (int e = tid; e < t.nz; e += kSnapThreads) {
       const SnapZ z = t.z[e];
-      const double* cgb = t.cg + z.cg;
+      const R* cgb = T.cg + z.cg;
       const int j1 = z.j1, j2 = z.j2;
       int jju1 = t.fblk[j1] + (j1 + 1) * z.mb1min;
       int jju2 = t.fblk[j2] + (j2 + 1) * z.mb2max;
       int icgb = z.mb1min * (j2 + 1) + z.mb2max;
-      C2 zt{0.0, 0.0};
+      CX<R> zt{R(0), R(0)};
       for (int ib = 0; ib < z.nb; ++ib) {
-        C2 sa{0.0, 0.0};
+        CX<R> sa{R(0), R(0)};
         int ma1 = z.ma1min, ma2 = z.ma2max;
         int icga = z.ma1min * (j2 + 1) + z.ma2max;
         for (int ia = 0; ia < z.na; ++ia) {
-          const C2 p = cmul(C2{utot[2 * (jju1 + ma1)], utot[2 * (jju1 + ma1) + 1]},
-                            C2{utot[2 * (jju2 + ma2)], utot[2 * (jju2 + ma2) + 1]});
+          const CX<R> p = cmul(CX<R>{utot[2 * (jju1 + ma1)], utot[2 * (jju1 + ma1) + 1]},
+                               CX<R>{utot[2 * (jju2 + ma2)], utot[2 * (jju2 + ma2) + 1]});
           sa.r = fma(cgb[icga], p.r, sa.r);
           sa.i = fma(cgb[icga], p.i, sa.i);
           ++ma1;
@@ -352,9 +380,9 @@ __global__ void __launch_bounds__(kSnapThreads)
       }
       atomicAdd(&yv[2 * z.y], zb[e] * zt.r);
       atomicAdd(&yv[2 * z.y + 1], zb[e] * zt.i);
-      if (with_pe && ze[e] != 0.0) {
-        const C2 u{utot[2 * z.uf], utot[2 * z.uf + 1]};
-        eloc += ze[e] * cmulc(u, zt).r;
+      if (with_pe && ze[e] != R(0)) {
+        const CX<R> u{utot[2 * z.uf], utot[2 * z.uf + 1]};
+        eloc += static_cast<double>(ze[e] * cmulc(u, zt).r);
       }
     }
     if (with_pe) {
@@ -370,107 +398,107 @@ __global__ void __launch_bounds__(kSnapThreads)
 
     // ---- forces by reverse mode: F = sum_e w Re(conj(U_e) Y_e) per neighbour,
     //      dF/da and dF/db from the adjoint w Y propagated down the levels ----
-    for (int q0 = 0; q0 < nn; q0 += t.group) {
-      const int gr = min(t.group, nn - q0);
+    for (int q0 = 0; q0 < nn; q0 += group) {
+      const int gr = min(group, nn - q0);
       const int lpn = kSnapThreads / gr;
       const int g = tid / lpn, slot = tid % lpn;
       const bool active = g < gr;
-      double* ug = uall + static_cast<size_t>(active ? g : 0) * 2 * nu;
-      double* adj0 = adj + static_cast<size_t>(active ? g : 0) * 4 * lvl_max;
-      double* adj1 = adj0 + 2 * lvl_max;
-      C2 ca{0.0, 0.0}, cb{0.0, 0.0};
+      R* ug = uall + static_cast<size_t>(active ? g : 0) * 2 * nu;
+      R* adj0 = adj + static_cast<size_t>(active ? g : 0) * 4 * lvl_max;
+      R* adj1 = adj0 + 2 * lvl_max;
+      CX<R> ca{R(0), R(0)}, cb{R(0), R(0)};
       if (active) {
         const int q = q0 + g;
         const double rcut = (radi + t.radelem[nt[q]]) * t.rcutfac;
         const Geo geo = geometry(nx[q], ny[q], nz[q], rcut, t, false);
-        ca = geo.a;
-        cb = geo.b;
-        if (nn > t.group && slot == 0) {  // U of this round's neighbours was overwritten
-          ug[0] = 1.0;
-          ug[1] = 0.0;
+        ca = CX<R>{R(geo.a.r), R(geo.a.i)};
+        cb = CX<R>{R(geo.b.r), R(geo.b.i)};
+        if (nn > group && slot == 0) {  // U of this round's neighbours was overwritten
+          ug[0] = R(1);
+          ug[1] = R(0);
         }
       }
-      if (nn > t.group) {
+      if (nn > group) {
         __syncthreads();
-        forward_levels(ug, active, slot, lpn, ca, cb, t);
+        forward_levels(ug, active, slot, lpn, ca, cb, t, T.rootpq);
       }
-      double F = 0.0, gar = 0.0, gai = 0.0, gbr = 0.0, gbi = 0.0;
+      R F = R(0), gar = R(0), gai = R(0), gbr = R(0), gbi = R(0);
       // seed the top level
       if (active) {
         const int nuJ = nunique(J);
         for (int e = slot; e < nuJ; e += lpn) {
-          const double wgt = ((J & 1) == 0 && e == nuJ - 1) ? 0.5 : 1.0;
+          const R wgt = ((J & 1) == 0 && e == nuJ - 1) ? R(0.5) : R(1);
           adj0[2 * e] = wgt * yv[2 * (t.ublk[J] + e)];
           adj0[2 * e + 1] = wgt * yv[2 * (t.ublk[J] + e) + 1];
         }
       }
       __syncthreads();
-      double* A = adj0;
-      double* Nx = adj1;
+      R* A = adj0;
+      R* Nx = adj1;
       for (int j = J; j >= 1; --j) {
         const int Lv = j - 1;
         if (active) {
           const int nuj = nunique(j);
-          const double* uj = ug + 2 * t.ublk[j];
-          const double* ul = ug + 2 * t.ublk[Lv];
-          const double* yj = yv + 2 * t.ublk[j];
+          const R* uj = ug + 2 * t.ublk[j];
+          const R* ul = ug + 2 * t.ublk[Lv];
+          const R* yj = yv + 2 * t.ublk[j];
           for (int e = slot; e < nuj; e += lpn) {
             const int mb = e / (j + 1), ma = e % (j + 1);
-            const double wgt = ((j & 1) == 0 && e == nuj - 1) ? 0.5 : 1.0;
+            const R wgt = ((j & 1) == 0 && e == nuj - 1) ? R(0.5) : R(1);
             F = fma(wgt, fma(uj[2 * e], yj[2 * e], uj[2 * e + 1] * yj[2 * e + 1]), F);
-            const double Gr = A[2 * e], Gi = A[2 * e + 1];
+            const R Gr = A[2 * e], Gi = A[2 * e + 1];
             if (ma < j) {
-              const C2 p = level_get(ul, 2, 0, Lv, mb, ma);
-              const double rp = t.rootpq[(j - ma) * (J + 1) + (j - mb)];
+              const CX<R> p = level_get(ul, 2, 0, Lv, mb, ma);
+              const R rp = T.rootpq[(j - ma) * (J + 1) + (j - mb)];
               gar = fma(rp, fma(Gr, p.r, Gi * p.i), gar);
               gai = fma(rp, fma(Gr, p.i, -(Gi * p.r)), gai);
             }
             if (ma > 0) {
-              const C2 p = level_get(ul, 2, 0, Lv, mb, ma - 1);
-              const double rp = t.rootpq[ma * (J + 1) + (j - mb)];
+              const CX<R> p = level_get(ul, 2, 0, Lv, mb, ma - 1);
+              const R rp = T.rootpq[ma * (J + 1) + (j - mb)];
               gbr = fma(-rp, fma(Gr, p.r, Gi * p.i), gbr);
               gbi = fma(-rp, fma(Gr, p.i, -(Gi * p.r)), gbi);
             }
           }
           // adjoint of level j-1 by gathering its readers in level j
           const int nul = nunique(Lv);
-          const double* yl = yv + 2 * t.ublk[Lv];
+          const R* yl = yv + 2 * t.ublk[Lv];
           for (int u = slot; u < nul; u += lpn) {
             const int r = u / (Lv + 1), cc = u % (Lv + 1);
-            const double wgt = ((Lv & 1) == 0 && u == nul - 1) ? 0.5 : 1.0;
-            double accr = wgt * yl[2 * u], acci = wgt * yl[2 * u + 1];
+            const R wgt = ((Lv & 1) == 0 && u == nul - 1) ? R(0.5) : R(1);
+            R accr = wgt * yl[2 * u], acci = wgt * yl[2 * u + 1];
             if (uq(j, r, cc)) {
               const int k = r * (j + 1) + cc;
-              const double rp = t.rootpq[(j - cc) * (J + 1) + (j - r)];
-              const C2 m = cmul(ca, C2{A[2 * k], A[2 * k + 1]});
+              const R rp = T.rootpq[(j - cc) * (J + 1) + (j - r)];
+              const CX<R> m = cmul(ca, CX<R>{A[2 * k], A[2 * k + 1]});
               accr = fma(rp, m.r, accr);
               acci = fma(rp, m.i, acci);
             }
             if (cc + 1 <= j && uq(j, r, cc + 1)) {
               const int k = r * (j + 1) + cc + 1;
-              const double rp = t.rootpq[(cc + 1) * (J + 1) + (j - r)];
-              const C2 m = cmul(cb, C2{A[2 * k], A[2 * k + 1]});
+              const R rp = T.rootpq[(cc + 1) * (J + 1) + (j - r)];
+              const CX<R> m = cmul(cb, CX<R>{A[2 * k], A[2 * k + 1]});
               accr = fma(-rp, m.r, accr);
               acci = fma(-rp, m.i, acci);
             }
             const int r2 = Lv - r, c2 = Lv - cc;
             if (!(r2 == r && c2 == cc) && !uq(Lv, r2, c2)) {
-              double tr = 0.0, tim = 0.0;
+              R tr = R(0), tim = R(0);
               if (uq(j, r2, c2)) {
                 const int k = r2 * (j + 1) + c2;
-                const double rp = t.rootpq[(j - c2) * (J + 1) + (j - r2)];
-                const C2 m = cmul(ca, C2{A[2 * k], A[2 * k + 1]});
+                const R rp = T.rootpq[(j - c2) * (J + 1) + (j - r2)];
+                const CX<R> m = cmul(ca, CX<R>{A[2 * k], A[2 * k + 1]});
                 tr = rp * m.r;
                 tim = rp * m.i;
               }
               if (c2 + 1 <= j && uq(j, r2, c2 + 1)) {
                 const int k = r2 * (j + 1) + c2 + 1;
-                const double rp = t.rootpq[(c2 + 1) * (J + 1) + (j - r2)];
-                const C2 m = cmul(cb, C2{A[2 * k], A[2 * k + 1]});
+                const R rp = T.rootpq[(c2 + 1) * (J + 1) + (j - r2)];
+                const CX<R> m = cmul(cb, CX<R>{A[2 * k], A[2 * k + 1]});
                 tr = fma(-rp, m.r, tr);
                 tim = fma(-rp, m.i, tim);
               }
-              const double sg = ((r2 + c2) & 1) ? -1.0 : 1.0;
+              const R sg = ((r2 + c2) & 1) ? R(-1) : R(1);
               accr = fma(sg, tr, accr);
               acci = fma(-sg, tim, acci);
             }
@@ -479,16 +507,16 @@ __global__ void __launch_bounds__(kSnapThreads)
           }
         }
         __syncthreads();
-        double* tmp = A;
+        R* tmp = A;
         A = Nx;
         Nx = tmp;
       }
-      if (active && slot == 0) F += 0.5 * yv[0];  // level 0: U = 1, centre weight 1/2
-      red[tid * 5 + 0] = active ? F : 0.0;
-      red[tid * 5 + 1] = gar;
-      red[tid * 5 + 2] = gai;
-      red[tid * 5 + 3] = gbr;
-      red[tid * 5 + 4] = gbi;
+      if (active && slot == 0) F += R(0.5) * yv[0];  // level 0: U = 1, centre weight 1/2
+      red[tid * 5 + 0] = active ? static_cast<double>(F) : 0.0;
+      red[tid * 5 + 1] = static_cast<double>(gar);
+      red[tid * 5 + 2] = static_cast<double>(gai);
+      red[tid * 5 + 3] = static_cast<double>(gbr);
+      red[tid * 5 + 4] = static_cast<double>(gbi);
       __syncthreads();
       if (tid < gr) {
         const int q = q0 + tid;
@@ -717,31 +745,54 @@ int snap_build(const xnb_snap_params& p, int device, SnapArgs& t, std::vector<vo
     *dst = d;
     return true;
   };
+  auto f32 = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
+  const std::vector<float> rootpq_f = f32(rootpq), cg_f = f32(cg), zbeta_f = f32(zbeta), zener_f = f32(zener);
   if (!up(rootpq.data(), rootpq.size() * 8, reinterpret_cast<const void**>(&t.rootpq)) ||
       !up(cg.data(), cg.size() * 8, reinterpret_cast<const void**>(&t.cg)) ||
       !up(zs.data(), zs.size() * sizeof(SnapZ), reinterpret_cast<const void**>(&t.z)) ||
       !up(zbeta.data(), zbeta.size() * 8, reinterpret_cast<const void**>(&t.zbeta)) ||
-      !up(zener.data(), zener.size() * 8, reinterpret_cast<const void**>(&t.zener))) {
+      !up(zener.data(), zener.size() * 8, reinterpret_cast<const void**>(&t.zener)) ||
+      !up(rootpq_f.data(), rootpq_f.size() * 4, reinterpret_cast<const void**>(&t.rootpq_f)) ||
+      !up(cg_f.data(), cg_f.size() * 4, reinterpret_cast<const void**>(&t.cg_f)) ||
+      !up(zbeta_f.data(), zbeta_f.size() * 4, reinterpret_cast<const void**>(&t.zbeta_f)) ||
+      !up(zener_f.data(), zener_f.size() * 4, reinterpret_cast<const void**>(&t.zener_f))) {
     err = "device memory for the SNAP tables";
     return XNB_ERR_NOMEM;
   }
-  // shared memory: fixed part plus, per neighbour of a round, its forward U
+  // shared memory: a double part (environment, reductions) and a compute-type part:
+  // U_tot, Y, the U accumulator and, per neighbour of a round, its forward U
   // (unique half of every level) and two adjoint levels; the round size is the
-  // largest that keeps a CTA within ~100 KB (two CTAs per SM)
+  // largest that keeps a CTA within ~100 KB (two CTAs per SM), at most 32
   const int lvl_max = nunique(J);
-  const size_t fixed = 4 * kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8 + 2 * t.nu_full + 4 * t.nu_unique +
-                       kSnapThreads * 5 + 12;
+  const size_t fixed_d = 4 * kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8 + kSnapThreads * 5 + 12;
+  const size_t fixed_r = 2 * t.nu_full + 4 * t.nu_unique;
   const size_t per = 2 * t.nu_unique + 4 * lvl_max;
-  const size_t budget = 100 * 1024 / sizeof(double);
-  long long grp = budget > fixed ? static_cast<long long>((budget - fixed) / per) : 1;
-  grp = std::max(1LL, std::min<long long>(grp, kSnapMaxGroup));
-  t.group = static_cast<int>(grp);
-  t.smem_bytes = (fixed + per * t.group) * sizeof(double);
+  auto plan = [&](size_t rsize, int& group, size_t& bytes) {
+    const size_t budget = 100 * 1024, base = fixed_d * 8 + fixed_r * rsize;
+    long long grp = budget > base ? static_cast<long long>((budget - base) / (per * rsize)) : 1;
+    grp = std::max(1LL, std::min<long long>(grp, kSnapMaxGroup));
+    group = static_cast<int>(grp);
+    bytes = base + per * rsize * group;
+  };
+  plan(8, t.group, t.smem_bytes);
+  plan(4, t.group_f, t.smem_bytes_f);
   return XNB_OK;
 }
 
+template <class R>
+void snap_go(const Extent& ex, const SysDesc* sys, const SysState* st, const DevArrays& a, const SnapArgs& t,
+             int group, size_t smem, int sys_only, bool with_pe, unsigned int* flags, cudaStream_t stream) {
+  cudaFuncSetAttribute(k_snap<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_snap<R>, kSnapThreads, smem);
+  long long g = static_cast<long long>(ex.sm_count) * std::max(1, per_sm) * 4;
+  if (g > static_cast<long long>(ex.n_part)) g = ex.n_part;
+  k_snap<R><<<static_cast<int>(std::max(1LL, g)), kSnapThreads, smem, stream>>>(ex.n_part, sys, st, a, t, group,
+                                                                             sys_only, with_pe, flags);
+}
+
 int launch_snap(const Extent& ex, const SysDesc* sys, const SysState* st, const DevArrays& a, const SnapArgs& t,
-                int sys_only, bool with_pe, bool accumulate, unsigned int* flags, cudaStream_t stream) {
+                int sys_only, bool with_pe, bool accumulate, bool mixed, unsigned int* flags, cudaStream_t stream) {
   if (ex.n_part == 0) return 0;
   int launches = 0;
   if (!accumulate || with_pe) {
@@ -749,13 +800,8 @@ int launch_snap(const Extent& ex, const SysDesc* sys, const SysState* st, const 
     k_snap_zero<<<g, 256, 0, stream>>>(ex.n_part, sys, st, a, sys_only, !accumulate, with_pe);
     ++launches;
   }
-  cudaFuncSetAttribute(k_snap, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(t.smem_bytes));
-  int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_snap, kSnapThreads, t.smem_bytes);
-  long long g = static_cast<long long>(ex.sm_count) * std::max(1, per_sm) * 4;
-  if (g > static_cast<long long>(ex.n_part)) g = ex.n_part;
-  k_snap<<<static_cast<int>(std::max(1LL, g)), kSnapThreads, t.smem_bytes, stream>>>(ex.n_part, sys, st, a, t,
-                                                                                   sys_only, with_pe, flags);
+  if (mixed) snap_go<float>(ex, sys, st, a, t, t.group_f, t.smem_bytes_f, sys_only, with_pe, flags, stream);
+  else snap_go<double>(ex, sys, st, a, t, t.group, t.smem_bytes, sys_only, with_pe, flags, stream);
   return launches + 1;
 }
 

@@ -32,7 +32,7 @@ struct SnapZ {
 
 struct SnapArgs {
   int twojmax, nz, nu_unique, nu_full, ntypes, switchflag;
-  int group;                   // neighbours per round (shared-memory budget)
+  int group, group_f;          // neighbours per round (shared-memory budget), FP64 / FP32 kernels
   int ublk[kSnapMaxTwoJ + 2];  // first unique-layout index of level j
   int fblk[kSnapMaxTwoJ + 2];  // first full-layout index of level j
   double rcutfac, rfac0, rmin0;
@@ -44,7 +44,8 @@ struct SnapArgs {
   const SnapZ* z;              // nz
   const double* zbeta;         // [ntypes][nz] multiplier of Z into Y
   const double* zener;         // [ntypes][nz] 2 w beta_k of canonical entries, else 0
-  size_t smem_bytes;
+  const float *rootpq_f, *cg_f, *zbeta_f, *zener_f;  // the same tables in FP32 (mixed path)
+  size_t smem_bytes, smem_bytes_f;
 };
 
 // Host tables for one potential; device arrays are owned by `allocs`.
@@ -52,9 +53,11 @@ int snap_build(const xnb_snap_params& p, int device, SnapArgs& t, std::vector<vo
 
 // zero_particle_force (unless accumulate) + snap_force_generic (+ the division by
 // the system's mass when it divides) for the systems selected by sys_only.
+// mixed: FP32 arithmetic for U, Z, Y and the adjoint (geometry, switching and
+// the force sums in FP64).
 // flags receives bit 0 for a particle type without coefficients, bit 1 for an
 // environment larger than kSnapMaxNbr.
 int launch_snap(const Extent& ex, const SysDesc* sys, const SysState* st, const DevArrays& a, const SnapArgs& t,
-                int sys_only, bool with_pe, bool accumulate, unsigned int* flags, cudaStream_t stream);
+                int sys_only, bool with_pe, bool accumulate, bool mixed, unsigned int* flags, cudaStream_t stream);
 
 }  // namespace xnb

@@ -452,9 +452,9 @@ struct SnapOp : OperatorNode {
         throw Error(std::string("snap_force_generic: ") + xnb_last_error_string());
     }
     if (ctx.dry_run || !gpu_ready(ctx)) return;
-    ck(xnb_snap_force(ctx.batch, ctx.sys, ctx.snap, XNB_FORCE_ENERGY | (ctx.forces_written ? XNB_FORCE_ACCUMULATE : 0),
-                      nullptr),
-       "snap_force_generic");
+    const int32_t fl = XNB_FORCE_ENERGY | (ctx.forces_written ? XNB_FORCE_ACCUMULATE : 0) |
+                       (ctx.precision == XNB_PREC_MIXED ? XNB_FORCE_MIXED : 0);
+    ck(xnb_snap_force(ctx.batch, ctx.sys, ctx.snap, fl, nullptr), "snap_force_generic");
     ctx.forces_written = true;
   }
 };

@@ -96,8 +96,10 @@ class Potential:
         except Exception:
             pass
 
-    def force(self, batch, s=-1, energy=False, accumulate=False):
-        flags = (xnb.FORCE_ENERGY if energy else 0) | (xnb.FORCE_ACCUMULATE if accumulate else 0)
+    def force(self, batch, s=-1, energy=False, accumulate=False, mixed=False):
+        """mixed: FP32 arithmetic for U, Z, Y and the adjoint; FP64 geometry and sums."""
+        flags = ((xnb.FORCE_ENERGY if energy else 0) | (xnb.FORCE_ACCUMULATE if accumulate else 0)
+                 | (xnb.FORCE_MIXED if mixed else 0))
         xnb._ck(self.lib.xnb_snap_force(batch.h, int(s), self.h, flags, batch.stream))
 
     @property
@@ -105,7 +107,7 @@ class Potential:
         return 2.0 * max(e["radelem"] for e in self.cfg["elements"]) * float(self.cfg["rcutfac"])
 
 
-def md_steps(batch, s, pot, nsteps, energy=False):
+def md_steps(batch, s, pot, nsteps, energy=False, mixed=False):
     """Velocity-Verlet steps of system s with snap_force_generic as the force
     chain (numerical-scheme.msp:13-25 with update-particles.msp): push_f_v_r,
     push_f_v, particle_displ_over and, when triggered, move_particles +
@@ -115,7 +117,7 @@ def md_steps(batch, s, pot, nsteps, energy=False):
         batch.push_f_v(0.5, s)
         if batch.particle_displ_over(s) > 0:
             batch.update_particles_full(s)
-        pot.force(batch, s, energy=energy)
+        pot.force(batch, s, energy=energy, mixed=mixed)
         batch.push_f_v(0.5, s)
 
 

@@ -39,6 +39,7 @@ EXPORTED = [
 
 FORCE_ENERGY = 1
 FORCE_ACCUMULATE = 2
+FORCE_MIXED = 4
 
 STREAM_CHECKS = ("format", "order", "self", "range", "far", "missing")
 

@@ -250,6 +250,7 @@ int xnb_system_set_types(xnb_batch* b, int32_t sys, const uint64_t* ids, const u
  * (zero_particle_force). A particle type without a mass returns XNB_ERR_ARG. */
 #define XNB_FORCE_ENERGY 1
 #define XNB_FORCE_ACCUMULATE 2
+#define XNB_FORCE_MIXED 4 /* xnb_snap_force: FP32 arithmetic for U, Z, Y and the adjoint */
 int xnb_gravitational_force(xnb_batch* b, int32_t sys, double G, const double* type_mass, int32_t ntypes,
                             double rcut, int32_t precision, int32_t flags, void* stream);
 
@@ -338,7 +339,9 @@ int xnb_snap_create(const xnb_snap_params* p, int32_t device, xnb_snap** out);
 int xnb_snap_destroy(xnb_snap* s);
 /* zero_particle_force + snap_force_generic + update_force_from_ghost (+ the
  * division by mass of systems whose force chain ends with it) over the current
- * lists, FP64. The SNAP cutoff (rad_a + rad_b) rcutfac must not exceed the
+ * lists, FP64; with XNB_FORCE_MIXED the U, Z, Y and adjoint arithmetic runs in
+ * FP32 while displacements, the Cayley-Klein parameters, the switching
+ * function and every force sum stay in FP64 (about 1e-7 relative force error). The SNAP cutoff (rad_a + rad_b) rcutfac must not exceed the
  * lists' rcut + rcut_inc. flags: XNB_FORCE_ENERGY writes the per-particle SNAP
  * energy to pe; XNB_FORCE_ACCUMULATE adds onto the current forces. An
  * environment of more than 128 neighbours or a particle type without

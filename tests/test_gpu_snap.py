@@ -88,3 +88,62 @@ def test_golden_decks_through_the_operator_runner(tmp_path, el):
         if line.startswith("** "):
             vals[line.split()[1]] = float(line.split("=")[1].split("/")[0])
     assert vals["Position"] < 1e-9 and vals["Acceleration"] < 1e-6 and vals["Velocity"] < 1e-8, vals
+
+
+@pytest.mark.parametrize("el,n,a,dims", [("Ni", 8, 3.52, 4), ("Mo", 8, 3.15, 4)])
+def test_mixed_forces_within_1e5_of_fp64(el, n, a, dims):
+    """XNB_FORCE_MIXED (FP32 U, Z, Y, adjoint; FP64 geometry and sums): force
+    error |dF_i| / max(|F_i|, F_rms) <= 1e-5 (measured ~1e-6), energies to 1e-5."""
+    cfg = potential(el)
+    r, L = block(el, n, a, 9, sigma=0.15)
+    ids = np.arange(1, len(r) + 1, dtype=np.uint64)
+    geom = {"origin": (0.0, 0.0, 0.0), "extent": (L, L, L), "dims": (dims,) * 3, "cell_size": L / dims}
+    b = new_batch([len(r)], [ncells(geom)])
+    s = b.add_system(xnb.lj_params(geom, rcut=cfg["rcutfac"], rcut_inc=1.0), r, np.zeros_like(r), ids)
+    b.init_particles(s, xnb.PREC_FP64)
+    pot = snap.Potential(cfg)
+    pot.force(b, s, energy=True)
+    P64 = b.download(s)
+    pot.force(b, s, energy=True, mixed=True)
+    P32 = b.download(s)
+    F64 = np.stack([P64[k] for k in ("fx", "fy", "fz")], 1)
+    F32 = np.stack([P32[k] for k in ("fx", "fy", "fz")], 1)
+    mag = np.linalg.norm(F64, axis=1)
+    frms = np.sqrt((mag ** 2).mean())
+    rel = np.linalg.norm(F32 - F64, axis=1) / np.maximum(mag, frms)
+    assert rel.max() <= 1e-5, rel.max()
+    assert np.max(np.abs(P32["pe"] - P64["pe"])) <= 1e-5 * np.max(np.abs(P64["pe"]))
+
+
+def test_mixed_nve_drift_matches_fp64():
+    """200 NVE steps of the Mo deck's system from a thermal start: the total
+    energy of the mixed path drifts no more than the FP64 path's (plus 1e-7)."""
+    from exanbody_gb300 import units
+
+    cfg = potential("Mo")
+    r = snap.lattice("BCC", 10, 3.15, 0.05, 3)
+    L = 31.5
+    geom = {"origin": (0.0, 0.0, 0.0), "extent": (L, L, L), "dims": (4, 4, 4), "cell_size": L / 4}
+    mass = 95.96
+    # 300 K Maxwell-Boltzmann velocities (k_B in Da A^2 / ps^2 / K)
+    kb = units.ev_to_internal(8.617333262e-5)
+    v = np.random.default_rng(4).normal(0.0, np.sqrt(kb * 300.0 / mass), r.shape)
+    v -= v.mean(axis=0)
+    ids = np.arange(1, len(r) + 1, dtype=np.uint64)
+    drift = {}
+    for mixed in (False, True):
+        b = new_batch([len(r)], [ncells(geom)])
+        s = b.add_system(xnb.lj_params(geom, rcut=cfg["rcutfac"], rcut_inc=1.0, dt=1e-3, mass=mass,
+                                       divide_by_mass=True), r, v, ids)
+        b.init_particles(s, xnb.PREC_FP64)
+        pot = snap.Potential(cfg)
+        pot.force(b, s, energy=True, mixed=mixed)
+        e = []
+        for _ in range(20):
+            snap.md_steps(b, s, pot, 10, energy=True, mixed=mixed)
+            P = b.download(s)
+            ke = 0.5 * mass * float((P["vx"] ** 2 + P["vy"] ** 2 + P["vz"] ** 2).sum())
+            e.append(ke + float(P["pe"].sum()))
+        e = np.array(e)
+        drift[mixed] = float(np.max(np.abs(e - e[0])) / abs(e[0]))
+    assert drift[True] <= 2.0 * drift[False] + 1e-7, drift
