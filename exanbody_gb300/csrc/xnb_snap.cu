@@ -147,6 +147,25 @@ __global__ void k_snap_zero(uint32_t n_part, const SysDesc* __restrict__ sys, co
   if (zero_pe) a.pe[i] = 0.0;
 }
 
+// (row, column) of element `e` of a level with n = j + 1 columns, advanced by
+// `step` elements without integer division (its conversion sequence would run
+// on the FP64 pipe)
+__device__ __forceinline__ void rc_start(int e, int n, int& r, int& c) {
+  r = 0;
+  c = e;
+  while (c >= n) {
+    c -= n;
+    ++r;
+  }
+}
+__device__ __forceinline__ void rc_step(int step, int n, int& r, int& c) {
+  c += step;
+  while (c >= n) {
+    c -= n;
+    ++r;
+  }
+}
+
 __device__ __forceinline__ bool uq(int j, int r, int c) {
   return r >= 0 && c >= 0 && c <= j && r * (j + 1) + c < nunique(j);
 }
@@ -163,8 +182,9 @@ __device__ __forceinline__ void forward_levels(R* u, bool active, int slot, int 
       const int nuj = nunique(j);
       const R* prev = u + 2 * t.ublk[j - 1];
       R* cur = u + 2 * t.ublk[j];
-      for (int e = slot; e < nuj; e += lpn) {
-        const int mb = e / (j + 1), ma = e % (j + 1);
+      int mb, ma;
+      rc_start(slot, j + 1, mb, ma);
+      for (int e = slot; e < nuj; e += lpn, rc_step(lpn, j + 1, mb, ma)) {
         CX<R> v{R(0), R(0)};
         if (ma < j) {
           const CX<R> p = level_get(prev, 2, 0, j - 1, mb, ma);
@@ -204,13 +224,15 @@ __global__ void __launch_bounds__(kSnapThreads)
   double* nx = sm;
   double* ny = nx + kSnapMaxNbr;
   double* nz = ny + kSnapMaxNbr;
-  double* nsw = nz + kSnapMaxNbr;                                          // wj sfac per neighbour
-  uint32_t* nj = reinterpret_cast<uint32_t*>(nsw + kSnapMaxNbr);           // kSnapMaxNbr u32
+  double* nspare = nz + kSnapMaxNbr;                                       // (unused double slot)
+  uint32_t* nj = reinterpret_cast<uint32_t*>(nspare + kSnapMaxNbr);        // kSnapMaxNbr u32
   uint8_t* nt = reinterpret_cast<uint8_t*>(nj + kSnapMaxNbr);              // kSnapMaxNbr u8
-  double* red = nsw + kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8;     // kSnapThreads x 5
+  double* red = nspare + kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8;  // kSnapThreads x 5
   double* misc = red + kSnapThreads * 5;                                    // 8 doubles: fsum[3], wsum[4]
   int* icnt = reinterpret_cast<int*>(misc + 8);                             // 8 ints
-  R* utot = reinterpret_cast<R*>(misc + 12);                               // 2 nu_full
+  R* nab = reinterpret_cast<R*>(misc + 12);                                // 4 per neighbour: a, b
+  R* nsw = nab + 4 * kSnapMaxNbr;                                           // wj sfac per neighbour
+  R* utot = nsw + kSnapMaxNbr;                                              // 2 nu_full
   R* yv = utot + 2 * t.nu_full;                                             // 2 nu
   R* uacc = yv + 2 * nu;                                                    // 2 nu
   R* uall = uacc + 2 * nu;                                                  // group x 2 nu
@@ -300,25 +322,30 @@ __global__ void __launch_bounds__(kSnapThreads)
       const int g = tid / lpn, slot = tid % lpn;
       const bool active = g < gr;
       R* ug = uall + static_cast<size_t>(active ? g : 0) * 2 * nu;
-      CX<R> ca{R(0), R(0)}, cb{R(0), R(0)};
-      if (active) {
+      if (active && slot == 0) {  // the neighbour's Cayley-Klein parameters, once
         const int q = q0 + g;
         const double rcut = (radi + t.radelem[nt[q]]) * t.rcutfac;
         const Geo geo = geometry(nx[q], ny[q], nz[q], rcut, t, false);
-        ca = CX<R>{R(geo.a.r), R(geo.a.i)};
-        cb = CX<R>{R(geo.b.r), R(geo.b.i)};
-        if (slot == 0) {
-          nsw[q] = t.wj[nt[q]] * geo.sfac;
-          ug[0] = R(1);
-          ug[1] = R(0);
-        }
+        nab[4 * q] = R(geo.a.r);
+        nab[4 * q + 1] = R(geo.a.i);
+        nab[4 * q + 2] = R(geo.b.r);
+        nab[4 * q + 3] = R(geo.b.i);
+        nsw[q] = R(t.wj[nt[q]] * geo.sfac);
+        ug[0] = R(1);
+        ug[1] = R(0);
       }
       __syncthreads();
+      CX<R> ca{R(0), R(0)}, cb{R(0), R(0)};
+      if (active) {
+        const int q = q0 + g;
+        ca = CX<R>{nab[4 * q], nab[4 * q + 1]};
+        cb = CX<R>{nab[4 * q + 2], nab[4 * q + 3]};
+      }
       forward_levels(ug, active, slot, lpn, ca, cb, t, T.rootpq);
       for (int e = tid; e < nu; e += kSnapThreads) {
         R re = R(0), im = R(0);
         for (int q = 0; q < gr; ++q) {
-          const R sw = R(nsw[q0 + q]);
+          const R sw = nsw[q0 + q];
           re = fma(sw, uall[static_cast<size_t>(q) * 2 * nu + 2 * e], re);
           im = fma(sw, uall[static_cast<size_t>(q) * 2 * nu + 2 * e + 1], im);
         }
@@ -409,10 +436,8 @@ __global__ void __launch_bounds__(kSnapThreads)
       CX<R> ca{R(0), R(0)}, cb{R(0), R(0)};
       if (active) {
         const int q = q0 + g;
-        const double rcut = (radi + t.radelem[nt[q]]) * t.rcutfac;
-        const Geo geo = geometry(nx[q], ny[q], nz[q], rcut, t, false);
-        ca = CX<R>{R(geo.a.r), R(geo.a.i)};
-        cb = CX<R>{R(geo.b.r), R(geo.b.i)};
+        ca = CX<R>{nab[4 * q], nab[4 * q + 1]};
+        cb = CX<R>{nab[4 * q + 2], nab[4 * q + 3]};
         if (nn > group && slot == 0) {  // U of this round's neighbours was overwritten
           ug[0] = R(1);
           ug[1] = R(0);
@@ -442,8 +467,9 @@ __global__ void __launch_bounds__(kSnapThreads)
           const R* uj = ug + 2 * t.ublk[j];
           const R* ul = ug + 2 * t.ublk[Lv];
           const R* yj = yv + 2 * t.ublk[j];
-          for (int e = slot; e < nuj; e += lpn) {
-            const int mb = e / (j + 1), ma = e % (j + 1);
+          int mb, ma;
+          rc_start(slot, j + 1, mb, ma);
+          for (int e = slot; e < nuj; e += lpn, rc_step(lpn, j + 1, mb, ma)) {
             const R wgt = ((j & 1) == 0 && e == nuj - 1) ? R(0.5) : R(1);
             F = fma(wgt, fma(uj[2 * e], yj[2 * e], uj[2 * e + 1] * yj[2 * e + 1]), F);
             const R Gr = A[2 * e], Gi = A[2 * e + 1];
@@ -463,8 +489,9 @@ __global__ void __launch_bounds__(kSnapThreads)
           // adjoint of level j-1 by gathering its readers in level j
           const int nul = nunique(Lv);
           const R* yl = yv + 2 * t.ublk[Lv];
-          for (int u = slot; u < nul; u += lpn) {
-            const int r = u / (Lv + 1), cc = u % (Lv + 1);
+          int r, cc;
+          rc_start(slot, Lv + 1, r, cc);
+          for (int u = slot; u < nul; u += lpn, rc_step(lpn, Lv + 1, r, cc)) {
             const R wgt = ((Lv & 1) == 0 && u == nul - 1) ? R(0.5) : R(1);
             R accr = wgt * yl[2 * u], acci = wgt * yl[2 * u + 1];
             if (uq(j, r, cc)) {
@@ -765,10 +792,13 @@ int snap_build(const xnb_snap_params& p, int device, SnapArgs& t, std::vector<vo
   // largest that keeps a CTA within ~100 KB (two CTAs per SM), at most 32
   const int lvl_max = nunique(J);
   const size_t fixed_d = 4 * kSnapMaxNbr + kSnapMaxNbr / 2 + kSnapMaxNbr / 8 + kSnapThreads * 5 + 12;
-  const size_t fixed_r = 2 * t.nu_full + 4 * t.nu_unique;
+  const size_t fixed_r = 5 * kSnapMaxNbr + 2 * t.nu_full + 4 * t.nu_unique;
   const size_t per = 2 * t.nu_unique + 4 * lvl_max;
+  // budgets: ~100 KB (two CTAs per SM) for the FP64 kernel, whose FP64 pipe is
+  // busy anyway; ~54 KB (four CTAs per SM with the per-CTA reserve) for the FP32 kernel, which needs the
+  // warps to hide shared-memory latency
   auto plan = [&](size_t rsize, int& group, size_t& bytes) {
-    const size_t budget = 100 * 1024, base = fixed_d * 8 + fixed_r * rsize;
+    const size_t budget = (rsize == 8 ? 100 : 54) * 1024, base = fixed_d * 8 + fixed_r * rsize;
     long long grp = budget > base ? static_cast<long long>((budget - base) / (per * rsize)) : 1;
     grp = std::max(1LL, std::min<long long>(grp, kSnapMaxGroup));
     group = static_cast<int>(grp);
