@@ -197,6 +197,29 @@ SysDesc make_desc(const xnb_lj_params& p) {
   d.nbh2 = nbh * nbh;
   const double max_displ = p.rcut_inc / 2.0;
   d.max_displ2 = max_displ * max_displ;
+  {
+    // Trigger pre-decision. Each FP32 mirror h = fl32(fl64(x - o)) is within
+    // u|X| (1 + 2^-29) of X = x - o, u = 2^-24; positions stay within one cell
+    // of the domain between rebuilds, so |X| <= P = max period + cell size. A
+    // mirror difference fl32(h_x - h_b) is then within E = u (2P + 1) (1 + 2^-20)
+    // of the exact displacement component d_k (|d_k| <= 1 when it matters), and
+    // fmaf(dz, dz, fmaf(dy, dy, dx dx)) within 2 sqrt(3) |d| E + 3 E^2 + 3 u |d|^2
+    // of |d|^2 (+ u^2 terms). The error grows with |d|, so the bound at
+    // |d| = max_displ decides both sides of the threshold; it is doubled and the
+    // thresholds are rounded outwards to FP32.
+    double P = 0.0;
+    for (int a = 0; a < 3; ++a) P = std::max(P, std::fabs(p.extent[a] - p.origin[a]));
+    P += p.cell_size;
+    const double u = std::ldexp(1.0, -24);
+    const double E = u * (2.0 * P + 1.0) * (1.0 + std::ldexp(1.0, -20));
+    const double m2 = 2.0 * (2.0 * std::sqrt(3.0) * max_displ * E + 3.0 * E * E + 3.0 * u * d.max_displ2 +
+                             4.0 * u * u * d.max_displ2);
+    float lo_f = static_cast<float>(d.max_displ2 - m2), hi_f = static_cast<float>(d.max_displ2 + m2);
+    if (static_cast<double>(lo_f) > d.max_displ2 - m2) lo_f = std::nextafter(lo_f, -1.0f);
+    if (static_cast<double>(hi_f) < d.max_displ2 + m2) hi_f = std::nextafter(hi_f, 2.0f * hi_f + 1.0f);
+    d.trig_lo_f = lo_f > 0.0f ? lo_f : 0.0f;
+    d.trig_hi_f = hi_f;
+  }
   d.epsilon = p.epsilon;
   d.sigma = p.sigma;
   {
@@ -391,7 +414,7 @@ int xnb_version(void) { return 10000; }
 int64_t xnb_system_bytes(int64_t n, int64_t ncells, double list_per_particle) {
   // doubles r v f pe, restored backup, rebin scratch (22); ids (2); u32 cell, backup,
   // rebin and list bookkeeping (10); FP32 hi/lo mirrors; types (2)
-  const int64_t per_part = 22 * 8 + 2 * 8 + 10 * 4 + 2 * 16 + 2;
+  const int64_t per_part = 22 * 8 + 2 * 8 + 10 * 4 + 3 * 16 + 2;
   const int64_t per_cell = 4 * 6 + 8 + 4;
   return n * per_part + ncells * per_cell + static_cast<int64_t>(static_cast<double>(n) * list_per_particle) * 4;
 }
@@ -431,6 +454,7 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   rc = rc ? rc : dalloc(b, &a.id, P);
   rc = rc ? rc : dalloc(b, &a.pf, P);
   rc = rc ? rc : dalloc(b, &a.pflo, P);
+  rc = rc ? rc : dalloc(b, &a.rbf, P);
   rc = rc ? rc : dalloc(b, &a.nbr_half, P);
   rc = rc ? rc : dalloc(b, &a.any_rebuild, 4);
   rc = rc ? rc : dalloc(b, &a.t_id, P);

@@ -363,9 +363,11 @@ __global__ void __launch_bounds__(256)
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
       const uint32_t c = a.pcell[i];
       if (c == kInvalid || !sys_flagged(st, a.cell_sys[c])) continue;
-      a.rbx[i] = a.rx[i];
-      a.rby[i] = a.ry[i];
-      a.rbz[i] = a.rz[i];
+      const double x = a.rx[i], y = a.ry[i], z = a.rz[i];
+      a.rbx[i] = x;
+      a.rby[i] = y;
+      a.rbz[i] = z;
+      a.rbf[i] = make_pf(sys[a.cell_sys[c]], x, y, z);
     }
   } else {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
@@ -384,6 +386,7 @@ __global__ void __launch_bounds__(256)
     a.rbx[i] = restore_u32(bx, lo[0], S.cell_size);
     a.rby[i] = restore_u32(by, lo[1], S.cell_size);
     a.rbz[i] = restore_u32(bz, lo[2], S.cell_size);
+    a.rbf[i] = make_pf(S, a.rbx[i], a.rby[i], a.rbz[i]);
   }
   }
 }

@@ -57,6 +57,10 @@ struct SysDesc {
   float outer_lo_f[3], outer_hi_f[3];
   float pre_margin_f, filter_margin_f;
   float inv_cell_f, q_margin_f;  // FP32 cell-index pre-decision: 1/cell_size and its proven margin (cells)
+  // FP32 pre-decision of the displacement trigger: |d|^2 from the FP32 mirrors of
+  // the position and of its backup is above trig_hi_f only when the FP64 |d|^2
+  // reaches max_displ2, below trig_lo_f only when it does not
+  float trig_lo_f, trig_hi_f;
   double inv_cell;               // fl(1/cell_size): reciprocal pre-decision of the backup encoding
   double m24eps, eps4, sig2, eps24;  // -24*eps, 4*eps (lennard_jones.cu:54-55), sigma^2, 24*eps
   int32_t dims[3];
@@ -92,6 +96,7 @@ struct DevArrays {
   uint32_t* pcell;                 // global cell of each particle
   uint32_t *bkx, *bky, *bkz;       // backup_r u32 encoding (backup_r.h:36-51)
   double *rbx, *rby, *rbz;         // the same backup restored once per rebuild (restore_u32_double)
+  float4* rbf;                     // FP32 hi part of (backup - origin), for the trigger's pre-decision
   // rebin scratch
   double *t_rx, *t_ry, *t_rz, *t_vx, *t_vy, *t_vz, *t_fx, *t_fy, *t_fz;
   uint64_t* t_id;
@@ -174,17 +179,24 @@ __device__ __forceinline__ void cell_ijk(const SysDesc& s, uint32_t local_cell, 
 
 __device__ __forceinline__ int pmod_i(int i, int n) { return ((i % n) + n) % n; }
 
+// fl32(x) and fl64(f) on the integer pipes (xnb_widen.h): the same bits as the
+// hardware conversions, which would occupy the FP64 pipe
+__device__ __forceinline__ float narrow_f64(double x) {
+  return __uint_as_float(narrow_f64_bits(static_cast<uint64_t>(__double_as_longlong(x))));
+}
+__device__ __forceinline__ double widen_f32(float f);
+
 // FP32 position relative to the system origin, as stored in DevArrays::pf, and
 // its residual (DevArrays::pflo): hi = fl32(x - o), lo = fl32((x - o) - hi).
+// Only the two subtractions per coordinate use the FP64 pipe.
 __device__ __forceinline__ float4 make_pf(const SysDesc& s, double x, double y, double z) {
-  return make_float4(static_cast<float>(x - s.origin[0]), static_cast<float>(y - s.origin[1]),
-                     static_cast<float>(z - s.origin[2]), 0.f);
+  return make_float4(narrow_f64(x - s.origin[0]), narrow_f64(y - s.origin[1]), narrow_f64(z - s.origin[2]), 0.f);
 }
 __device__ __forceinline__ void make_pf2(const SysDesc& s, double x, double y, double z, float4& hi, float4& lo) {
   const double rx = x - s.origin[0], ry = y - s.origin[1], rz = z - s.origin[2];
-  hi = make_float4(static_cast<float>(rx), static_cast<float>(ry), static_cast<float>(rz), 0.f);
-  lo = make_float4(static_cast<float>(rx - static_cast<double>(hi.x)), static_cast<float>(ry - static_cast<double>(hi.y)),
-                   static_cast<float>(rz - static_cast<double>(hi.z)), 0.f);
+  hi = make_float4(narrow_f64(rx), narrow_f64(ry), narrow_f64(rz), 0.f);
+  lo = make_float4(narrow_f64(rx - widen_f32(hi.x)), narrow_f64(ry - widen_f32(hi.y)), narrow_f64(rz - widen_f32(hi.z)),
+                   0.f);
 }
 
 __device__ __forceinline__ float image_coord_f(float x, float period, int d) {

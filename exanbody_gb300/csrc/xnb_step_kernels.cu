@@ -52,6 +52,7 @@ __global__ void __launch_bounds__(256)
       double x = a.rx[i], y = a.ry[i], z = a.rz[i];
       double vx = a.vx[i], vy = a.vy[i], vz = a.vz[i];
       const double fx = a.fx[i], fy = a.fy[i], fz = a.fz[i];
+      float4 cur_hi;  // FP32 mirror of the position the trigger sees
       if (push_r) {
         if (EXACT) {
           x = __dadd_rn(x, __dadd_rn(__dmul_rn(vx, dt), __dmul_rn(fx, dt2)));
@@ -69,6 +70,9 @@ __global__ void __launch_bounds__(256)
         make_pf2(S, x, y, z, hi, lo);
         a.pf[i] = hi;
         a.pflo[i] = lo;
+        cur_hi = hi;
+      } else if (!EXACT && trigger) {
+        cur_hi = a.pf[i];
       }
       if (push_v) {
         if (EXACT) {
@@ -85,11 +89,26 @@ __global__ void __launch_bounds__(256)
         a.vz[i] = vz;
       }
       if (trigger && st[s].rebuild_armed) {
-        const double dx = __dsub_rn(x, a.rbx[i]);
-        const double dy = __dsub_rn(y, a.rby[i]);
-        const double dz = __dsub_rn(z, a.rbz[i]);
-        const double d2 = EXACT ? norm2_rn(dx, dy, dz) : fma(dz, dz, fma(dy, dy, dx * dx));
-        over = d2 >= S.max_displ2;
+        // FP32 pre-decision from the mirrors, FP64 inside the proven band
+        bool decided = false;
+        if (!EXACT) {
+          const float4 rb = a.rbf[i];
+          const float ex = cur_hi.x - rb.x, ey = cur_hi.y - rb.y, ez = cur_hi.z - rb.z;
+          const float d2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+          if (d2f > S.trig_hi_f) {
+            over = true;
+            decided = true;
+          } else if (d2f < S.trig_lo_f) {
+            decided = true;
+          }
+        }
+        if (!decided) {
+          const double dx = __dsub_rn(x, a.rbx[i]);
+          const double dy = __dsub_rn(y, a.rby[i]);
+          const double dz = __dsub_rn(z, a.rbz[i]);
+          const double d2 = EXACT ? norm2_rn(dx, dy, dz) : fma(dz, dz, fma(dy, dy, dx * dx));
+          over = d2 >= S.max_displ2;
+        }
       }
     }
     if (trigger) {
@@ -262,10 +281,13 @@ __global__ void __launch_bounds__(256)
       fy = fma(-ya, psum, fy);
       fz = fma(-za, psum, fz);
     }
-    // the force field was zeroed (zero_particle_force.cu:39-46) and receives the sum
-    fx = __dadd_rn(0.0, fx);
-    fy = __dadd_rn(0.0, fy);
-    fz = __dadd_rn(0.0, fz);
+    // the force field was zeroed (zero_particle_force.cu:39-46) and receives the
+    // sum; 0 + s differs from s only for s = -0, which the exact path keeps
+    if (P == kFp64Exact) {
+      fx = __dadd_rn(0.0, fx);
+      fy = __dadd_rn(0.0, fy);
+      fz = __dadd_rn(0.0, fz);
+    }
     if (S.divide_by_mass) {
       // divide_force_by_type_scalar (compute/vec3_typescalar_op.cu:156, math_functors.h:140)
       fx = __ddiv_rn(fx, S.mass);

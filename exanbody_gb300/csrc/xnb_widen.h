@@ -1,5 +1,5 @@
-// Float-to-double widening on integer operations, shared by the force kernels
-// and the host-side check (tests/test_widen.py compiles this header with g++).
+// Float <-> double conversions on integer operations, shared by the kernels and
+// the host-side check (tests/test_widen.py compiles this header with g++).
 #pragma once
 
 #include <cstdint>
@@ -41,5 +41,36 @@ XNB_HD uint64_t widen_f32_bits(uint32_t u) {
   return (static_cast<uint64_t>(hi) << 32) | static_cast<uint64_t>(u << 29);
 }
 
+// IEEE 754 binary64 -> binary32 conversion, round to nearest (ties to even), on
+// integer operations (the hardware conversion occupies the FP64 pipe). With
+// e the binary64 exponent field, the binary32 exponent field is e - 896; the 52
+// fraction bits plus the implicit one are shifted right by 29 (by 29 + 1 - fe
+// for a binary32 subnormal result) and rounded on the dropped bits; a carry out
+// of the fraction moves into the exponent, and results at or above the largest
+// exponent become infinities. Binary64 zeros and subnormals give a signed zero;
+// infinities stay infinite and NaNs stay NaN (quiet bit set, top payload kept).
+XNB_HD uint32_t narrow_f64_bits(uint64_t b) {
+  const uint32_t sign = static_cast<uint32_t>(b >> 32) & 0x80000000u;
+  const int e = static_cast<int>((b >> 52) & 0x7ffu);
+  const uint64_t m = b & 0x000fffffffffffffull;
+  if (e == 0x7ff) return sign | 0x7f800000u | (m ? (0x00400000u | static_cast<uint32_t>(m >> 29)) : 0u);
+  if (e == 0) return sign;
+  int fe = e - 896;
+  int shift = 29;
+  if (fe <= 0) {
+    shift += 1 - fe;
+    fe = 0;
+    if (shift > 62) return sign;
+  }
+  const uint64_t mant = m | (1ull << 52);
+  uint64_t q = mant >> shift;
+  const uint64_t rem = mant & ((1ull << shift) - 1u);
+  const uint64_t half = 1ull << (shift - 1);
+  if (rem > half || (rem == half && (q & 1u))) ++q;
+  const uint32_t r = fe == 0 ? static_cast<uint32_t>(q)
+                             : (static_cast<uint32_t>(fe) << 23) + (static_cast<uint32_t>(q) - (1u << 23));
+  if (fe >= 255 || r >= 0x7f800000u) return sign | 0x7f800000u;
+  return sign | r;
+}
 
 }  // namespace xnb
