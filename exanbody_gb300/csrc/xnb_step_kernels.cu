@@ -123,11 +123,19 @@ __global__ void __launch_bounds__(256)
 }
 
 // ---------------------------------------------------------------------------
-// Double-precision reciprocal from an FP32 seed (relative error <= 2^-23)
-// refined by two Newton-Raphson steps y <- y + y*(1 - d*y) in FP64: the error
-// squares twice (2^-46, then below the FP64 rounding), not correctly rounded.
+// Double-precision reciprocal of d > 0 from an FP32 seed refined by two
+// Newton-Raphson steps y <- y + y*(1 - d*y) in FP64, not correctly rounded.
+// The seed stays off the FP64 pipe: d is truncated to binary32 by moving its
+// exponent (re-biased by -896) and the top 23 fraction bits with one funnel
+// shift, the exponent field clamped to [1, 252] so that the FP32 reciprocal is
+// a positive normal, which widens back by the inverse bit move. For d in
+// [2^-126, 2^126) the seed is within 2^-23 + 2^-24 of 1/d, and
+// the two steps take the error to 2^-44, then below the FP64 rounding.
 __device__ __forceinline__ double rcp_nr(double d) {
-  double y = static_cast<double>(__frcp_rn(static_cast<float>(d)));
+  const int hi = min(max(__double2hiint(d) - 0x38000000, 0x00100000), 0x0fcfffff);
+  const float s = __uint_as_float(__funnelshift_l(static_cast<uint32_t>(__double2loint(d)), static_cast<uint32_t>(hi), 3));
+  const uint32_t r = __float_as_uint(__frcp_rn(s));
+  double y = __hiloint2double(static_cast<int>((r >> 3) + 0x38000000u), static_cast<int>(r << 29));
   double e = fma(-d, y, 1.0);
   y = fma(y, e, y);
   e = fma(-d, y, 1.0);
@@ -242,9 +250,9 @@ __global__ void __launch_bounds__(256)
           dyf = (hb.y - paf.y) + (lb.y - pal.y);
           dzf = (hb.z - paf.z) + (lb.z - pal.z);
         } else {
-          dxf = static_cast<float>(__dsub_rn(xb, xa));
-          dyf = static_cast<float>(__dsub_rn(yb, ya));
-          dzf = static_cast<float>(__dsub_rn(zb, za));
+          dxf = narrow_f64(__dsub_rn(xb, xa));
+          dyf = narrow_f64(__dsub_rn(yb, ya));
+          dzf = narrow_f64(__dsub_rn(zb, za));
         }
         const float r2 = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
         bool in;
@@ -393,9 +401,9 @@ __global__ void __launch_bounds__(256)
           dyf = (hb.y - paf.y) + (lb.y - pal.y);
           dzf = (hb.z - paf.z) + (lb.z - pal.z);
         } else {
-          dxf = static_cast<float>(__dsub_rn(xb, xa));
-          dyf = static_cast<float>(__dsub_rn(yb, ya));
-          dzf = static_cast<float>(__dsub_rn(zb, za));
+          dxf = narrow_f64(__dsub_rn(xb, xa));
+          dyf = narrow_f64(__dsub_rn(yb, ya));
+          dzf = narrow_f64(__dsub_rn(zb, za));
         }
         const float r2 = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
         if (r2 > S.rc2_f + S.rc_margin_f) {
