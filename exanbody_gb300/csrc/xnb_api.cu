@@ -466,6 +466,8 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   uint32_t** u32c[] = {&a.cell_start, &a.cell_n, &a.cell_sys, &a.cell_cnt, &a.cell_stay, &a.cell_nmov};
   for (uint32_t** p : u32c) rc = rc ? rc : dalloc(b, p, Cc + 1);
   rc = rc ? rc : dalloc(b, &a.cell_scan, Cc + 1);
+  rc = rc ? rc : dalloc(b, &a.nbr_wide, Cc + 1);
+  rc = rc ? rc : dalloc(b, &a.nbr_wide_n, 1);
   rc = rc ? rc : dalloc(b, &a.scan_blocks, scan_scratch_elems(static_cast<uint32_t>(Cc + 1)) + 8);
   rc = rc ? rc : dalloc(b, &a.nbr, L);
   rc = rc ? rc : dalloc(b, &b->d_sys, static_cast<uint64_t>(cfg->max_systems));
@@ -485,6 +487,7 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   cudaMemset(a.cell_start, 0, (Cc + 1) * sizeof(uint32_t));
   cudaMemset(b->d_st, 0, sizeof(SysState) * cfg->max_systems);
   cudaMemset(a.any_rebuild, 0, sizeof(unsigned int));
+  cudaMemset(a.nbr_wide_n, 0, sizeof(unsigned int));
   if (cudaDeviceSynchronize() != cudaSuccess) {
     xnb_batch_destroy(b);
     return fail(XNB_ERR_CUDA, "initialisation failed");

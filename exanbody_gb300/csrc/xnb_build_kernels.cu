@@ -412,8 +412,7 @@ __global__ void k_arm(int nsys, SysState* st, const unsigned int* any) {
 // the FP64 ghost filter) decide, so the pair set is bit-exact.
 constexpr uint32_t kAmbiguousBit = 0x80000000u;  // entry flag: ghost filter undecided in FP32
 
-__device__ __forceinline__ float4 stage_candidate(const SysDesc& S, const DevArrays& a, uint32_t j, uint32_t gc) {
-  const float4 pb = a.pf[j];
+__device__ __forceinline__ float4 stage_from(const SysDesc& S, const float4 pb, uint32_t j, uint32_t gc) {
   float4 rb;
   rb.x = image_coord_f(pb.x, S.period_f[0], static_cast<int>(gc % 3u));
   rb.y = image_coord_f(pb.y, S.period_f[1], static_cast<int>((gc / 3u) % 3u));
@@ -436,6 +435,10 @@ __device__ __forceinline__ float4 stage_candidate(const SysDesc& S, const DevArr
   }
   rb.w = __uint_as_float(ent);
   return rb;
+}
+
+__device__ __forceinline__ float4 stage_candidate(const SysDesc& S, const DevArrays& a, uint32_t j, uint32_t gc) {
+  return stage_from(S, a.pf[j], j, gc);
 }
 
 // The reference's FP64 decision for one (particle i, candidate entry) pair.
@@ -482,7 +485,8 @@ __device__ __forceinline__ void finish_particle(const DevArrays& a, uint32_t* se
   }
 }
 
-// One block per cell. The block stages the cell's candidates (up to `cap` per
+// One block per cell, for the cells listed by k_neighbors_warp as too large for
+// it (a.nbr_wide). The block stages the cell's candidates (up to `cap` per
 // round) once in shared memory for all its warps; warp w takes the cell's
 // particles w, w + 4, ... two at a time, so each candidate load serves two
 // tests. Each particle's hits go into its fixed slot of S.list_slot entries at
@@ -508,8 +512,10 @@ __global__ void __launch_bounds__(128, 8)
   const unsigned lt = lanemask_lt();
   uint32_t acc_s = kInvalid, acc_max = 0;
   unsigned long long acc_sum = 0;
-  for (uint32_t c = blockIdx.x; c < n_cells; c += gridDim.x) {
+  const uint32_t n_wide = min(*a.nbr_wide_n, n_cells);
+  for (uint32_t it = blockIdx.x; it < n_wide; it += gridDim.x) {
     // every condition below depends on the cell only: the block stays together
+    const uint32_t c = a.nbr_wide[it];
     const uint32_t s = a.cell_sys[c];
     if (s == kInvalid || !sys_flagged(st, s)) continue;
     const uint32_t na = a.cell_n[c];
@@ -687,8 +693,220 @@ __global__ void __launch_bounds__(128, 8)
   if (lane == 0) flush_list_stats(st, sys, acc_s, acc_max, acc_sum);
 }
 
+// ---------------------------------------------------------------------------
+// Warp-per-cell form of the same build, for every cell whose candidates fit the
+// warp's stage (cap) and whose system's slot fits its list buffers (lbuf > slot);
+// the others are appended to a.nbr_wide for k_neighbors. Each warp stages its
+// cell's candidates itself (no block barrier), then tests kNbrP particles per
+// staged load: lanes hold 32 candidates, a ballot per particle keeps its hits in
+// order, and the hits gather in the particle's shared-memory buffer, written out
+// in full lines once its pass ends. Two rare cases leave the fast test through
+// warp-uniform branches: a chunk holding a candidate whose ghost filter is
+// undecided in FP32, and an FP32 distance inside the error band around nbh^2
+// (both then take the reference's FP64 decision, as in k_neighbors).
+constexpr int kNbrP = 4;  // particles tested per staged candidate load
+
+template <bool AMB>
+__device__ __forceinline__ void nbr_chunk(const SysDesc& S, const DevArrays& a, const float4 b, const float (&px)[kNbrP],
+                                          const float (&py)[kNbrP], const float (&pz)[kNbrP], uint32_t i0,
+                                          uint32_t self0, uint32_t t0, uint32_t low0, float nb_lo, float nb_hi,
+                                          float nb_zero, unsigned lt, uint32_t* sbuf, uint32_t lbuf,
+                                          uint32_t (&cur)[kNbrP], uint32_t (&half)[kNbrP]) {
+  const uint32_t ent = __float_as_uint(b.w);
+  const bool amb = AMB && (ent & kAmbiguousBit) != 0;
+  bool hit[kNbrP], may[kNbrP];
+  bool any_may = false;
+#pragma unroll
+  for (int k = 0; k < kNbrP; ++k) {
+    const float dx = px[k] - b.x, dy = py[k] - b.y, dz = pz[k] - b.z;
+    const float d = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    hit[k] = d < nb_lo && d > nb_zero && !amb;
+    may[k] = !hit[k] && d <= nb_hi && ent != self0 + (static_cast<uint32_t>(k) << 5);
+    any_may |= may[k];
+  }
+  if (__any_sync(0xffffffffu, any_may)) {
+#pragma unroll
+    for (int k = 0; k < kNbrP; ++k)
+      if (may[k]) hit[k] = exact_neighbor_test(S, a, i0 + k, ent);
+  }
+  const uint32_t e = AMB ? (ent & ~kAmbiguousBit) : ent;
+  // the particles' own entries (lower-half ends) sit at stage indices low0 + k
+  const bool self_chunk = t0 < low0 + kNbrP && low0 < t0 + 32u;
+#pragma unroll
+  for (int k = 0; k < kNbrP; ++k) {
+    const unsigned m = __ballot_sync(0xffffffffu, hit[k]);
+    // entries past the slot land in the buffer's last word, which is never written out
+    if (hit[k]) sbuf[k * lbuf + min(cur[k] + __popc(m & lt), lbuf - 1u)] = e;
+    if (self_chunk) {
+      const uint32_t w = low0 + static_cast<uint32_t>(k) - t0;
+      if (w < 32u) half[k] = cur[k] + __popc(m & ((1u << w) - 1u));
+    }
+    cur[k] += __popc(m);
+  }
+}
+
+__global__ void __launch_bounds__(128)
+    k_neighbors_warp(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap, int lbuf) {
+  if (*a.any_rebuild == 0) return;
+  extern __shared__ float4 stage_w[];
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t wib = threadIdx.x >> 5;
+  const uint32_t nwarp = blockDim.x >> 5;
+  float4* srel = stage_w + static_cast<size_t>(wib) * cap;
+  uint32_t* sbuf = reinterpret_cast<uint32_t*>(stage_w + static_cast<size_t>(nwarp) * cap) +
+                   static_cast<size_t>(wib) * kNbrP * lbuf;
+  const unsigned lt = lanemask_lt();
+  uint32_t acc_s = kInvalid, acc_max = 0;
+  unsigned long long acc_sum = 0;
+  const uint32_t nw_all = gridDim.x * nwarp;
+  for (uint32_t c = blockIdx.x * nwarp + wib; c < n_cells; c += nw_all) {
+    const uint32_t s = a.cell_sys[c];
+    if (s == kInvalid || !sys_flagged(st, s)) continue;
+    const uint32_t na = a.cell_n[c];
+    if (na == 0) continue;
+    const SysDesc& S = sys[s];
+    const uint32_t sa = a.cell_start[c];
+    int ci, cj, ck;
+    cell_ijk(S, c - S.cell_base, ci, cj, ck);
+
+    // group table: lane g < 27 describes neighbour cell g in (dk, dj, di) order
+    uint32_t g_start = 0, g_n = 0, g_code = kImageCenter;
+    if (lane < 27) {
+      const int di = static_cast<int>(lane % 3) - 1, dj = static_cast<int>((lane / 3) % 3) - 1,
+                dk = static_cast<int>(lane / 9) - 1;
+      int n3[3] = {ci + di, cj + dj, ck + dk};
+      int img[3];
+      for (int ax = 0; ax < 3; ++ax) {
+        img[ax] = 1;
+        if (n3[ax] < 0) { n3[ax] += S.dims[ax]; img[ax] = 0; }
+        else if (n3[ax] >= S.dims[ax]) { n3[ax] -= S.dims[ax]; img[ax] = 2; }
+      }
+      const uint32_t src = S.cell_base + static_cast<uint32_t>((n3[2] * S.dims[1] + n3[1]) * S.dims[0] + n3[0]);
+      g_start = a.cell_start[src];
+      g_n = a.cell_n[src];
+      g_code = static_cast<uint32_t>(img[0] + 3 * img[1] + 9 * img[2]);
+    }
+    uint32_t g_off = g_n;  // inclusive scan over lanes
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint32_t v = __shfl_up_sync(0xffffffffu, g_off, off);
+      if (lane >= static_cast<uint32_t>(off)) g_off += v;
+    }
+    const uint32_t ncand = __shfl_sync(0xffffffffu, g_off, 26);
+    g_off -= g_n;
+    const uint32_t slot = S.list_slot;
+    if (ncand > static_cast<uint32_t>(cap) || slot >= static_cast<uint32_t>(lbuf)) {
+      if (lane == 0) a.nbr_wide[atomicAdd(a.nbr_wide_n, 1u)] = c;
+      continue;
+    }
+    if (s != acc_s) {
+      if (lane == 0) flush_list_stats(st, sys, acc_s, acc_max, acc_sum);
+      acc_s = s;
+      acc_max = 0;
+      acc_sum = 0;
+    }
+    const uint32_t off_self = __shfl_sync(0xffffffffu, g_off, 13);
+    float4 own = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (na <= 32 && lane < na) own = a.pf[sa + lane];
+
+    // stage: candidate u belongs to the last group g with g_off[g] <= u; four
+    // candidates per lane are located and loaded before any is converted
+    const uint32_t mpad = (ncand + 31u) & ~31u;
+    for (uint32_t t0 = 0; t0 < mpad; t0 += 128u) {
+      float4 pb[4];
+      uint32_t jj[4], gcs[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t u = t0 + 32u * k + lane;
+        uint32_t g = 0;
+#pragma unroll
+        for (uint32_t step = 16; step > 0; step >>= 1) {
+          const uint32_t probe = g + step;
+          const uint32_t po = __shfl_sync(0xffffffffu, g_off, probe < 27u ? probe : 26u);
+          if (probe < 27u && po <= u) g = probe;
+        }
+        const uint32_t gs = __shfl_sync(0xffffffffu, g_start, g);
+        const uint32_t go = __shfl_sync(0xffffffffu, g_off, g);
+        gcs[k] = __shfl_sync(0xffffffffu, g_code, g);
+        jj[k] = gs + (u - go);
+        pb[k] = u < ncand ? __ldg(a.pf + jj[k]) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t u = t0 + 32u * k + lane;
+        if (u < ncand) srel[u] = stage_from(S, pb[k], jj[k], gcs[k]);
+        else if (u < mpad) srel[u] = make_float4(1.0e18f, 1.0e18f, 1.0e18f, __uint_as_float(kInvalid));
+      }
+    }
+    __syncwarp();
+
+    const float nb_hi = S.nbh2_f + S.nbh_margin_f;
+    const float nb_lo = S.nbh2_f - S.nbh_margin_f;
+    const float nb_zero = S.nbh_margin_f;
+    uint32_t* const seg = a.nbr + S.list_base;
+    for (uint32_t p0 = 0; p0 < na; p0 += kNbrP) {
+      // particles past the cell's end sit at -1e18: never within reach of a
+      // candidate (real ones, or the +1e18 dummies), so they need no test
+      float px[kNbrP], py[kNbrP], pz[kNbrP];
+      uint32_t cur[kNbrP], half[kNbrP];
+#pragma unroll
+      for (int k = 0; k < kNbrP; ++k) {
+        const uint32_t pk = p0 + k;
+        float4 q;
+        if (na <= 32) {
+          q.x = __shfl_sync(0xffffffffu, own.x, pk & 31u);
+          q.y = __shfl_sync(0xffffffffu, own.y, pk & 31u);
+          q.z = __shfl_sync(0xffffffffu, own.z, pk & 31u);
+        } else {
+          q = pk < na ? a.pf[sa + pk] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        const bool valid = pk < na;
+        px[k] = valid ? q.x : -1.0e18f;
+        py[k] = valid ? q.y : -1.0e18f;
+        pz[k] = valid ? q.z : -1.0e18f;
+        cur[k] = 0;
+        half[k] = 0;
+      }
+      const uint32_t i0 = sa + p0;
+      const uint32_t self0 = ((i0 - S.part_base) << 5) | static_cast<uint32_t>(kImageCenter);
+      const uint32_t low0 = off_self + p0;
+      for (uint32_t t0 = 0; t0 < mpad; t0 += 32) {
+        const float4 b = srel[t0 + lane];
+        const uint32_t ent = __float_as_uint(b.w);
+        // entries in [kAmbiguousBit, kInvalid): ghost filter undecided in FP32
+        if (__any_sync(0xffffffffu, ent - kAmbiguousBit < kInvalid - kAmbiguousBit))
+          nbr_chunk<true>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, sbuf,
+                          static_cast<uint32_t>(lbuf), cur, half);
+        else
+          nbr_chunk<false>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, sbuf,
+                           static_cast<uint32_t>(lbuf), cur, half);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int k = 0; k < kNbrP; ++k) {
+        const uint32_t pk = p0 + k;
+        if (pk < na) {
+          const uint32_t i = sa + pk;
+          const uint32_t base = (i - S.part_base) * slot;  // the host keeps npart * slot below 2^32
+          const uint32_t nw = min(cur[k], slot);
+          for (uint32_t q = lane; q < nw; q += 32) seg[base + q] = sbuf[k * lbuf + q];
+          if (lane == 0) {
+            a.nbr_cnt[i] = cur[k];
+            a.nbr_half[i] = half[k];
+            a.nbr_start[i] = base;
+          }
+          acc_max = max(acc_max, cur[k]);
+          acc_sum += cur[k];
+        }
+      }
+      __syncwarp();
+    }
+  }
+  if (lane == 0) flush_list_stats(st, sys, acc_s, acc_max, acc_sum);
+}
+
 // Clears the per-build list statistics of the flagged systems.
-__global__ void k_nbr_reset(int nsys, SysState* st, const unsigned int* any) {
+__global__ void k_nbr_reset(int nsys, SysState* st, const unsigned int* any, unsigned int* wide_n) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *wide_n = 0;
   if (*any == 0) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsys || !st[s].rebuild) return;
@@ -848,11 +1066,22 @@ int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const D
                      cudaStream_t stream) {
   if (ex.n_cells == 0) return 0;
   const size_t smem = static_cast<size_t>(cap) * sizeof(float4) + static_cast<size_t>(4) * 2 * lbuf * sizeof(uint32_t);
-  // a per-device attribute: set it on the current device every time (a host call, no GPU work)
+  // warp-per-cell buffers: one slot of each of kNbrP particles plus a spill word
+  // (lbuf_w > slot); slots above 512 entries leave every cell to k_neighbors
+  const int lbuf_w = (lbuf > 0 && lbuf <= 512) ? lbuf + 32 : 32;
+  const size_t smem_w = 4 * (static_cast<size_t>(cap) * sizeof(float4) + static_cast<size_t>(kNbrP) * lbuf_w * 4);
+  // per-device attributes: set them on the current device every time (host calls, no GPU work)
   cudaFuncSetAttribute(k_neighbors, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-  k_nbr_reset<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild);
+  cudaFuncSetAttribute(k_neighbors_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_neighbors_warp, 128, smem_w) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  const long long want_w = (static_cast<long long>(ex.n_cells) + 3) / 4;
+  const int grid_w = static_cast<int>(std::max(1ll, std::min(want_w, static_cast<long long>(per_sm) * ex.sm_count)));
+  k_nbr_reset<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild, a.nbr_wide_n);
+  k_neighbors_warp<<<grid_w, 128, smem_w, stream>>>(ex.n_cells, sys, st, a, cap, lbuf_w);
   k_neighbors<<<warp_grid(ex.n_cells, 1, ex.sm_count), 128, smem, stream>>>(ex.n_cells, sys, st, a, cap, lbuf);
-  return 2;
+  return 3;
 }
 
 }  // namespace xnb

@@ -118,6 +118,8 @@ struct DevArrays {
   uint32_t* nbr_half;              // per particle: entries before it in the reference order
                                    // ((cell_b, p_b) < (cell_a, p_a)), the Newton half list
   uint32_t* nbr;                   // all segments
+  uint32_t* nbr_wide;              // cells whose candidates or slot exceed the warp-per-cell build's buffers
+  unsigned int* nbr_wide_n;        // number of them (reset by each build)
   // scan scratch
   unsigned long long* scan_blocks;
 };

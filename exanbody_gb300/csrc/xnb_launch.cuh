@@ -44,8 +44,10 @@ int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevAr
 // backup_r alone.
 int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream);
 // chunk_neighbors for systems with rebuild != 0: one pass writing each list
-// into its particle's slot (statistics reset + build, two kernels). lbuf: the
-// per-warp shared-memory list buffer in entries (slots up to lbuf are buffered).
+// into its particle's slot (statistics reset, the warp-per-cell build, and the
+// block-per-cell build of the cells too large for it: three kernels). lbuf: the
+// largest slot rounded up to 32 entries, 0 above 1024 or when no system has a
+// slot yet; it sizes the shared-memory list buffers.
 int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int stage_cap,
                      int lbuf, cudaStream_t stream);
 

@@ -123,6 +123,32 @@ def test_small_and_dense_systems_bit_exact(n, rho, T):
     assert_bitwise_equal(b.download(s), o.particles())
 
 
+@pytest.mark.parametrize("cap", [32, 512, 544])
+def test_stage_cap_splits_cells_between_builds(cap):
+    """Cells whose candidates exceed the stage cap are built block-per-cell, the
+    others warp-per-cell; a cap near the mean candidate count (~515 here) splits
+    one system between both builds. Lists match the oracle's, and the lower-half
+    lengths give Newton-list forces equal to the full-list ones."""
+    w = workloads.lj_fcc_system(12, 0.8442, 1.44, 99)
+    b, s = gpu_system(w)
+    b.set_tuning(cap, 128)
+    b.init_particles(s, xnb.PREC_FP64_EXACT)
+    o = oracle_from(w)
+    o.init()
+    compare_pairs(b, s, o)
+    # off the lattice first: there the net forces are rounding-sized
+    for _ in range(30):
+        b.step(1, xnb.PREC_FP64_EXACT, xnb.STEP_HOST_SYNC)
+        if o.step():
+            compare_pairs(b, s, o)
+    assert_bitwise_equal(b.download(s), o.particles())
+    b.lennard_jones_force(s, xnb.PREC_FP64, True)
+    full = forces(b.download(s))
+    b.lennard_jones_force(s, xnb.PREC_FP64 | xnb.PREC_NEWTON, True)
+    e, _ = force_error(forces(b.download(s)), full)
+    assert e <= FP64_TOL, e
+
+
 def test_slab_with_empty_cells_bit_exact():
     w = workloads.lj_slab_system(8, 0.8442, 0.8, 5)
     b, s = gpu_system(w)
