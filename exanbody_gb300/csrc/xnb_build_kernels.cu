@@ -704,9 +704,9 @@ __global__ void __launch_bounds__(128, 8)
 // warp-uniform branches: a chunk holding a candidate whose ghost filter is
 // undecided in FP32, and an FP32 distance inside the error band around nbh^2
 // (both then take the reference's FP64 decision, as in k_neighbors).
-constexpr int kNbrP = 4;  // particles tested per staged candidate load
+constexpr int kNbrP = 4;  // particles tested per staged candidate load (even: FP32x2 pairs)
 
-template <bool AMB>
+template <bool AMB, bool SELF>
 __device__ __forceinline__ void nbr_chunk(const SysDesc& S, const DevArrays& a, const float4 b, const float (&px)[kNbrP],
                                           const float (&py)[kNbrP], const float (&pz)[kNbrP], uint32_t i0,
                                           uint32_t self0, uint32_t t0, uint32_t low0, float nb_lo, float nb_hi,
@@ -716,12 +716,35 @@ __device__ __forceinline__ void nbr_chunk(const SysDesc& S, const DevArrays& a, 
   const bool amb = AMB && (ent & kAmbiguousBit) != 0;
   bool hit[kNbrP], may[kNbrP];
   bool any_may = false;
+  // squared FP32 distances two particles at a time on the packed FP32x2 path:
+  // per particle the roundings of fmaf(dx, dx, fmaf(dy, dy, dz * dz)) exactly
+  float dd[kNbrP];
+  {
+    unsigned long long bx2, by2, bz2;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(bx2) : "f"(b.x));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(by2) : "f"(b.y));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(bz2) : "f"(b.z));
+#pragma unroll
+    for (int k = 0; k < kNbrP; k += 2) {
+      unsigned long long x2, y2, z2, dx, dy, dz, d;
+      asm("mov.b64 %0, {%1, %2};" : "=l"(x2) : "f"(px[k]), "f"(px[k + 1]));
+      asm("mov.b64 %0, {%1, %2};" : "=l"(y2) : "f"(py[k]), "f"(py[k + 1]));
+      asm("mov.b64 %0, {%1, %2};" : "=l"(z2) : "f"(pz[k]), "f"(pz[k + 1]));
+      asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(dx) : "l"(x2), "l"(bx2));
+      asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(dy) : "l"(y2), "l"(by2));
+      asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(dz) : "l"(z2), "l"(bz2));
+      asm("mul.rn.f32x2 %0, %1, %1;" : "=l"(d) : "l"(dz));
+      asm("fma.rn.f32x2 %0, %1, %1, %2;" : "=l"(d) : "l"(dy), "l"(d));
+      asm("fma.rn.f32x2 %0, %1, %1, %2;" : "=l"(d) : "l"(dx), "l"(d));
+      asm("mov.b64 {%0, %1}, %2;" : "=f"(dd[k]), "=f"(dd[k + 1]) : "l"(d));
+    }
+  }
 #pragma unroll
   for (int k = 0; k < kNbrP; ++k) {
-    const float dx = px[k] - b.x, dy = py[k] - b.y, dz = pz[k] - b.z;
-    const float d = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float d = dd[k];
     hit[k] = d < nb_lo && d > nb_zero && !amb;
-    may[k] = !hit[k] && d <= nb_hi && ent != self0 + (static_cast<uint32_t>(k) << 5);
+    // the particle's own entry only sits in a SELF chunk (d = 0 there: no hit)
+    may[k] = !hit[k] && d <= nb_hi && (!SELF || ent != self0 + (static_cast<uint32_t>(k) << 5));
     any_may |= may[k];
   }
   if (__any_sync(0xffffffffu, any_may)) {
@@ -730,14 +753,12 @@ __device__ __forceinline__ void nbr_chunk(const SysDesc& S, const DevArrays& a, 
       if (may[k]) hit[k] = exact_neighbor_test(S, a, i0 + k, ent);
   }
   const uint32_t e = AMB ? (ent & ~kAmbiguousBit) : ent;
-  // the particles' own entries (lower-half ends) sit at stage indices low0 + k
-  const bool self_chunk = t0 < low0 + kNbrP && low0 < t0 + 32u;
 #pragma unroll
   for (int k = 0; k < kNbrP; ++k) {
     const unsigned m = __ballot_sync(0xffffffffu, hit[k]);
     // entries past the slot land in the buffer's last word, which is never written out
     if (hit[k]) sbuf[k * lbuf + min(cur[k] + __popc(m & lt), lbuf - 1u)] = e;
-    if (self_chunk) {
+    if (SELF) {
       const uint32_t w = low0 + static_cast<uint32_t>(k) - t0;
       if (w < 32u) half[k] = cur[k] + __popc(m & ((1u << w) - 1u));
     }
@@ -872,13 +893,20 @@ __global__ void __launch_bounds__(128)
       for (uint32_t t0 = 0; t0 < mpad; t0 += 32) {
         const float4 b = srel[t0 + lane];
         const uint32_t ent = __float_as_uint(b.w);
+        const uint32_t lb = static_cast<uint32_t>(lbuf);
+        // the particles' own entries (lower-half ends) sit at stage indices low0 + k
+        const bool self_chunk = t0 < low0 + kNbrP && low0 < t0 + 32u;
         // entries in [kAmbiguousBit, kInvalid): ghost filter undecided in FP32
-        if (__any_sync(0xffffffffu, ent - kAmbiguousBit < kInvalid - kAmbiguousBit))
-          nbr_chunk<true>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, sbuf,
-                          static_cast<uint32_t>(lbuf), cur, half);
-        else
-          nbr_chunk<false>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, sbuf,
-                           static_cast<uint32_t>(lbuf), cur, half);
+        if (__any_sync(0xffffffffu, ent - kAmbiguousBit < kInvalid - kAmbiguousBit)) {
+          if (self_chunk)
+            nbr_chunk<true, true>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, sbuf, lb, cur, half);
+          else
+            nbr_chunk<true, false>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, sbuf, lb, cur, half);
+        } else if (self_chunk) {
+          nbr_chunk<false, true>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, sbuf, lb, cur, half);
+        } else {
+          nbr_chunk<false, false>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, sbuf, lb, cur, half);
+        }
       }
       __syncwarp();
 #pragma unroll
