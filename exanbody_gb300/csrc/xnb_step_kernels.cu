@@ -129,17 +129,30 @@ __global__ void __launch_bounds__(256)
 // exponent (re-biased by -896) and the top 23 fraction bits with one funnel
 // shift, the exponent field clamped to [1, 252] so that the FP32 reciprocal is
 // a positive normal, which widens back by the inverse bit move. For d in
-// [2^-126, 2^126) the seed is within 2^-23 + 2^-24 of 1/d, and
-// the two steps take the error to 2^-44, then below the FP64 rounding.
+// [2^-126, 2^126) the seed (truncation, then the hardware FP32 reciprocal,
+// within 1 ulp) is within 2^-22 of 1/d, and the two steps take the error to
+// 2^-44, then below the FP64 rounding.
 __device__ __forceinline__ double rcp_nr(double d) {
   const int hi = min(max(__double2hiint(d) - 0x38000000, 0x00100000), 0x0fcfffff);
   const float s = __uint_as_float(__funnelshift_l(static_cast<uint32_t>(__double2loint(d)), static_cast<uint32_t>(hi), 3));
-  const uint32_t r = __float_as_uint(__frcp_rn(s));
+  float rf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(s));
+  const uint32_t r = __float_as_uint(rf);
   double y = __hiloint2double(static_cast<int>((r >> 3) + 0x38000000u), static_cast<int>(r << 29));
   double e = fma(-d, y, 1.0);
   y = fma(y, e, y);
   e = fma(-d, y, 1.0);
   return fma(y, e, y);
+}
+
+// FP32 -> FP64 widening for a finite normal or zero input in a few integer
+// operations; subnormal, infinite and NaN inputs take the general routine.
+__device__ __forceinline__ double widen_f32_fast(float f) {
+  const uint32_t u = __float_as_uint(f);
+  if ((u & 0x7f800000u) - 0x00800000u >= 0x7f000000u && (u & 0x7fffffffu) != 0u) return widen_f32(f);
+  const uint32_t mag = u & 0x7fffffffu;
+  const uint32_t hi = (mag ? (mag >> 3) + 0x38000000u : 0u) | (u & 0x80000000u);
+  return __hiloint2double(static_cast<int>(hi), static_cast<int>(u << 29));
 }
 
 // ---------------------------------------------------------------------------
@@ -270,11 +283,13 @@ __global__ void __launch_bounds__(256)
           // so a pair costs 3 DFMA + 1 DADD instead of 3 DADD + 3 DFMA; the
           // subtraction happens once per particle below (cancellation error
           // <= ~u_64 |r| sum|pd|, about 1e-12 of |F| at box sizes of 10^3 sigma).
-          const float ir2 = __frcp_rn(r2);
+          // the hardware reciprocal (within 1 ulp): part of the FP32 force magnitude
+          float ir2;
+          asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ir2) : "f"(r2));
           const float s2 = S.sig2_f * ir2;
           const float s6 = s2 * s2 * s2;
           const float pd = S.eps24_f * s6 * fmaf(-2.0f, s6, 1.0f) * ir2;
-          const double pdd = widen_f32(pd);  // exact, on the integer pipes
+          const double pdd = widen_f32_fast(pd);  // exact, on the integer pipes
           fx = fma(pdd, xb, fx);
           fy = fma(pdd, yb, fy);
           fz = fma(pdd, zb, fz);
@@ -415,10 +430,11 @@ __global__ void __launch_bounds__(256)
           in = (d2 > 0.0 && d2 <= rcut2);
         }
         if (in) {
-          const float ir2 = __frcp_rn(r2);
+          float ir2;
+          asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ir2) : "f"(r2));
           const float s2 = S.sig2_f * ir2;
           const float s6 = s2 * s2 * s2;
-          pd = widen_f32(S.eps24_f * s6 * fmaf(-2.0f, s6, 1.0f) * ir2);
+          pd = widen_f32_fast(S.eps24_f * s6 * fmaf(-2.0f, s6, 1.0f) * ir2);
           if (PE) en = static_cast<double>(fmaf(S.eps4_f * s6, s6 - 1.0f, -S.e_shift_f));
         }
       }
