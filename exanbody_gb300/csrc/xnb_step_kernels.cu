@@ -155,6 +155,62 @@ __device__ __forceinline__ double widen_f32_fast(float f) {
   return __hiloint2double(static_cast<int>(hi), static_cast<int>(u << 29));
 }
 
+// One marked entry of the mixed path: r^2 in FP32 (the compensated hi/lo
+// mirror difference for an entry in the same periodic image, the FP64
+// displacement converted for an image entry), the cutoff decided in FP32 outside
+// the proven band and in FP64 inside it, then the FP32 force factor pd and the
+// FP64 accumulation of pd * r_b and pd.
+template <bool PE>
+__device__ __forceinline__ void mixed_pair(const SysDesc& S, uint32_t e, double xb, double yb, double zb, float4 hb,
+                                           float4 lb, double xa, double ya, double za, float4 paf, float4 pal,
+                                           double rcut2, double& fx, double& fy, double& fz, double& psum,
+                                           double& pe) {
+  const uint32_t code = e & 31u;
+  float dxf, dyf, dzf;
+  if (code == static_cast<uint32_t>(kImageCenter)) {
+    // within 2u|d| of the FP64 displacement (u = 2^-24), without FP64 work
+    dxf = (hb.x - paf.x) + (lb.x - pal.x);
+    dyf = (hb.y - paf.y) + (lb.y - pal.y);
+    dzf = (hb.z - paf.z) + (lb.z - pal.z);
+  } else {
+    xb = image_coord(xb, S.period[0], static_cast<int>(code % 3u));
+    yb = image_coord(yb, S.period[1], static_cast<int>((code / 3u) % 3u));
+    zb = image_coord(zb, S.period[2], static_cast<int>(code / 9u));
+    dxf = narrow_f64(__dsub_rn(xb, xa));
+    dyf = narrow_f64(__dsub_rn(yb, ya));
+    dzf = narrow_f64(__dsub_rn(zb, za));
+  }
+  const float r2 = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
+  bool in;
+  if (r2 > S.rc2_f + S.rc_margin_f) {
+    in = false;
+  } else if (r2 < S.rc2_f - S.rc_margin_f && r2 > S.rc_margin_f) {
+    in = true;
+  } else {
+    const double d2 = norm2_rn(__dsub_rn(xb, xa), __dsub_rn(yb, ya), __dsub_rn(zb, za));
+    in = (d2 > 0.0 && d2 <= rcut2);
+  }
+  if (in) {
+    // FP64 displacement folded into the FP64 accumulation:
+    //   sum_b pd_b (r_b - r_a) = sum_b pd_b r_b - r_a sum_b pd_b,
+    // so a pair costs 3 DFMA + 1 DADD instead of 3 DADD + 3 DFMA; the
+    // subtraction happens once per particle (cancellation error
+    // <= ~u_64 |r| sum|pd|, about 1e-12 of |F| at box sizes of 10^3 sigma).
+    // The hardware reciprocal (within 1 ulp) is part of the FP32 force magnitude.
+    float ir2;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ir2) : "f"(r2));
+    const float s2 = S.sig2_f * ir2;
+    const float s6 = s2 * s2 * s2;
+    const float pd = S.eps24_f * s6 * fmaf(-2.0f, s6, 1.0f) * ir2;
+    const double pdd = widen_f32_fast(pd);  // exact, on the integer pipes
+    fx = fma(pdd, xb, fx);
+    fy = fma(pdd, yb, fy);
+    fz = fma(pdd, zb, fz);
+    psum += pdd;
+    if (PE) pe += static_cast<double>(0.5f * fmaf(S.eps4_f * s6, s6 - 1.0f, -S.e_shift_f));
+  }
+}
+
 // ---------------------------------------------------------------------------
 // zero_particle_force + lennard_jones_force over the neighbour lists.
 // compute_cell_particle_pairs_cell (compute/include/exanb/compute/
@@ -175,7 +231,9 @@ __device__ __forceinline__ double widen_f32_fast(float f) {
 //                    and the FP32 factor is widened on the integer pipes: a
 //                    pair costs 3 DFMA + 1 DADD on the FP64 pipe.
 template <int P, bool PE, bool KICK>
-__global__ void __launch_bounds__(256)
+// 72 registers: 7 blocks of 128 threads per SM (measured faster than the
+// unconstrained 79 despite a few spilled bytes).
+__global__ void __maxnreg__(72)
     k_force(uint32_t n_part, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a,
             int sys_only) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
@@ -200,104 +258,82 @@ __global__ void __launch_bounds__(256)
     // Windows of 128 entries: the FP32 prefilter marks the entries that may lie
     // within rc, then the FP64 block runs for the marked ones in list order, so
     // a warp executes it as often as its busiest lane has marked entries.
-    for (uint32_t kw = 0; kw < n; kw += 128) {
-     Marks mk = prefilter_window(L, kw, min(n, kw + 128u), a.pf, pbase, self_e, paf, pfx, pfy, pfz, pre_hi);
-     uint32_t b;
-     while (next_mark(mk, b)) {
-      const uint32_t e = __ldg(L + kw + b);
-      const uint32_t j = pbase + (e >> 5);
-      const uint32_t code = e & 31u;
-      double xb = __ldg(a.rx + j), yb = __ldg(a.ry + j), zb = __ldg(a.rz + j);
-      if (code != static_cast<uint32_t>(kImageCenter)) {
-        xb = image_coord(xb, px, static_cast<int>(code % 3u));
-        yb = image_coord(yb, py, static_cast<int>((code / 3u) % 3u));
-        zb = image_coord(zb, pz, static_cast<int>(code / 9u));
+    if (P == kMixed) {
+      // Two marked entries per iteration: their list entries, then their five
+      // gathers each, are in flight together (list order is kept: b0 < b1).
+      for (uint32_t kw = 0; kw < n; kw += 128) {
+        Marks mk = prefilter_window(L, kw, min(n, kw + 128u), a.pf, pbase, self_e, paf, pfx, pfy, pfz, pre_hi);
+        uint32_t b0 = 0, b1 = 0;
+        bool h0 = next_mark(mk, b0);
+        while (h0) {
+          const bool h1 = next_mark(mk, b1);
+          const uint32_t e0 = __ldg(L + kw + b0);
+          const uint32_t e1 = __ldg(L + kw + (h1 ? b1 : b0));
+          const uint32_t j0 = pbase + (e0 >> 5), j1 = pbase + (e1 >> 5);
+          const double x0 = __ldg(a.rx + j0), y0 = __ldg(a.ry + j0), z0 = __ldg(a.rz + j0);
+          const double x1 = __ldg(a.rx + j1), y1 = __ldg(a.ry + j1), z1 = __ldg(a.rz + j1);
+          const float4 hi0 = __ldg(a.pf + j0), lo0 = __ldg(a.pflo + j0);
+          const float4 hi1 = __ldg(a.pf + j1), lo1 = __ldg(a.pflo + j1);
+          mixed_pair<PE>(S, e0, x0, y0, z0, hi0, lo0, xa, ya, za, paf, pal, rcut2, fx, fy, fz, psum, pe);
+          if (h1) mixed_pair<PE>(S, e1, x1, y1, z1, hi1, lo1, xa, ya, za, paf, pal, rcut2, fx, fy, fz, psum, pe);
+          h0 = h1 && next_mark(mk, b0);
+        }
       }
-      if (P == kFp64Exact) {
-        const double dx = __dsub_rn(xb, xa);
-        const double dy = __dsub_rn(yb, ya);
-        const double dz = __dsub_rn(zb, za);
-        const double d2 = norm2_rn(dx, dy, dz);
-        if (d2 > 0.0 && d2 <= rcut2) {
-          // lj_compute_energy (lennard_jones.cu:46-56) then pair_de *= w / r with w = 1
-          const double r = __dsqrt_rn(d2);
-          const double inv_r = __ddiv_rn(1.0, r);
-          const double ratio = __dmul_rn(S.sigma, inv_r);
-          const double ratio2 = __dmul_rn(ratio, ratio);
-          const double ratio6 = __dmul_rn(__dmul_rn(ratio2, ratio2), ratio2);
-          const double ratio12 = __dmul_rn(ratio6, ratio6);
-          double de = __dmul_rn(__dmul_rn(S.m24eps, __dsub_rn(__dmul_rn(2.0, ratio12), ratio6)), inv_r);
-          de = __dmul_rn(de, inv_r);
-          fx = __dadd_rn(fx, __dmul_rn(de, dx));
-          fy = __dadd_rn(fy, __dmul_rn(de, dy));
-          fz = __dadd_rn(fz, __dmul_rn(de, dz));
-          if (PE) {
-            const double en = __dmul_rn(S.eps4, __dsub_rn(ratio12, ratio6));
-            pe = __dadd_rn(pe, __dmul_rn(0.5, __dsub_rn(en, S.e_shift)));
+    } else {
+      for (uint32_t kw = 0; kw < n; kw += 128) {
+       Marks mk = prefilter_window(L, kw, min(n, kw + 128u), a.pf, pbase, self_e, paf, pfx, pfy, pfz, pre_hi);
+       uint32_t b;
+       while (next_mark(mk, b)) {
+        const uint32_t e = __ldg(L + kw + b);
+        const uint32_t j = pbase + (e >> 5);
+        const uint32_t code = e & 31u;
+        double xb = __ldg(a.rx + j), yb = __ldg(a.ry + j), zb = __ldg(a.rz + j);
+        if (code != static_cast<uint32_t>(kImageCenter)) {
+          xb = image_coord(xb, px, static_cast<int>(code % 3u));
+          yb = image_coord(yb, py, static_cast<int>((code / 3u) % 3u));
+          zb = image_coord(zb, pz, static_cast<int>(code / 9u));
+        }
+        if (P == kFp64Exact) {
+          const double dx = __dsub_rn(xb, xa);
+          const double dy = __dsub_rn(yb, ya);
+          const double dz = __dsub_rn(zb, za);
+          const double d2 = norm2_rn(dx, dy, dz);
+          if (d2 > 0.0 && d2 <= rcut2) {
+            // lj_compute_energy (lennard_jones.cu:46-56) then pair_de *= w / r with w = 1
+            const double r = __dsqrt_rn(d2);
+            const double inv_r = __ddiv_rn(1.0, r);
+            const double ratio = __dmul_rn(S.sigma, inv_r);
+            const double ratio2 = __dmul_rn(ratio, ratio);
+            const double ratio6 = __dmul_rn(__dmul_rn(ratio2, ratio2), ratio2);
+            const double ratio12 = __dmul_rn(ratio6, ratio6);
+            double de = __dmul_rn(__dmul_rn(S.m24eps, __dsub_rn(__dmul_rn(2.0, ratio12), ratio6)), inv_r);
+            de = __dmul_rn(de, inv_r);
+            fx = __dadd_rn(fx, __dmul_rn(de, dx));
+            fy = __dadd_rn(fy, __dmul_rn(de, dy));
+            fz = __dadd_rn(fz, __dmul_rn(de, dz));
+            if (PE) {
+              const double en = __dmul_rn(S.eps4, __dsub_rn(ratio12, ratio6));
+              pe = __dadd_rn(pe, __dmul_rn(0.5, __dsub_rn(en, S.e_shift)));
+            }
+          }
+        } else if (P == kFp64) {
+          const double dx = __dsub_rn(xb, xa);
+          const double dy = __dsub_rn(yb, ya);
+          const double dz = __dsub_rn(zb, za);
+          const double d2 = norm2_rn(dx, dy, dz);
+          if (d2 > 0.0 && d2 <= rcut2) {
+            const double ir2 = rcp_nr(d2);
+            const double s2 = S.sig2 * ir2;
+            const double s6 = s2 * s2 * s2;
+            const double pd = S.eps24 * s6 * fma(-2.0, s6, 1.0) * ir2;
+            fx = fma(pd, dx, fx);
+            fy = fma(pd, dy, fy);
+            fz = fma(pd, dz, fz);
+            if (PE) pe += 0.5 * fma(S.eps4 * s6, s6 - 1.0, -S.e_shift);
           }
         }
-      } else if (P == kFp64) {
-        const double dx = __dsub_rn(xb, xa);
-        const double dy = __dsub_rn(yb, ya);
-        const double dz = __dsub_rn(zb, za);
-        const double d2 = norm2_rn(dx, dy, dz);
-        if (d2 > 0.0 && d2 <= rcut2) {
-          const double ir2 = rcp_nr(d2);
-          const double s2 = S.sig2 * ir2;
-          const double s6 = s2 * s2 * s2;
-          const double pd = S.eps24 * s6 * fma(-2.0, s6, 1.0) * ir2;
-          fx = fma(pd, dx, fx);
-          fy = fma(pd, dy, fy);
-          fz = fma(pd, dz, fz);
-          if (PE) pe += 0.5 * fma(S.eps4 * s6, s6 - 1.0, -S.e_shift);
-        }
-      } else {
-        // r^2 in FP32. For an entry in the same periodic image, the compensated
-        // difference (hi_b - hi_a) + (lo_b - lo_a) of the FP32 hi/lo mirrors is
-        // within 2u|d| of the FP64 displacement (u = 2^-24), as close as
-        // converting it, without FP64 work; image entries convert the FP64 one.
-        float dxf, dyf, dzf;
-        if (code == static_cast<uint32_t>(kImageCenter)) {
-          const float4 hb = __ldg(a.pf + j), lb = __ldg(a.pflo + j);
-          dxf = (hb.x - paf.x) + (lb.x - pal.x);
-          dyf = (hb.y - paf.y) + (lb.y - pal.y);
-          dzf = (hb.z - paf.z) + (lb.z - pal.z);
-        } else {
-          dxf = narrow_f64(__dsub_rn(xb, xa));
-          dyf = narrow_f64(__dsub_rn(yb, ya));
-          dzf = narrow_f64(__dsub_rn(zb, za));
-        }
-        const float r2 = fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf));
-        bool in;
-        if (r2 > S.rc2_f + S.rc_margin_f) {
-          in = false;
-        } else if (r2 < S.rc2_f - S.rc_margin_f && r2 > S.rc_margin_f) {
-          in = true;
-        } else {
-          const double d2 = norm2_rn(__dsub_rn(xb, xa), __dsub_rn(yb, ya), __dsub_rn(zb, za));
-          in = (d2 > 0.0 && d2 <= rcut2);
-        }
-        if (in) {
-          // FP64 displacement folded into the FP64 accumulation:
-          //   sum_b pd_b (r_b - r_a) = sum_b pd_b r_b - r_a sum_b pd_b,
-          // so a pair costs 3 DFMA + 1 DADD instead of 3 DADD + 3 DFMA; the
-          // subtraction happens once per particle below (cancellation error
-          // <= ~u_64 |r| sum|pd|, about 1e-12 of |F| at box sizes of 10^3 sigma).
-          // the hardware reciprocal (within 1 ulp): part of the FP32 force magnitude
-          float ir2;
-          asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ir2) : "f"(r2));
-          const float s2 = S.sig2_f * ir2;
-          const float s6 = s2 * s2 * s2;
-          const float pd = S.eps24_f * s6 * fmaf(-2.0f, s6, 1.0f) * ir2;
-          const double pdd = widen_f32_fast(pd);  // exact, on the integer pipes
-          fx = fma(pdd, xb, fx);
-          fy = fma(pdd, yb, fy);
-          fz = fma(pdd, zb, fz);
-          psum += pdd;
-          if (PE) pe += static_cast<double>(0.5f * fmaf(S.eps4_f * s6, s6 - 1.0f, -S.e_shift_f));
-        }
+       }
       }
-     }
     }
     if (P == kMixed) {
       fx = fma(-xa, psum, fx);
