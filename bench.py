@@ -323,7 +323,22 @@ def run_ours(args):
     ms_force64 = timed(lambda: b.lennard_jones_force(s, FP64, False), 3) / 3
     peak64 = fp64_peak_tflops(torch, dev)
     achieved = FLOP64_PER_ATOM_MIXED * N / (ms_force * 1e-3) / 1e12
+    # ---- the rebuild path's parts, each call host-synchronised like the operator ----
+    ms_nbr = timed(lambda: b.chunk_neighbors(s), 5) / 5
+    ms_upd = timed(lambda: b.update_particles_full(s), 5) / 5
+    b.check_errors()
     b.close()
+    step_phases = {
+        "force_only_mixed": {"ms": ms_force, "atom_steps_per_s": N / (ms_force * 1e-3)},
+        "force_only_fp64": {"ms": ms_force64, "atom_steps_per_s": N / (ms_force64 * 1e-3),
+                            "traversal": "newton" if FP64 & xnb.PREC_NEWTON else "full"},
+        "neighbour_build_ms_per_rebuild": ms_nbr,
+        "rebuild_path_ms_per_rebuild": ms_upd,
+        "rebuilds_in_timed_steps": rebuilds,
+        "note": "force-only: lennard_jones_force on the post-run state; neighbour build: xnb_chunk_neighbors "
+                "(rebuild mark + one-pass list build); rebuild path: xnb_update_particles_full (rebin, backup, "
+                "list build); CUDA events around each call",
+    }
 
     # ---- end to end through the C ABI: host arrays in, K steps, host arrays out ----
     e2e = None
@@ -392,9 +407,18 @@ def run_ours(args):
         for _ in range(sample):
             so.step()
         dt = time.perf_counter() - t0
+        reb = so.rebuilds - r0
+        t0 = time.perf_counter()
+        so.compute_forces()
+        dt_force = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        so.chunk_neighbors()
+        dt_nbr = time.perf_counter() - t0
         cpu = {"value": N * sample / dt, "unit": "atom-steps/s", "cores": used, "kind": "port",
                "sample": "%d MD steps of the same %d-atom system after init (%d rebuilds), oracle OpenMP build"
-                         % (sample, N, so.rebuilds - r0)}
+                         % (sample, N, reb),
+               "phases": {"force_only_atom_steps_per_s": N / dt_force, "neighbour_build_ms_per_rebuild": dt_nbr * 1e3,
+                          "rebuilds_in_sample": reb}}
         del so
 
     if rank == 0:
@@ -419,6 +443,7 @@ def run_ours(args):
                                chosen={"mixed": "newton" if MIXED & xnb.PREC_NEWTON else "full",
                                        "fp64": "newton" if FP64 & xnb.PREC_NEWTON else "full"}),
             "force_error_mixed_vs_fp64": {"max": err_max, "rms": err_rms, "tolerance": 1e-5},
+            "phases": step_phases,
             "clocks": clocks,
             "e2e": e2e,
             "gpu_launches": launches,

@@ -49,6 +49,8 @@ def _lib(kind="parity"):
     lib.xo_set_snap.argtypes = [C.c_void_p, i32, d, d, d, i32, i32, i32, P(d), P(d), i32, P(d), d, i32]
     lib.xo_init.argtypes = [C.c_void_p]
     lib.xo_step.argtypes = [C.c_void_p]
+    lib.xo_compute_forces.argtypes = [C.c_void_p]
+    lib.xo_chunk_neighbors.argtypes = [C.c_void_p]
     for f in ("xo_num_particles", "xo_rebuild_count", "xo_num_cells", "xo_pair_count", "xo_displ_over_count"):
         getattr(lib, f).restype = i64
         getattr(lib, f).argtypes = [C.c_void_p]
@@ -139,6 +141,16 @@ class OracleSystem:
         if rc < 0:
             raise RuntimeError("oracle step failed: %d" % rc)
         return rc
+
+    def compute_forces(self):
+        """The force pass alone on the current state (CPU-baseline timing)."""
+        if self.lib.xo_compute_forces(self.h) != 0:
+            raise RuntimeError("oracle force pass failed")
+
+    def chunk_neighbors(self):
+        """The neighbour build alone on the current state (CPU-baseline timing)."""
+        if self.lib.xo_chunk_neighbors(self.h) != 0:
+            raise RuntimeError("oracle neighbour build failed")
 
     @property
     def n(self):

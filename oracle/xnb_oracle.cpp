@@ -999,6 +999,19 @@ int xo_step(xo_sys* s) {
   return rebuilt;
 }
 
+/* Timing hooks of the CPU baseline, on an initialised state: the force pass
+ * alone (zero_particle_force + lennard_jones_force) and the neighbour build alone
+ * (chunk_neighbors over the current grid and ghosts). Neither moves particles. */
+int xo_compute_forces(xo_sys* s) {
+  if (!s || !s->ready) return -1;
+  return s->compute_forces();
+}
+
+int xo_chunk_neighbors(xo_sys* s) {
+  if (!s || !s->ready) return -1;
+  return s->chunk_neighbors();
+}
+
 int64_t xo_num_particles(const xo_sys* s) {
   int64_t n = 0;
   for (size_t c = 0; c < s->cells.size(); ++c)

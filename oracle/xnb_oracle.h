@@ -63,6 +63,8 @@ int xo_init(xo_sys* s);
 /* One numerical_scheme step (numerical-scheme.msp:21-25). Returns 1 if the
  * neighbour lists were rebuilt during this step, 0 if not, <0 on error. */
 int xo_step(xo_sys* s);
+int xo_compute_forces(xo_sys* s);   /* force pass alone, on an initialised state */
+int xo_chunk_neighbors(xo_sys* s);  /* neighbour build alone, on an initialised state */
 
 int64_t xo_num_particles(const xo_sys* s);
 int64_t xo_rebuild_count(const xo_sys* s);

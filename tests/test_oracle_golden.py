@@ -126,6 +126,22 @@ def test_neighbor_set_matches_brute_force_at_build():
         assert set(zip(a.tolist(), b.tolist())) == brute_force_pairs(P, w["geom"], 2.8)
 
 
+def test_timing_hooks_leave_the_state_unchanged():
+    """The CPU baseline times the force pass and the neighbour build alone on the
+    current state: both recompute what the state already holds."""
+    s, w = small_lj(n=6)
+    s.init()
+    s.step()
+    P0, pairs0 = s.particles(), s.pairs()
+    s.compute_forces()
+    s.chunk_neighbors()
+    P1, pairs1 = s.particles(), s.pairs()
+    for k in ("rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz"):
+        assert np.array_equal(P0[k], P1[k]), k
+    for x, y in zip(pairs0, pairs1):
+        assert np.array_equal(x, y)
+
+
 def test_stream_format_and_sorted_order():
     s, w = small_lj(n=6)
     s.init()
