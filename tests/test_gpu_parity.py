@@ -149,6 +149,25 @@ def test_stage_cap_splits_cells_between_builds(cap):
     assert e <= FP64_TOL, e
 
 
+@pytest.mark.parametrize("list_factor", [8.0, 12.0])
+def test_large_slots_take_the_block_build(list_factor):
+    """Slots above 512 entries leave every cell to the block-per-cell build: its
+    shared-memory list buffer up to 1024 entries (factor 8: ~760), direct global
+    writes above (factor 12: ~1130). Lists and trajectories stay the oracle's."""
+    w = workloads.lj_fcc_system(8, 0.8442, 1.44, 31)
+    b = new_batch([w["n_atoms"]], [ncells(w["geom"])], list_per_atom=1300.0)
+    s = b.add_system(xnb.lj_params(w["geom"]), w["r"], w["v"], w["id"], list_factor=list_factor)
+    b.init_particles(s, xnb.PREC_FP64_EXACT)
+    o = oracle_from(w)
+    o.init()
+    compare_pairs(b, s, o)
+    for _ in range(20):
+        b.step(1, xnb.PREC_FP64_EXACT, xnb.STEP_HOST_SYNC)
+        if o.step():
+            compare_pairs(b, s, o)
+    assert_bitwise_equal(b.download(s), o.particles())
+
+
 def test_slab_with_empty_cells_bit_exact():
     w = workloads.lj_slab_system(8, 0.8442, 0.8, 5)
     b, s = gpu_system(w)
