@@ -398,7 +398,7 @@ def run_ours(args):
                       % args.steps, "phases": phases}
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:  # the CPU baseline is an N=1 figure
         threads = os.cpu_count() or 1
         so, used = cpu_oracle_run(w, 0, threads)
         sample = 10
@@ -645,7 +645,7 @@ def run_snap(args):
                       % steps}
         del out
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:  # the CPU baseline is an N=1 figure
         from oracle.oracle import OracleSystem
 
         so = OracleSystem((0, 0, 0), (L, L, L), geom["dims"], geom["cell_size"], cfg["rcutfac"], 2.0, 1.0, 1.0,
