@@ -13,7 +13,7 @@
 namespace xnb {
 
 // Exact IEEE 754 binary32 -> binary64 widening done on the integer pipes, so
-// that it costs no FP64 issue slot (GB300 issues FP64 at ~1/40 of the FP32/INT
+// that it costs no FP64 issue slot (GB300 issues FP64 at ~1/74 of the FP32/INT
 // rate). The binary64 fields follow from the binary32 ones: sign kept, exponent
 // re-biased from 127 to 1023 (+896), the 23 fraction bits placed at the top of
 // the 52-bit fraction. A subnormal input m * 2^-149 is normalised first: with
