@@ -183,6 +183,11 @@ SysDesc make_desc(const xnb_lj_params& p) {
     d.period[a] = p.extent[a] - p.origin[a];
     d.dims[a] = p.dims[a];
   }
+  // +0 only: x - (+0) is x for every x (including -0); x - (-0) would turn -0 into +0
+  d.origin_zero = (p.origin[0] == 0.0 && !std::signbit(p.origin[0]) && p.origin[1] == 0.0 &&
+                   !std::signbit(p.origin[1]) && p.origin[2] == 0.0 && !std::signbit(p.origin[2]))
+                      ? 1
+                      : 0;
   d.cell_size = p.cell_size;
   const double ghost_dist = (p.rcut + p.rcut_inc) / 1.0;  // nbh_dist.cpp:63-65
   for (int a = 0; a < 3; ++a) {

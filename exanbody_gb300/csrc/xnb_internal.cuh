@@ -66,6 +66,7 @@ struct SysDesc {
   int32_t dims[3];
   int32_t divide_by_mass;
   int32_t amr_enabled;
+  int32_t origin_zero;  // origin is (+0, +0, +0): x - origin is x itself, no subtraction needed
   uint32_t cell_base, ncells;
   uint32_t part_base, npart;
   uint64_t list_base;  // first entry of the system's list segment
@@ -192,10 +193,16 @@ __device__ __forceinline__ double widen_f32(float f);
 // its residual (DevArrays::pflo): hi = fl32(x - o), lo = fl32((x - o) - hi).
 // Only the two subtractions per coordinate use the FP64 pipe.
 __device__ __forceinline__ float4 make_pf(const SysDesc& s, double x, double y, double z) {
+  if (s.origin_zero) return make_float4(narrow_f64(x), narrow_f64(y), narrow_f64(z), 0.f);
   return make_float4(narrow_f64(x - s.origin[0]), narrow_f64(y - s.origin[1]), narrow_f64(z - s.origin[2]), 0.f);
 }
 __device__ __forceinline__ void make_pf2(const SysDesc& s, double x, double y, double z, float4& hi, float4& lo) {
-  const double rx = x - s.origin[0], ry = y - s.origin[1], rz = z - s.origin[2];
+  double rx = x, ry = y, rz = z;
+  if (!s.origin_zero) {
+    rx = x - s.origin[0];
+    ry = y - s.origin[1];
+    rz = z - s.origin[2];
+  }
   hi = make_float4(narrow_f64(rx), narrow_f64(ry), narrow_f64(rz), 0.f);
   lo = make_float4(narrow_f64(rx - widen_f32(hi.x)), narrow_f64(ry - widen_f32(hi.y)), narrow_f64(rz - widen_f32(hi.z)),
                    0.f);

@@ -59,9 +59,10 @@ __global__ void __launch_bounds__(256)
           y = __dadd_rn(y, __dadd_rn(__dmul_rn(vy, dt), __dmul_rn(fy, dt2)));
           z = __dadd_rn(z, __dadd_rn(__dmul_rn(vz, dt), __dmul_rn(fz, dt2)));
         } else {
-          x += fma(vx, dt, fx * dt2);
-          y += fma(vy, dt, fy * dt2);
-          z += fma(vz, dt, fz * dt2);
+          // r + v dt + f dt^2/2 as two nested FMAs (two roundings, two FP64 instructions)
+          x = fma(fx, dt2, fma(vx, dt, x));
+          y = fma(fy, dt2, fma(vy, dt, y));
+          z = fma(fz, dt2, fma(vz, dt, z));
         }
         a.rx[i] = x;
         a.ry[i] = y;
