@@ -85,7 +85,8 @@ typedef struct xnb_batch_config {
   int64_t particle_capacity; /* particles over all resident systems */
   int64_t cell_capacity;     /* cells over all resident systems */
   int64_t list_capacity;     /* neighbour entries over all resident systems */
-  int32_t stage_cap;         /* neighbour-build candidates staged per cell round (<= 1024); 0 = default (640) */
+  int32_t stage_cap;         /* neighbour-build candidates staged per cell (<= 1024): cells with more go to the
+                                block-per-cell build, in rounds of this size; 0 = default (640) */
   int32_t force_block;       /* threads per block of the full-list force traversal; 0 = default (128) */
 } xnb_batch_config;
 
@@ -183,7 +184,7 @@ int64_t xnb_stats_kernel_launches(const xnb_batch* b);
 /* ---- tuning ---- */
 
 typedef struct xnb_tuning {
-  int32_t stage_cap;          /* neighbour-build candidates staged per cell round */
+  int32_t stage_cap;          /* neighbour-build candidates staged per cell (see xnb_batch_config) */
   int32_t force_block;        /* threads per block of the full-list force traversal */
   int32_t newton;             /* 1: XNB_PREC_NEWTON traversal */
   int32_t trials;             /* configurations timed */
