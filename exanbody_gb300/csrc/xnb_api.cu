@@ -244,6 +244,16 @@ SysDesc make_desc(const xnb_lj_params& p) {
   d.divide_by_mass = p.divide_by_mass;
   d.amr_enabled = p.amr_enabled;
   d.sub_grid_density = p.sub_grid_density > 0 ? p.sub_grid_density : 6.5;
+  {
+    // sub_grid_side returns 1 while the rounded quotient n / density stays below
+    // 8; the same IEEE division here gives the first count where it does not
+    double n0 = std::floor(8.0 * d.sub_grid_density) - 2.0;
+    if (!(n0 >= 1.0)) n0 = 1.0;
+    uint64_t n = static_cast<uint64_t>(std::min(n0, 4294967295.0));
+    while (n < 4294967295ull && static_cast<double>(n) / d.sub_grid_density < 8.0) ++n;
+    while (n > 1 && static_cast<double>(n - 1) / d.sub_grid_density >= 8.0) --n;
+    d.amr_min_n = static_cast<uint32_t>(n);
+  }
   d.dt = p.dt;
   d.dt_full = p.dt * 1.0;
   d.dt_sq_half = d.dt_full * d.dt_full * 0.5;

@@ -297,11 +297,13 @@ __global__ void __launch_bounds__(128)
     const uint32_t ns = S.part_base + static_cast<uint32_t>(a.cell_scan[c] - a.cell_scan[S.cell_base]);
     const uint32_t n = a.cell_cnt[c];
     int ci, cj, ck;
-    cell_ijk(S, c - S.cell_base, ci, cj, ck);
-    const double lo[3] = {cell_lo(S, 0, ci), cell_lo(S, 1, cj), cell_lo(S, 2, ck)};
-    const int side = S.amr_enabled ? sub_grid_side(n, S.sub_grid_density) : 1;
+    // the FP64 division of sub_grid_side only for counts that can give a side > 1
+    // (a warp-wide FP64 instruction costs the same for one lane as for 32)
+    const int side = (S.amr_enabled && n >= S.amr_min_n) ? sub_grid_side(n, S.sub_grid_density) : 1;
     // backup_r runs afterwards in k_backup, one thread per particle
     if (side > 1) {
+      cell_ijk(S, c - S.cell_base, ci, cj, ck);
+      const double lo[3] = {cell_lo(S, 0, ci), cell_lo(S, 1, cj), cell_lo(S, 2, ck)};
       // sub-cell key of each particle (Grid::particle_pcoord, grid.h:184-190), kept in pdest
       for (uint32_t q = lane; q < n; q += 32) {
         const double r[3] = {a.t_rx[ns + q], a.t_ry[ns + q], a.t_rz[ns + q]};

@@ -47,6 +47,7 @@ struct SysDesc {
   double dt;
   double dt_full, dt_sq_half, dt_half;  // dt*1.0, (dt*dt)*0.5, dt*0.5 (push_vec3_2nd_order.h:87-88)
   double sub_grid_density;
+  uint32_t amr_min_n;    // smallest cell count n with fl(n / sub_grid_density) >= 8: below it the sub-grid side is 1
   float nbh2_f, nbh_margin_f;  // FP32 prefilter of the neighbour test and its proven error margin
   float rc2_f, rc_margin_f;    // same for the force cutoff test (mixed path)
   float sig2_f, eps24_f, eps4_f, e_shift_f;
