@@ -168,6 +168,27 @@ def test_large_slots_take_the_block_build(list_factor):
     assert_bitwise_equal(b.download(s), o.particles())
 
 
+def test_warp_build_cells_above_32_particles():
+    """Cells of more than 32 particles whose candidates still fit the warp's
+    stage: the warp build loads those particles' mirrors per pass instead of
+    shuffling them across lanes. 3^3 cells of 3 sigma with ~25 uniformly random
+    particles each (Poisson counts up to ~40), stage 1024: the oracle's lists."""
+    rng = np.random.default_rng(7)
+    geom = workloads.geometry((9.0, 9.0, 9.0))
+    assert tuple(geom["dims"]) == (3, 3, 3)
+    n = 675
+    w = {"r": rng.uniform(0.0, 9.0, (n, 3)), "v": rng.normal(0.0, 0.1, (n, 3)),
+         "id": np.arange(n, dtype=np.uint64), "geom": geom, "n_atoms": n}
+    b, s = gpu_system(w)
+    b.set_tuning(1024, 128)
+    b.init_particles(s, xnb.PREC_FP64_EXACT)
+    o = oracle_from(w)
+    o.init()
+    assert o.cell_counts().max() > 32
+    compare_pairs(b, s, o)
+    assert_bitwise_equal(b.download(s), o.particles())
+
+
 def test_slab_with_empty_cells_bit_exact():
     w = workloads.lj_slab_system(8, 0.8442, 0.8, 5)
     b, s = gpu_system(w)
