@@ -189,6 +189,35 @@ def test_warp_build_cells_above_32_particles():
     assert_bitwise_equal(b.download(s), o.particles())
 
 
+@pytest.mark.parametrize("cap", [640, 1024])
+def test_ghost_filter_and_cutoff_boundaries_bit_exact(cap):
+    """Periodic images placed on the ghost-filter bound (outer_lo = -nbh) and
+    pairs placed on nbh itself, ulps apart: the FP32 tests are undecided there,
+    so both builds take the reference's FP64 decisions (block build at stage
+    640 < 691 candidates, warp build at 1024). The lists stay the oracle's."""
+    rng = np.random.default_rng(11)
+    geom = workloads.geometry((9.0, 9.0, 9.0))
+    r = [rng.uniform(0.0, 9.0, (675, 3))]
+    yz = rng.uniform(0.5, 8.5, (8, 2))
+    xb = 9.0 - 2.8
+    for k in range(8):
+        # b's image through the -x wall sits ulps from -2.8; a at x = 0 faces it at ~2.8
+        x = xb
+        for _ in range(k - 4 if k >= 4 else 4 - k):
+            x = np.nextafter(x, np.inf if k >= 4 else -np.inf)
+        r.append(np.array([[0.0, yz[k, 0], yz[k, 1]], [x, yz[k, 0], yz[k, 1]]]))
+    r = np.concatenate(r)
+    n = len(r)
+    w = {"r": r, "v": np.zeros((n, 3)), "id": np.arange(n, dtype=np.uint64), "geom": geom, "n_atoms": n}
+    b, s = gpu_system(w)
+    b.set_tuning(cap, 128)
+    b.init_particles(s, xnb.PREC_FP64_EXACT)
+    o = oracle_from(w)
+    o.init()
+    compare_pairs(b, s, o)
+    assert_bitwise_equal(b.download(s), o.particles())
+
+
 def test_slab_with_empty_cells_bit_exact():
     w = workloads.lj_slab_system(8, 0.8442, 0.8, 5)
     b, s = gpu_system(w)
