@@ -218,6 +218,39 @@ def test_ghost_filter_and_cutoff_boundaries_bit_exact(cap):
     assert_bitwise_equal(b.download(s), o.particles())
 
 
+def test_mixed_pair_set_at_the_cutoff():
+    """Isolated pairs at rc shifted by 0..4 ulps either way: each particle's force
+    is its one pair force or zero, so the mixed path's FP32 cutoff test (FP64
+    inside its error band) must select exactly the FP64 pairs; the FP64-exact
+    forces stay the oracle's bits."""
+    geom = workloads.geometry((12.0, 12.0, 12.0))
+    pts = []
+    for k in range(8):
+        a = np.array([1.0 + (k % 2) * 6.0, 1.0 + ((k // 2) % 2) * 6.0, 1.0 + (k // 4) * 6.0])
+        x = a[0] + 2.5
+        for _ in range(abs(k - 4)):
+            x = np.nextafter(x, np.inf if k >= 4 else -np.inf)
+        pts += [a, np.array([x, a[1], a[2]])]
+    r = np.array(pts)
+    n = len(r)
+    w = {"r": r, "v": np.zeros((n, 3)), "id": np.arange(n, dtype=np.uint64), "geom": geom, "n_atoms": n}
+    b, s = gpu_system(w)
+    b.init_particles(s, xnb.PREC_FP64_EXACT)
+    o = oracle_from(w)
+    o.init()
+    assert_bitwise_equal(b.download(s), o.particles())
+    b.lennard_jones_force(s, xnb.PREC_FP64, False)
+    f64 = forces(b.download(s))
+    b.lennard_jones_force(s, xnb.PREC_MIXED, False)
+    fmx = forces(b.download(s))
+    in64 = np.linalg.norm(f64, axis=1) > 0
+    inmx = np.linalg.norm(fmx, axis=1) > 0
+    assert np.array_equal(in64, inmx)
+    assert 0 < in64.sum() < n  # pairs on both sides of rc
+    e, _ = force_error(fmx, f64)
+    assert e <= MIXED_TOL, e
+
+
 def test_slab_with_empty_cells_bit_exact():
     w = workloads.lj_slab_system(8, 0.8442, 0.8, 5)
     b, s = gpu_system(w)
