@@ -222,5 +222,8 @@ __device__ __forceinline__ double image_coord(double x, double period, int d) {
 __device__ __forceinline__ double widen_f32(float f) {
   return __longlong_as_double(static_cast<long long>(widen_f32_bits(__float_as_uint(f))));
 }
+__device__ __forceinline__ double widen_f32_fast(float f) {
+  return __longlong_as_double(static_cast<long long>(widen_f32_fast_bits(__float_as_uint(f))));
+}
 
 }  // namespace xnb

@@ -146,16 +146,6 @@ __device__ __forceinline__ double rcp_nr(double d) {
   return fma(y, e, y);
 }
 
-// FP32 -> FP64 widening for a finite normal or zero input in a few integer
-// operations; subnormal, infinite and NaN inputs take the general routine.
-__device__ __forceinline__ double widen_f32_fast(float f) {
-  const uint32_t u = __float_as_uint(f);
-  if ((u & 0x7f800000u) - 0x00800000u >= 0x7f000000u && (u & 0x7fffffffu) != 0u) return widen_f32(f);
-  const uint32_t mag = u & 0x7fffffffu;
-  const uint32_t hi = (mag ? (mag >> 3) + 0x38000000u : 0u) | (u & 0x80000000u);
-  return __hiloint2double(static_cast<int>(hi), static_cast<int>(u << 29));
-}
-
 // One marked entry of the mixed path: r^2 in FP32 (the compensated hi/lo
 // mirror difference for an entry in the same periodic image, the FP64
 // displacement converted for an image entry), the cutoff decided in FP32 outside

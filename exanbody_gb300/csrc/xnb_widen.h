@@ -41,6 +41,16 @@ XNB_HD uint64_t widen_f32_bits(uint32_t u) {
   return (static_cast<uint64_t>(hi) << 32) | static_cast<uint64_t>(u << 29);
 }
 
+// The same widening with a short path for finite normal inputs and zeros (the
+// FP32 pair-force factor of the mixed kernels): the exponent re-bias and the
+// fraction move only. Subnormal, infinite and NaN inputs take widen_f32_bits.
+XNB_HD uint64_t widen_f32_fast_bits(uint32_t u) {
+  if ((u & 0x7f800000u) - 0x00800000u >= 0x7f000000u && (u & 0x7fffffffu) != 0u) return widen_f32_bits(u);
+  const uint32_t mag = u & 0x7fffffffu;
+  const uint32_t hi = (mag ? (mag >> 3) + 0x38000000u : 0u) | (u & 0x80000000u);
+  return (static_cast<uint64_t>(hi) << 32) | static_cast<uint64_t>(u << 29);
+}
+
 // IEEE 754 binary64 -> binary32 conversion, round to nearest (ties to even), on
 // integer operations (the hardware conversion occupies the FP64 pipe). With
 // e the binary64 exponent field, the binary32 exponent field is e - 896; the 52

@@ -2,7 +2,8 @@
 operations (exanbody_gb300/csrc/xnb_widen.h). The same header compiled for the
 host must agree bit for bit with the C++ float -> double conversion: every
 subnormal, every exponent with a stride through the fraction, zeros, infinities
-and NaNs (NaN: any NaN with the same sign)."""
+and NaNs (NaN: any NaN with the same sign); its short path for normal inputs
+and zeros (widen_f32_fast_bits) must give the same bits as the general one."""
 import os
 import shutil
 import subprocess
@@ -24,6 +25,10 @@ static void one(uint32_t u) {
   uint64_t want; std::memcpy(&want, &d, 8);
   const uint64_t got = xnb::widen_f32_bits(u);
   ++tested;
+  if (xnb::widen_f32_fast_bits(u) != got) {  // the short path gives the same bits
+    if (bad < 5) std::printf("fast path differs u=%08x\n", u);
+    ++bad;
+  }
   if ((u & 0x7f800000u) == 0x7f800000u && (u & 0x7fffffu)) {
     const bool ok = (got & 0x7ff0000000000000ull) == 0x7ff0000000000000ull && (got & 0xfffffffffffffull) &&
                     (got >> 63) == (u >> 31);
