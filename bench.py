@@ -42,8 +42,8 @@ FLOP64_PER_ATOM_FP64_PATH = 669.6
 FLOP64_PER_ATOM_MIXED = 282.2
 FLOP32_PER_ATOM_MIXED = 387.4
 # DRAM bytes (read + write) per atom of one mixed k_force launch, from an ncu capture of
-# the 256,000-atom case of this workload (profiles/k_force_mixed_lj256k.md); traffic grows
-# with the atom count at fixed density, so a launch moves this many bytes per atom.
+# the 256,000-atom case of this workload (FCC 40^3); traffic grows with the atom count at
+# fixed density, so a launch moves this many bytes per atom.
 FORCE_DRAM_BYTES_PER_ATOM = 546.0
 
 WORKLOAD = dict(n=100, rho=0.8442, T=1.44, seed=12345, rcut=2.5, skin=0.3, dt=0.005)
@@ -57,6 +57,29 @@ def hbm_peak_gbs():
             return float(json.load(f)["hbm_gbs"])
     except (OSError, KeyError, ValueError):
         return 6800.0
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the CPU-baseline record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        fields = dict(l.split(":", 1) for l in out.splitlines() if ":" in l)
+        name = fields.get("Model name", "").strip()
+        vendor = fields.get("Vendor ID", "").strip()
+        if name:
+            return (vendor + " " + name).strip()
+    except (OSError, subprocess.SubprocessError, ValueError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.machine()
 
 
 def config_of(n, atoms, **extra):
@@ -193,7 +216,7 @@ def run_reference(args):
         "dtype": "f64",
         "data": "synthetic",
         "config": config_of(args.n, w["n_atoms"], parallelism="single"),
-        "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": used, "kind": "port",
+        "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": used, "cpu_model": cpu_model(), "kind": "port",
                          "sample": "%d MD steps of the %d-atom system (%d rebuilds), oracle/xnb_oracle.cpp OpenMP"
                                    % (args.steps, w["n_atoms"], s.rebuilds - r0)},
         "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -422,7 +445,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         so.chunk_neighbors()
         dt_nbr = time.perf_counter() - t0
-        cpu = {"value": N * sample / dt, "unit": "atom-steps/s", "cores": used, "kind": "port",
+        cpu = {"value": N * sample / dt, "unit": "atom-steps/s", "cores": used, "cpu_model": cpu_model(), "kind": "port",
                "sample": "%d MD steps of the same %d-atom system after init (%d rebuilds), oracle OpenMP build"
                          % (sample, N, reb),
                "phases": {"force_only_atom_steps_per_s": N / dt_force, "neighbour_build_ms_per_rebuild": dt_nbr * 1e3,
@@ -565,7 +588,7 @@ def run_snap(args):
                           "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
                           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                           "data": "synthetic", "config": conf,
-                          "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": used, "kind": "port",
+                          "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": used, "cpu_model": cpu_model(), "kind": "port",
                                            "sample": "%d SNAP MD steps, oracle/xnb_snap_oracle.h OpenMP" % args.steps},
                           "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
                                   "d2h_bytes_per_step": 0}}), flush=True)
@@ -667,7 +690,7 @@ def run_snap(args):
         for _ in range(sample):
             so.step()
         dt = time.perf_counter() - t0
-        cpu = {"value": N * sample / dt, "unit": "atom-steps/s", "cores": used, "kind": "port",
+        cpu = {"value": N * sample / dt, "unit": "atom-steps/s", "cores": used, "cpu_model": cpu_model(), "kind": "port",
                "sample": "%d SNAP MD steps of the same system, oracle OpenMP build" % sample}
     if rank == 0:
         print(json.dumps({

@@ -802,6 +802,54 @@ int xnb_system_pairs(xnb_batch* b, int32_t s, uint64_t* id_a, uint64_t* id_b, in
   return XNB_OK;
 }
 
+// The pairs of a particle range: only that range's counts, starts and list
+// block cross to the host (with the system's ids, to translate the entries).
+int xnb_system_pairs_range(xnb_batch* b, int32_t s, int64_t first, int64_t count, uint64_t* id_b,
+                           int32_t* nbh_count, int64_t cap, int64_t* n_out, void* stream) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0) return fail(XNB_ERR_ARG, "pairs needs one system");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const SysHost& h = b->sys[s];
+  const int64_t n = h.d.npart;
+  if (first < 0 || count < 0 || first + count > n) return fail(XNB_ERR_ARG, "particle range outside the system");
+  const size_t o = h.d.part_base + static_cast<size_t>(first), m = static_cast<size_t>(count);
+  std::vector<uint32_t> start(m), cnt(m);
+  std::vector<uint64_t> ids(static_cast<size_t>(n));
+  if (m) {
+    XCK(cudaMemcpyAsync(start.data(), b->a.nbr_start + o, m * 4, cudaMemcpyDeviceToHost, st));
+    XCK(cudaMemcpyAsync(cnt.data(), b->a.nbr_cnt + o, m * 4, cudaMemcpyDeviceToHost, st));
+  }
+  if (n) XCK(cudaMemcpyAsync(ids.data(), b->a.id + h.d.part_base, static_cast<size_t>(n) * 8, cudaMemcpyDeviceToHost, st));
+  XCK(cudaStreamSynchronize(st));
+  const uint64_t used = h.list_off >= 0 ? h.list_cap : 0;
+  uint64_t lo = used, hi = 0;
+  for (size_t q = 0; q < m; ++q) {
+    if (!cnt[q]) continue;
+    lo = std::min<uint64_t>(lo, start[q]);
+    hi = std::max<uint64_t>(hi, static_cast<uint64_t>(start[q]) + cnt[q]);
+  }
+  if (hi > used) return fail(XNB_ERR_DEVICE, "neighbour entry outside the list segment");
+  std::vector<uint32_t> list(hi > lo ? hi - lo : 0);
+  if (!list.empty()) {
+    XCK(cudaMemcpyAsync(list.data(), b->a.nbr + h.d.list_base + lo, list.size() * 4, cudaMemcpyDeviceToHost, st));
+    XCK(cudaStreamSynchronize(st));
+  }
+  int64_t k = 0;
+  for (size_t q = 0; q < m; ++q) {
+    if (nbh_count) nbh_count[q] = static_cast<int32_t>(cnt[q]);
+    for (uint32_t t = 0; t < cnt[q]; ++t, ++k) {
+      if (k < cap && id_b) {
+        const uint32_t e = list[static_cast<uint64_t>(start[q]) + t - lo];
+        if ((e >> 5) >= static_cast<uint64_t>(n)) return fail(XNB_ERR_DEVICE, "neighbour entry outside the system");
+        id_b[k] = ids[e >> 5];
+      }
+    }
+  }
+  if (n_out) *n_out = k;
+  return XNB_OK;
+}
+
 int xnb_system_energy(xnb_batch* b, int32_t s, double* ke, double* pe, void* stream) {
   int rc = check_sys(b, s);
   if (rc) return rc;
@@ -1412,12 +1460,13 @@ int xnb_chunk_neighbors_noalloc(const xnb_lj_params* p, int64_t n, const double*
     return fail(XNB_ERR_ARG, "chunk_neighbors without allocation: null buffer or negative size");
   SysDesc d = make_desc(*p);
   d.cell_base = 0;
-  d.ncells = static_cast<uint32_t>(static_cast<uint64_t>(p->dims[0]) * p->dims[1] * p->dims[2]);
   d.part_base = 0;
-  d.npart = static_cast<uint32_t>(n);
+  // the cell count stays 64-bit until the launcher has checked it against its limit
+  const uint64_t ncells = static_cast<uint64_t>(p->dims[0]) * static_cast<uint64_t>(p->dims[1]) *
+                          static_cast<uint64_t>(p->dims[2]);
   unsigned long long total = 0;
   std::string err;
-  const int lr = launch_neighbors_static(d, static_cast<uint32_t>(n), rx, ry, rz, cell_start, cell_count, nbr,
+  const int lr = launch_neighbors_static(d, ncells, static_cast<uint64_t>(n), rx, ry, rz, cell_start, cell_count, nbr,
                                          static_cast<uint64_t>(nbr_capacity), nbr_start, nbr_count, &total,
                                          static_cast<cudaStream_t>(stream), &err);
   if (lr == -1) return fail(XNB_ERR_ARG, err);

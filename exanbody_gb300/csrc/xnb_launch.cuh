@@ -113,10 +113,10 @@ size_t scan_scratch_elems(uint32_t n);
 
 // Allocation-free neighbour build of one system (xnb_static_scratch.cu): scratch
 // in a file-scope device array; returns 0, -1 (size above the array's limit,
-// *err says which) or -2 (CUDA error).
-int launch_neighbors_static(const SysDesc& S, uint32_t n, const double* rx, const double* ry, const double* rz,
-                            const uint32_t* cell_start, const uint32_t* cell_n, uint32_t* nbr, uint64_t cap,
-                            uint32_t* nbr_start, uint32_t* nbr_cnt, unsigned long long* total_out,
+// *err says which) or -2 (CUDA error). cap is clamped to 2^32 - 1 entries.
+int launch_neighbors_static(const SysDesc& S, uint64_t ncells, uint64_t n, const double* rx, const double* ry,
+                            const double* rz, const uint32_t* cell_start, const uint32_t* cell_n, uint32_t* nbr,
+                            uint64_t cap, uint32_t* nbr_start, uint32_t* nbr_cnt, unsigned long long* total_out,
                             cudaStream_t stream, std::string* err);
 
 }  // namespace xnb

@@ -3,14 +3,15 @@
 // Some callers cannot allocate device memory at the point where they need a
 // neighbour list: a host framework that owns every device allocation through
 // its own pool (as the reference's onika allocators do) and forbids plugins to
-// call cudaMalloc mid-step, or code running while a CUDA stream is being
-// captured into a graph, where allocation calls are not permitted. This file
-// gives them a build that takes only caller-owned inputs and outputs and keeps
-// its scratch in one file-scope device array.
+// call cudaMalloc mid-step, or a time-stepping loop that must not stall on the
+// device-wide synchronisation cudaFree can impose. This file gives them a build
+// that takes only caller-owned inputs and outputs and keeps its scratch in one
+// file-scope device array.
 //
-// Limits: at most kMaxParticles particles and kMaxCells cells per call. The
-// array (about 5.3 MB) is part of the library image, so every GPU that loads
-// the library holds it until the process exits.
+// Limits: at most kMaxParticles particles and kMaxCells cells per call, and at
+// most 2^32 - 1 list entries (entry positions are 32-bit). The array (about
+// 5.3 MB) is part of the library image, so every GPU that loads the library
+// holds it until the process exits.
 //
 // Sharing: every call uses the same array. Calls whose kernels overlap on the
 // GPU (different streams, or different host threads on one device) race on it
@@ -19,7 +20,8 @@
 //
 // Set-up: the first call on a device looks up the array's device address with
 // cudaGetSymbolAddress while that device is current and caches it; make that
-// first call before any stream capture that would include this entry point.
+// first call before any stream capture begins on the device. Each call ends by
+// copying the entry total to the host and synchronising its stream.
 #include <cstdio>
 #include <mutex>
 #include <string>
@@ -217,16 +219,21 @@ void* g_scratch_ptr[64] = {};  // device address of g_nbr_scratch, per device or
 
 }  // namespace
 
-int launch_neighbors_static(const SysDesc& S, uint32_t n, const double* rx, const double* ry, const double* rz,
-                            const uint32_t* cell_start, const uint32_t* cell_n, uint32_t* nbr, uint64_t cap,
-                            uint32_t* nbr_start, uint32_t* nbr_cnt, unsigned long long* total_out,
+int launch_neighbors_static(const SysDesc& S_in, uint64_t ncells, uint64_t n, const double* rx, const double* ry,
+                            const double* rz, const uint32_t* cell_start, const uint32_t* cell_n, uint32_t* nbr,
+                            uint64_t cap, uint32_t* nbr_start, uint32_t* nbr_cnt, unsigned long long* total_out,
                             cudaStream_t stream, std::string* err) {
-  if (n > kMaxParticles || S.ncells > kMaxCells) {
+  if (n > kMaxParticles || ncells > kMaxCells) {
     *err = "chunk_neighbors without allocation: at most " + std::to_string(kMaxParticles) + " particles and " +
            std::to_string(kMaxCells) + " cells per call (got " + std::to_string(n) + " particles, " +
-           std::to_string(S.ncells) + " cells)";
+           std::to_string(ncells) + " cells)";
     return -1;
   }
+  SysDesc S = S_in;
+  S.ncells = static_cast<uint32_t>(ncells);
+  S.npart = static_cast<uint32_t>(n);
+  // entry positions are 32-bit: a total above 2^32 - 1 reports as a capacity error
+  if (cap > 0xFFFFFFFFull) cap = 0xFFFFFFFFull;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= 64) {
@@ -247,30 +254,40 @@ int launch_neighbors_static(const SysDesc& S, uint32_t n, const double* rx, cons
     }
     base = g_scratch_ptr[dev];
   }
+  auto failed = [&](const char* what, cudaError_t ce) {
+    *err = std::string("chunk_neighbors without allocation: ") + what + ": " + cudaGetErrorString(ce);
+    return -2;
+  };
   unsigned char* scratch = static_cast<unsigned char*>(base);
   int sm = 1;
-  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return failed("cudaDeviceGetAttribute", e);
   const size_t smem = static_cast<size_t>(4) * kStageCap * (sizeof(float4) + sizeof(uint32_t));
-  cudaFuncSetAttribute(k_neighbors_static<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  cudaFuncSetAttribute(k_neighbors_static<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  e = cudaFuncSetAttribute(k_neighbors_static<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return failed("cudaFuncSetAttribute", e);
+  e = cudaFuncSetAttribute(k_neighbors_static<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return failed("cudaFuncSetAttribute", e);
   long long want = (static_cast<long long>(S.ncells) + 3) / 4;
   const long long capb = static_cast<long long>(sm) * 16;
   const int grid = static_cast<int>(want < 1 ? 1 : (want > capb ? capb : want));
   k_neighbors_static<false><<<grid, 128, smem, stream>>>(S, rx, ry, rz, cell_start, cell_n, nbr, nbr_start, nbr_cnt,
                                                          cap, scratch);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return failed("count pass launch", e);
   launch_scan_u32_to_u64(reinterpret_cast<const uint32_t*>(scratch + kTotalsOff),
                          reinterpret_cast<unsigned long long*>(scratch + kOffsetsOff), S.ncells,
                          reinterpret_cast<unsigned long long*>(scratch + kBlocksOff), stream);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return failed("offset scan launch", e);
   k_neighbors_static<true><<<grid, 128, smem, stream>>>(S, rx, ry, rz, cell_start, cell_n, nbr, nbr_start, nbr_cnt,
                                                         cap, scratch);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return failed("fill pass launch", e);
   e = cudaMemcpyAsync(total_out, scratch + kOffsetsOff + sizeof(unsigned long long) * S.ncells,
                       sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-  if (e == cudaSuccess) e = cudaGetLastError();
-  if (e != cudaSuccess) {
-    *err = std::string("chunk_neighbors without allocation: ") + cudaGetErrorString(e);
-    return -2;
-  }
+  if (e != cudaSuccess) return failed("cudaMemcpyAsync", e);
+  e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return failed("cudaStreamSynchronize", e);
   return 0;
 }
 

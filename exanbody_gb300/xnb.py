@@ -21,6 +21,12 @@ PRECISIONS = {"fp64_exact": PREC_FP64_EXACT, "fp64": PREC_FP64, "mixed": PREC_MI
 STEP_HOST_SYNC = 1
 STEP_ENERGY = 2
 
+ERR_ARG = -1
+ERR_CUDA = -2
+ERR_NOMEM = -3
+ERR_CAPACITY = -4
+ERR_DEVICE = -5
+
 ERRBIT_LIST_OVERFLOW = 1
 ERRBIT_FAR_MOVER = 2
 ERRBIT_CELL_INDEX = 4
@@ -34,7 +40,7 @@ EXPORTED = [
     "xnb_check_errors", "xnb_stats_kernel_launches", "xnb_chunk_neighbors_noalloc", "xnb_chunk_neighbors_stream",
     "xnb_verify_chunk_neighbors", "xnb_simulation_stats", "xnb_sample_particles", "xnb_system_set_types",
     "xnb_gravitational_force", "xnb_batch_set_tuning", "xnb_autotune", "xnb_snap_create", "xnb_snap_destroy",
-    "xnb_snap_force",
+    "xnb_snap_force", "xnb_system_pairs_range",
 ]
 
 FORCE_ENERGY = 1
@@ -154,6 +160,7 @@ def load(build_if_missing=True):
     lib.xnb_system_info_get.argtypes = [vp, i32, P(SystemInfo), vp]
     lib.xnb_system_download.argtypes = [vp, i32] + [P(d)] * 9 + [P(u64), P(i32), P(d), vp]
     lib.xnb_system_pairs.argtypes = [vp, i32, P(u64), P(u64), P(i32), i64, P(i64), vp]
+    lib.xnb_system_pairs_range.argtypes = [vp, i32, i64, i64, P(u64), P(i32), i64, P(i64), vp]
     lib.xnb_system_energy.argtypes = [vp, i32, P(d), P(d), vp]
     lib.xnb_init_particles.argtypes = [vp, i32, i32, vp]
     lib.xnb_push_f_v_r.argtypes = [vp, i32, d, vp]
@@ -306,6 +313,20 @@ class Batch:
                                       cnt.ctypes.data_as(C.POINTER(C.c_int32)), m, C.byref(nout), self.stream))
         return a[: nout.value], b[: nout.value], cnt
 
+    def pairs_range(self, s, first, count, entries):
+        """Partner ids (list order) and per-particle lengths of particles
+        [first, first + count); `entries` bounds the id array (the range's list total)."""
+        b = np.empty(int(entries), np.uint64)
+        cnt = np.empty(int(count), np.int32)
+        nout = C.c_int64()
+        _ck(self.lib.xnb_system_pairs_range(self.h, s, int(first), int(count),
+                                            b.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                            cnt.ctypes.data_as(C.POINTER(C.c_int32)), int(entries), C.byref(nout),
+                                            self.stream))
+        if nout.value > len(b):
+            raise XnbError(-4, "pairs_range: %d entries, %d requested" % (nout.value, len(b)))
+        return b[: nout.value], cnt
+
     def energy(self, s):
         ke, pe = C.c_double(), C.c_double()
         _ck(self.lib.xnb_system_energy(self.h, s, C.byref(ke), C.byref(pe), self.stream))
@@ -422,12 +443,17 @@ class Batch:
 def chunk_neighbors_noalloc(params, n, rx, ry, rz, cell_start, cell_count, nbr, nbr_capacity, nbr_start, nbr_count,
                             stream=None):
     """xnb_chunk_neighbors_noalloc on caller-owned device buffers (device pointers as ints).
-    Returns the number of entries written."""
+    Returns the number of entries written; an XnbError carries `.total`, the
+    entries needed, which the library sets with XNB_ERR_CAPACITY."""
     lib = load()
-    total = C.c_int64()
-    _ck(lib.xnb_chunk_neighbors_noalloc(C.byref(params), int(n), rx, ry, rz, cell_start, cell_count, nbr,
-                                        int(nbr_capacity), nbr_start, nbr_count, C.byref(total),
-                                        C.c_void_p(stream) if stream else None))
+    total = C.c_int64(-1)
+    rc = lib.xnb_chunk_neighbors_noalloc(C.byref(params), int(n), rx, ry, rz, cell_start, cell_count, nbr,
+                                         int(nbr_capacity), nbr_start, nbr_count, C.byref(total),
+                                         C.c_void_p(stream) if stream else None)
+    if rc != 0:
+        err = XnbError(rc, lib.xnb_last_error_string().decode())
+        err.total = total.value  # entries needed (set with XNB_ERR_CAPACITY)
+        raise err
     return total.value
 
 

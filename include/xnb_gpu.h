@@ -134,6 +134,11 @@ int xnb_system_download(xnb_batch* b, int32_t sys, double* rx, double* ry, doubl
  * particle (storage order). cap is the size of id_a/id_b; n_out the pair count. */
 int xnb_system_pairs(xnb_batch* b, int32_t sys, uint64_t* id_a, uint64_t* id_b, int32_t* nbh_count, int64_t cap,
                      int64_t* n_out, void* stream);
+/* The same for the particles [first, first + count) of the system (storage
+ * order): partner ids in list order and one length per particle of the range,
+ * so that large systems cross to the host in slices. Synchronises. */
+int xnb_system_pairs_range(xnb_batch* b, int32_t sys, int64_t first, int64_t count, uint64_t* id_b,
+                           int32_t* nbh_count, int64_t cap, int64_t* n_out, void* stream);
 /* Kinetic 0.5*m*v^2 and truncated-and-shifted LJ energy of the last force call
  * made with energies. */
 int xnb_system_energy(xnb_batch* b, int32_t sys, double* ke, double* pe, void* stream);
@@ -282,8 +287,8 @@ int xnb_sample_particles(xnb_batch* b, int32_t sys, const uint64_t* ids, int64_t
 /* No counterpart in the reference. chunk_neighbors for one system, for callers
  * that cannot allocate device memory where they need the lists: a host
  * framework that owns all device memory through its own pools and forbids
- * cudaMalloc inside a step, or code running while a stream is being captured
- * into a CUDA graph (allocation is not permitted there). It allocates nothing:
+ * cudaMalloc inside a step, or a time-stepping loop that must not stall on the
+ * device-wide synchronisation cudaFree can impose. It allocates nothing:
  * inputs and outputs are the caller's device buffers, and scratch is one
  * file-scope device array of the library (about 5.3 MB, held by every GPU that
  * loads the library until exit).
@@ -293,13 +298,16 @@ int xnb_sample_particles(xnb_batch* b, int32_t sys, const uint64_t* ids, int64_t
  *                    the reference's (cell_enc, p_b) order; capacity nbr_capacity
  *   nbr_start/count  output per particle: first entry and number of entries
  *   total_out        entries needed (set also when the capacity is too small)
- * Limits: n <= 1,048,576 particles and <= 131,072 cells; larger inputs return
- * XNB_ERR_ARG with the limit in xnb_last_error_string(). Returns XNB_ERR_CAPACITY
- * when total_out > nbr_capacity (nbr is then left unwritten).
+ * Limits: n <= 1,048,576 particles, <= 131,072 cells (the dims product, checked
+ * in 64 bits) and at most 2^32 - 1 entries (a larger nbr_capacity counts as
+ * 2^32 - 1); larger inputs return XNB_ERR_ARG with the limit in
+ * xnb_last_error_string(). Returns XNB_ERR_CAPACITY when total_out >
+ * nbr_capacity (nbr and nbr_start are then left unwritten; nbr_count holds the
+ * per-particle counts).
  * The first call on a device looks up the scratch array's address (set-up);
- * make it before any stream capture that includes this call. All calls share the
+ * make it before any stream capture begins on that device. All calls share the
  * array: calls that overlap on the GPU race and must be serialised by the
- * caller. The call synchronises `stream` to return total_out. */
+ * caller. Each call copies total_out to the host and synchronises `stream`. */
 int xnb_chunk_neighbors_noalloc(const xnb_lj_params* p, int64_t n, const double* rx, const double* ry,
                                 const double* rz, const uint32_t* cell_start, const uint32_t* cell_count,
                                 uint32_t* nbr, int64_t nbr_capacity, uint32_t* nbr_start, uint32_t* nbr_count,

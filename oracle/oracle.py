@@ -59,6 +59,9 @@ def _lib(kind="parity"):
     lib.xo_gravitational_force.argtypes = [C.c_void_p, d, P(d), C.c_int32, d]
     lib.xo_get_cell_counts.argtypes = [C.c_void_p, P(i64)]
     lib.xo_get_pairs.argtypes = [C.c_void_p, P(u64), P(u64), P(i32)]
+    lib.xo_pair_count_cells.restype = i64
+    lib.xo_pair_count_cells.argtypes = [C.c_void_p, i64, i64]
+    lib.xo_get_pairs_cells.argtypes = [C.c_void_p, i64, i64, P(u64), P(i32)]
     lib.xo_cell_stream_size.restype = i64
     lib.xo_cell_stream_size.argtypes = [C.c_void_p, i64]
     lib.xo_get_cell_stream.argtypes = [C.c_void_p, i64, P(u16)]
@@ -187,6 +190,15 @@ class OracleSystem:
         cnt = np.empty(self.n, np.int32)
         self.lib.xo_get_pairs(self.h, _ptr(a, C.c_uint64), _ptr(b, C.c_uint64), _ptr(cnt, C.c_int32))
         return a, b, cnt
+
+    def pairs_of_cells(self, ci0, ci1, n_particles):
+        """Partner ids (list order) and per-particle lengths of the n_particles
+        particles of interior cells [ci0, ci1)."""
+        m = int(self.lib.xo_pair_count_cells(self.h, int(ci0), int(ci1)))
+        b = np.empty(m, np.uint64)
+        cnt = np.empty(int(n_particles), np.int32)
+        self.lib.xo_get_pairs_cells(self.h, int(ci0), int(ci1), _ptr(b, C.c_uint64), _ptr(cnt, C.c_int32))
+        return b, cnt
 
     def cell_stream(self, interior_cell):
         m = int(self.lib.xo_cell_stream_size(self.h, interior_cell))

@@ -1053,10 +1053,14 @@ int xo_get_cell_counts(const xo_sys* s, int64_t* counts) {
   return 0;
 }
 
-static int64_t walk_pairs(const xo_sys* s, uint64_t* ida, uint64_t* idb, int32_t* cnt) {
+// The stream entries of the interior cells [ci0, ci1) as ids, in stream order
+// (the decoding of compute_cell_particle_pairs_impl_default.h:148-180).
+static int64_t walk_pairs(const xo_sys* s, uint64_t* ida, uint64_t* idb, int32_t* cnt, long ci0 = 0,
+                          long ci1 = -1) {
   int64_t k = 0, q = 0;
   const long nint = s->D[0] * s->D[1] * s->D[2];
-  for (long ci = 0; ci < nint; ++ci) {
+  if (ci1 < 0 || ci1 > nint) ci1 = nint;
+  for (long ci = ci0 < 0 ? 0 : ci0; ci < ci1; ++ci) {
     const long c = s->interior_to_grid(ci);
     const Cell& A = s->cells[c];
     const size_t na = A.size();
@@ -1093,6 +1097,15 @@ int64_t xo_pair_count(const xo_sys* s) { return walk_pairs(s, nullptr, nullptr, 
 
 int xo_get_pairs(const xo_sys* s, uint64_t* id_a, uint64_t* id_b, int32_t* nbh_count) {
   walk_pairs(s, id_a, id_b, nbh_count);
+  return 0;
+}
+
+int64_t xo_pair_count_cells(const xo_sys* s, int64_t ci0, int64_t ci1) {
+  return walk_pairs(s, nullptr, nullptr, nullptr, static_cast<long>(ci0), static_cast<long>(ci1));
+}
+
+int xo_get_pairs_cells(const xo_sys* s, int64_t ci0, int64_t ci1, uint64_t* id_b, int32_t* nbh_count) {
+  walk_pairs(s, nullptr, id_b, nbh_count, static_cast<long>(ci0), static_cast<long>(ci1));
   return 0;
 }
 

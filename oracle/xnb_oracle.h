@@ -82,6 +82,10 @@ int xo_get_cell_counts(const xo_sys* s, int64_t* counts);
  * the per-particle list lengths (nbh_count, one per particle). */
 int64_t xo_pair_count(const xo_sys* s);
 int xo_get_pairs(const xo_sys* s, uint64_t* id_a, uint64_t* id_b, int32_t* nbh_count);
+/* The same for the particles of interior cells [ci0, ci1) only (partner ids and
+ * per-particle lengths), so that large systems can be compared slice by slice. */
+int64_t xo_pair_count_cells(const xo_sys* s, int64_t ci0, int64_t ci1);
+int xo_get_pairs_cells(const xo_sys* s, int64_t ci0, int64_t ci1, uint64_t* id_b, int32_t* nbh_count);
 
 /* Reference-format u16 chunk stream of one interior cell (chunk_neighbors_execute.h:249-398). */
 int64_t xo_cell_stream_size(const xo_sys* s, int64_t interior_cell);

@@ -10,7 +10,9 @@ import json
 import os
 import sys
 
-src_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python %s <root of the exaNBody source tree>" % sys.argv[0])
+src_root = sys.argv[1]
 src = os.path.join(src_root, "contribs/microStamp/samples/benchmark_lj_snap/check_values_lj_Ni.dat")
 rows = []
 with open(src) as f:

@@ -14,7 +14,9 @@ import os
 import shutil
 import sys
 
-src_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python %s <root of the exaNBody source tree>" % sys.argv[0])
+src_root = sys.argv[1]
 dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "snap")
 os.makedirs(dst, exist_ok=True)
 bench = os.path.join(src_root, "contribs/microStamp/samples/benchmark_lj_snap")
