@@ -97,6 +97,7 @@ struct xnb_batch {
   xnb_batch_config cfg{};
   int stage_cap = 640;
   int force_block = 128;
+  int build_form = kBuildWarp;  // neighbour-build kernel (xnb_batch_set_build_form)
   DevArrays a{};
   SysDesc* d_sys = nullptr;
   SysState* d_st = nullptr;
@@ -378,7 +379,7 @@ int size_lists(xnb_batch* b, int s, uint32_t need, cudaStream_t st) {
 int neighbors_sync(xnb_batch* b, cudaStream_t st) {
   const Extent ex = b->extent();
   for (int pass = 0; pass < 3; ++pass) {
-    b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, list_buf(b), st);
+    b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, list_buf(b), st, b->build_form);
     int rc = pull_states(b, st);
     if (rc) return rc;
     bool again = false;
@@ -1022,7 +1023,7 @@ int xnb_step(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, voi
         int rc = neighbors_sync(b, st);
         if (rc) return rc;
       } else {
-        b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, list_buf(b), st);
+        b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, list_buf(b), st, b->build_form);
       }
     }
     // compute_all_forces_energy + verlet_second_half
@@ -1097,6 +1098,13 @@ int xnb_batch_set_tuning(xnb_batch* b, int32_t stage_cap, int32_t force_block) {
   return XNB_OK;
 }
 
+int xnb_batch_set_build_form(xnb_batch* b, int32_t form) {
+  if (!b) return fail(XNB_ERR_ARG, "null batch");
+  if (form != XNB_BUILD_ROWS && form != XNB_BUILD_WARP) return fail(XNB_ERR_ARG, "unknown neighbour-build form");
+  b->build_form = form == XNB_BUILD_ROWS ? kBuildRows : kBuildWarp;
+  return XNB_OK;
+}
+
 int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* stream, xnb_tuning* out) {
   if (!b || !out) return fail(XNB_ERR_ARG, "null argument");
   if (trial_steps <= 0) return fail(XNB_ERR_ARG, "trial_steps must be positive");
@@ -1112,8 +1120,10 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
   XCK(cudaEventCreate(&e0));
   XCK(cudaEventCreate(&e1));
   int trials = 0;
-  auto rate_of = [&](int sc, int fb, int nw, double* rate) -> int {
+  auto rate_of = [&](int sc, int fb, int nw, int bf, double* rate) -> int {
     int rc = xnb_batch_set_tuning(b, sc, fb);
+    if (rc) return rc;
+    rc = xnb_batch_set_build_form(b, bf);
     if (rc) return rc;
     const int32_t prec = precision | (nw ? XNB_PREC_NEWTON : 0);
     rc = xnb_step(b, 1, prec, 0, stream);
@@ -1129,25 +1139,31 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
     *rate = static_cast<double>(atoms) * trial_steps / (static_cast<double>(ms) * 1e-3);
     return xnb_check_errors(b, stream);
   };
-  const int caps[3] = {384, 640, 1024}, blocks[2] = {128, 256};
+  const int caps[3] = {384, 640, 1024}, blocks[2] = {128, 256}, forms[2] = {XNB_BUILD_ROWS, XNB_BUILD_WARP};
   int best_sc = b->stage_cap, best_fb = b->force_block, best_nw = 0;
+  int best_bf = b->build_form == kBuildRows ? XNB_BUILD_ROWS : XNB_BUILD_WARP;
   double best = 0.0;
-  int rc = rate_of(best_sc, best_fb, best_nw, &best);
+  int rc = rate_of(best_sc, best_fb, best_nw, best_bf, &best);
   // coordinate search: one parameter at a time, the others at their best so far
-  for (int pass = 0; pass < 3 && rc == 0; ++pass) {
-    for (int v = 0; v < (pass == 0 ? 3 : (pass == 1 ? 2 : 2)) && rc == 0; ++v) {
-      int sc = best_sc, fb = best_fb, nw = best_nw;
-      if (pass == 0) sc = caps[v];
-      else if (pass == 1) fb = blocks[v];
+  // (neighbour-build form, then the stage cap of the forms that stage whole
+  // neighbourhoods, the force block size and the Newton traversal)
+  const int nvals[4] = {2, 3, 2, 2};
+  for (int pass = 0; pass < 4 && rc == 0; ++pass) {
+    for (int v = 0; v < nvals[pass] && rc == 0; ++v) {
+      int sc = best_sc, fb = best_fb, nw = best_nw, bf = best_bf;
+      if (pass == 0) bf = forms[v];
+      else if (pass == 1) sc = caps[v];
+      else if (pass == 2) fb = blocks[v];
       else nw = v;
-      if (sc == best_sc && fb == best_fb && nw == best_nw) continue;
+      if (sc == best_sc && fb == best_fb && nw == best_nw && bf == best_bf) continue;
       double r = 0.0;
-      rc = rate_of(sc, fb, nw, &r);
+      rc = rate_of(sc, fb, nw, bf, &r);
       if (rc == 0 && r > best) {
         best = r;
         best_sc = sc;
         best_fb = fb;
         best_nw = nw;
+        best_bf = bf;
       }
     }
   }
@@ -1156,8 +1172,11 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
   if (rc) return rc;
   rc = xnb_batch_set_tuning(b, best_sc, best_fb);
   if (rc) return rc;
+  rc = xnb_batch_set_build_form(b, best_bf);
+  if (rc) return rc;
   out->stage_cap = best_sc;
   out->force_block = best_fb;
+  out->build_form = best_bf;
   out->newton = best_nw;
   out->trials = trials;
   out->atom_steps_per_s = best;
@@ -1380,6 +1399,47 @@ int xnb_gravitational_force(xnb_batch* b, int32_t s, double G, const double* typ
   XCK(cudaStreamSynchronize(st));
   if (flag & 1u) return fail(XNB_ERR_ARG, "a particle type has no mass");
   return check_launch();
+}
+
+int xnb_system_pair_view(xnb_batch* b, int32_t s, xnb_pair_view* out) {
+  int rc = check_sys(b, s);
+  if (rc) return rc;
+  if (s < 0 || !out) return fail(XNB_ERR_ARG, "pair view needs one system and an output");
+  const SysHost& h = b->sys[s];
+  const size_t o = h.d.part_base;
+  xnb_pair_view v{};
+  v.n_particles = h.d.npart;
+  v.rx = b->a.rx + o;
+  v.ry = b->a.ry + o;
+  v.rz = b->a.rz + o;
+  v.vx = b->a.vx + o;
+  v.vy = b->a.vy + o;
+  v.vz = b->a.vz + o;
+  v.fx = b->a.fx + o;
+  v.fy = b->a.fy + o;
+  v.fz = b->a.fz + o;
+  v.pe = b->a.pe + o;
+  v.id = b->a.id + o;
+  v.type = b->a.ptype + o;
+  v.mirror = b->a.pf + o;
+  v.mirror_lo = b->a.pflo + o;
+  v.nbr = b->a.nbr + h.d.list_base;
+  v.nbr_start = b->a.nbr_start + o;
+  v.nbr_count = b->a.nbr_cnt + o;
+  v.nbr_half = b->a.nbr_half + o;
+  double P = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    v.origin[a] = h.d.origin[a];
+    v.period[a] = h.d.period[a];
+    P = std::max(P, std::fabs(h.d.period[a]));
+  }
+  v.nbh_dist = std::sqrt(h.d.nbh2);
+  v.max_period = P;
+  v.mass = h.d.mass;
+  v.divide_by_mass = h.d.divide_by_mass;
+  v.sys = s;
+  *out = v;
+  return XNB_OK;
 }
 
 int64_t xnb_stats_kernel_launches(const xnb_batch* b) { return b ? static_cast<int64_t>(b->launches) : -1; }

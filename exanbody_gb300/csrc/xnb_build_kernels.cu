@@ -1,21 +1,15 @@
 // Rebuild-path kernels: move/rebin with periodic wrap, AMR in-cell ordering,
 // backup_r, and the cell-grid neighbour build; plus the device scan they use.
+#include "xnb_build_common.cuh"
 #include "xnb_launch.cuh"
 
 namespace xnb {
 
 namespace {
 
-constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+using namespace build;
 constexpr uint32_t kMoverBit = 0x80000000u;
 
-__device__ __forceinline__ bool sys_flagged(const SysState* st, uint32_t s) { return st[s].rebuild != 0; }
-
-__device__ __forceinline__ unsigned lanemask_lt() {
-  unsigned m;
-  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-  return m;
-}
 
 // sub_grid_size (amr/include/exanb/amr/amr_grid_algorithm.h:66-78): the largest
 // side s with s^3 <= n/density (1 below side 2, capped at 16), computed from the
@@ -412,63 +406,6 @@ __global__ void k_arm(int nsys, SysState* st, const unsigned int* any) {
 // against one particle of the cell and a ballot keeps the hits in order. The FP32 distance decides whenever it lies farther than a
 // proven error bound from the threshold; otherwise the reference's FP64 d2 (and
 // the FP64 ghost filter) decide, so the pair set is bit-exact.
-constexpr uint32_t kAmbiguousBit = 0x80000000u;  // entry flag: ghost filter undecided in FP32
-
-__device__ __forceinline__ float4 stage_from(const SysDesc& S, const float4 pb, uint32_t j, uint32_t gc) {
-  float4 rb;
-  rb.x = image_coord_f(pb.x, S.period_f[0], static_cast<int>(gc % 3u));
-  rb.y = image_coord_f(pb.y, S.period_f[1], static_cast<int>((gc / 3u) % 3u));
-  rb.z = image_coord_f(pb.z, S.period_f[2], static_cast<int>(gc / 9u));
-  uint32_t ent = ((j - S.part_base) << 5) | gc;
-  if (gc != static_cast<uint32_t>(kImageCenter)) {
-    const float fm = S.filter_margin_f;
-    const float v[3] = {rb.x, rb.y, rb.z};
-    bool out = false, amb = false;
-    for (int ax = 0; ax < 3; ++ax) {
-      if (v[ax] < S.outer_lo_f[ax] - fm || v[ax] > S.outer_hi_f[ax] + fm) out = true;
-      else if (v[ax] < S.outer_lo_f[ax] + fm || v[ax] > S.outer_hi_f[ax] - fm) amb = true;
-    }
-    if (out) {
-      ent = kInvalid;
-      rb.x = rb.y = rb.z = 1.0e18f;  // never within reach: the test needs no validity check
-    } else if (amb) {
-      ent |= kAmbiguousBit;
-    }
-  }
-  rb.w = __uint_as_float(ent);
-  return rb;
-}
-
-__device__ __forceinline__ float4 stage_candidate(const SysDesc& S, const DevArrays& a, uint32_t j, uint32_t gc) {
-  return stage_from(S, a.pf[j], j, gc);
-}
-
-// The reference's FP64 decision for one (particle i, candidate entry) pair.
-__device__ __noinline__ bool exact_neighbor_test(const SysDesc& S, const DevArrays& a, uint32_t i, uint32_t ent) {
-  const uint32_t e = ent & ~kAmbiguousBit;
-  const uint32_t j = S.part_base + (e >> 5);
-  const uint32_t gc = e & 31u;
-  const double xb = image_coord(a.rx[j], S.period[0], static_cast<int>(gc % 3u));
-  const double yb = image_coord(a.ry[j], S.period[1], static_cast<int>((gc / 3u) % 3u));
-  const double zb = image_coord(a.rz[j], S.period[2], static_cast<int>(gc / 9u));
-  bool keep = true;
-  if (gc != static_cast<uint32_t>(kImageCenter))
-    keep = xb >= S.outer_lo[0] && xb <= S.outer_hi[0] && yb >= S.outer_lo[1] && yb <= S.outer_hi[1] &&
-           zb >= S.outer_lo[2] && zb <= S.outer_hi[2];
-  const double d2 = norm2_rn(__dsub_rn(a.rx[i], xb), __dsub_rn(a.ry[i], yb), __dsub_rn(a.rz[i], zb));
-  return keep && d2 > 0.0 && d2 <= S.nbh2;
-}
-
-// Per-warp list statistics, flushed to the system's state when the warp moves
-// on to another system's cells and at the end.
-__device__ __forceinline__ void flush_list_stats(SysState* st, const SysDesc* sys, uint32_t s, uint32_t mx,
-                                                 unsigned long long sum) {
-  if (s == kInvalid) return;
-  if (mx > sys[s].list_slot) atomicOr(&st[s].error, kErrListOverflow);
-  atomicMax(&st[s].max_nbr, mx);
-  atomicAdd(&st[s].list_used, sum);
-}
-
 // Writes one particle's finished list: the buffered entries in full lines, its
 // count, lower-half length and slot start.
 __device__ __forceinline__ void finish_particle(const DevArrays& a, uint32_t* seg, const uint32_t* sbuf, bool buffered,
@@ -1093,7 +1030,7 @@ int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevA
 }
 
 int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int cap, int lbuf,
-                     cudaStream_t stream) {
+                     cudaStream_t stream, int form) {
   if (ex.n_cells == 0) return 0;
   const size_t smem = static_cast<size_t>(cap) * sizeof(float4) + static_cast<size_t>(4) * 2 * lbuf * sizeof(uint32_t);
   // warp-per-cell buffers: one slot of each of kNbrP particles plus a spill word
@@ -1109,7 +1046,8 @@ int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const D
   const long long want_w = (static_cast<long long>(ex.n_cells) + 3) / 4;
   const int grid_w = static_cast<int>(std::max(1ll, std::min(want_w, static_cast<long long>(per_sm) * ex.sm_count)));
   k_nbr_reset<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild, a.nbr_wide_n);
-  k_neighbors_warp<<<grid_w, 128, smem_w, stream>>>(ex.n_cells, sys, st, a, cap, lbuf_w);
+  if (form == kBuildRows) launch_neighbors_rows(ex, sys, st, a, stream);
+  else k_neighbors_warp<<<grid_w, 128, smem_w, stream>>>(ex.n_cells, sys, st, a, cap, lbuf_w);
   k_neighbors<<<warp_grid(ex.n_cells, 1, ex.sm_count), 128, smem, stream>>>(ex.n_cells, sys, st, a, cap, lbuf);
   return 3;
 }

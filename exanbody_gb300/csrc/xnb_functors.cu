@@ -1,5 +1,6 @@
-// Pair functors other than Lennard-Jones over the same per-particle lists and
-// the same FP32-prefiltered traversal (prefilter_window / next_mark).
+// Pair functors other than Lennard-Jones over the same per-particle lists,
+// written against the pair-functor API (include/xnb_pair.cuh) and run through
+// its FP32-prefiltered traversal.
 //
 // gravitational_force (contribs/pi/gravitational_force.cu:42-141) is a
 // buffer-less functor: compute_cell_particle_pairs calls it per stream entry
@@ -19,84 +20,75 @@ constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 
 // P = kFp64Exact: the functor's operations and roundings, bit-identical to the
 // CPU restatement. P = kFp64: same pairs, 1/r^3 from one correctly rounded
-// square root and one division, FMA accumulation.
+// square root and one division, FMA accumulation. A pair-functor API functor
+// (include/xnb_pair.cuh): buffer-less, called per pair within gp.rcut.
 template <int P, bool PE>
-__global__ void __launch_bounds__(128)
-    k_grav(uint32_t n_part, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a,
-           int sys_only, GravParams gp, bool accumulate, unsigned int* flags) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_part) return;
-  const uint32_t c = a.pcell[i];
-  if (c == kInvalid) return;
-  const uint32_t s = a.cell_sys[c];
-  if (sys_only >= 0 && s != static_cast<uint32_t>(sys_only)) return;
-  if (st[s].error) return;
-  const SysDesc& S = sys[s];
-  const uint32_t ta = a.ptype[i];
-  if (ta >= static_cast<uint32_t>(gp.ntypes)) {
-    atomicOr(flags, 1u);
-    return;
+struct GravForce {
+  DevArrays a;
+  GravParams gp;
+  bool accumulate;
+  unsigned int* flags;
+  struct Acc {
+    double fx, fy, fz, pe, ma;
+  };
+
+  __device__ __forceinline__ double rcut2(const pair::ParticleContext&) const { return gp.rcut2; }
+  __device__ __forceinline__ float prefilter_hi(const pair::ParticleContext&) const { return gp.pre_hi_f; }
+  __device__ __forceinline__ bool start(Acc& q, const pair::ParticleContext& c) const {
+    const uint32_t ta = a.ptype[c.i];
+    if (ta >= static_cast<uint32_t>(gp.ntypes)) {
+      atomicOr(flags, 1u);
+      return false;
+    }
+    q.ma = gp.mass[ta];
+    q.fx = accumulate ? a.fx[c.i] : 0.0;
+    q.fy = accumulate ? a.fy[c.i] : 0.0;
+    q.fz = accumulate ? a.fz[c.i] : 0.0;
+    q.pe = 0.0;
+    return true;
   }
-  const double ma = gp.mass[ta];
-  const double xa = a.rx[i], ya = a.ry[i], za = a.rz[i];
-  const uint32_t* __restrict__ L = a.nbr + S.list_base + a.nbr_start[i];
-  const uint32_t n = a.nbr_cnt[i];
-  const uint32_t pbase = S.part_base;
-  const float4 paf = a.pf[i];
-  const float pfx = S.period_f[0], pfy = S.period_f[1], pfz = S.period_f[2];
-  double fx = accumulate ? a.fx[i] : 0.0, fy = accumulate ? a.fy[i] : 0.0, fz = accumulate ? a.fz[i] : 0.0;
-  double pe = 0.0;
-  const uint32_t self_e = ((i - pbase) << 5) | static_cast<uint32_t>(kImageCenter);
-  for (uint32_t kw = 0; kw < n; kw += 128) {
-    Marks mk = prefilter_window(L, kw, min(n, kw + 128u), a.pf, pbase, self_e, paf, pfx, pfy, pfz, gp.pre_hi_f);
-    uint32_t b;
-    while (next_mark(mk, b)) {
-      const uint32_t e = __ldg(L + kw + b);
-      const uint32_t j = pbase + (e >> 5);
-      const uint32_t code = e & 31u;
-      double xb = __ldg(a.rx + j), yb = __ldg(a.ry + j), zb = __ldg(a.rz + j);
-      if (code != static_cast<uint32_t>(kImageCenter)) {
-        xb = image_coord(xb, S.period[0], static_cast<int>(code % 3u));
-        yb = image_coord(yb, S.period[1], static_cast<int>((code / 3u) % 3u));
-        zb = image_coord(zb, S.period[2], static_cast<int>(code / 9u));
+  __device__ __forceinline__ void pair(Acc& q, const pair::ParticleContext&, const pair::PairData& p) const {
+    const uint32_t tb = a.ptype[p.j];
+    if (tb >= static_cast<uint32_t>(gp.ntypes)) {
+      atomicOr(flags, 1u);
+      return;
+    }
+    const double mb = gp.mass[tb];
+    if (P == kFp64Exact) {
+      const double r = __dsqrt_rn(p.d2);
+      const double inv_r = __ddiv_rn(1.0, r);
+      double de = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(gp.G, q.ma), mb), inv_r), inv_r);
+      de = __dmul_rn(de, __ddiv_rn(1.0, r));
+      q.fx = __dadd_rn(q.fx, __dmul_rn(de, p.dx));
+      q.fy = __dadd_rn(q.fy, __dmul_rn(de, p.dy));
+      q.fz = __dadd_rn(q.fz, __dmul_rn(de, p.dz));
+      if (PE) {
+        const double en = __dmul_rn(__dmul_rn(__dmul_rn(-gp.G, q.ma), mb), inv_r);
+        q.pe = __dadd_rn(q.pe, __dmul_rn(0.5, en));
       }
-      const double dx = __dsub_rn(xb, xa), dy = __dsub_rn(yb, ya), dz = __dsub_rn(zb, za);
-      const double d2 = norm2_rn(dx, dy, dz);
-      if (!(d2 > 0.0 && d2 <= gp.rcut2)) continue;
-      const uint32_t tb = a.ptype[j];
-      if (tb >= static_cast<uint32_t>(gp.ntypes)) {
-        atomicOr(flags, 1u);
-        continue;
-      }
-      const double mb = gp.mass[tb];
-      if (P == kFp64Exact) {
-        const double r = __dsqrt_rn(d2);
-        const double inv_r = __ddiv_rn(1.0, r);
-        double de = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(gp.G, ma), mb), inv_r), inv_r);
-        de = __dmul_rn(de, __ddiv_rn(1.0, r));
-        fx = __dadd_rn(fx, __dmul_rn(de, dx));
-        fy = __dadd_rn(fy, __dmul_rn(de, dy));
-        fz = __dadd_rn(fz, __dmul_rn(de, dz));
-        if (PE) {
-          const double en = __dmul_rn(__dmul_rn(__dmul_rn(-gp.G, ma), mb), inv_r);
-          pe = __dadd_rn(pe, __dmul_rn(0.5, en));
-        }
-      } else {
-        const double r = sqrt(d2);
-        const double inv_r3 = 1.0 / (d2 * r);
-        const double gm = gp.G * ma * mb;
-        const double de = gm * inv_r3;
-        fx = fma(de, dx, fx);
-        fy = fma(de, dy, fy);
-        fz = fma(de, dz, fz);
-        if (PE) pe -= 0.5 * gm / r;
-      }
+    } else {
+      const double r = sqrt(p.d2);
+      const double inv_r3 = 1.0 / (p.d2 * r);
+      const double gm = gp.G * q.ma * mb;
+      const double de = gm * inv_r3;
+      q.fx = fma(de, p.dx, q.fx);
+      q.fy = fma(de, p.dy, q.fy);
+      q.fz = fma(de, p.dz, q.fz);
+      if (PE) q.pe -= 0.5 * gm / r;
     }
   }
-  a.fx[i] = fx;
-  a.fy[i] = fy;
-  a.fz[i] = fz;
-  if (PE) a.pe[i] = accumulate ? a.pe[i] + pe : pe;
+  __device__ __forceinline__ void stop(Acc& q, const pair::ParticleContext& c) const {
+    a.fx[c.i] = q.fx;
+    a.fy[c.i] = q.fy;
+    a.fz[c.i] = q.fz;
+    if (PE) a.pe[c.i] = accumulate ? a.pe[c.i] + q.pe : q.pe;
+  }
+};
+
+template <int P, bool PE>
+__global__ void __launch_bounds__(128) k_grav(uint32_t n_part, BatchSource src, GravForce<P, PE> f) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_part) pair::traverse_particle(src, i, f);
 }
 
 // field::type of the particles whose ids are listed (sorted ascending, n of
@@ -141,12 +133,13 @@ int launch_gravity(const Extent& ex, const SysDesc* sys, const SysState* st, con
   if (ex.n_part == 0) return 0;
   const int threads = 128;
   const int g = static_cast<int>((static_cast<long long>(ex.n_part) + threads - 1) / threads);
+  const BatchSource src(sys, st, a, sys_only);
   if (precision == kFp64Exact) {
-    if (with_pe) k_grav<kFp64Exact, true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only, gp, accumulate, flags);
-    else k_grav<kFp64Exact, false><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only, gp, accumulate, flags);
+    if (with_pe) k_grav<kFp64Exact, true><<<g, threads, 0, stream>>>(ex.n_part, src, {a, gp, accumulate, flags});
+    else k_grav<kFp64Exact, false><<<g, threads, 0, stream>>>(ex.n_part, src, {a, gp, accumulate, flags});
   } else {
-    if (with_pe) k_grav<kFp64, true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only, gp, accumulate, flags);
-    else k_grav<kFp64, false><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only, gp, accumulate, flags);
+    if (with_pe) k_grav<kFp64, true><<<g, threads, 0, stream>>>(ex.n_part, src, {a, gp, accumulate, flags});
+    else k_grav<kFp64, false><<<g, threads, 0, stream>>>(ex.n_part, src, {a, gp, accumulate, flags});
   }
   return 1;
 }

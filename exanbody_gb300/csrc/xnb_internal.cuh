@@ -18,9 +18,15 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "xnb_pair.cuh"
 #include "xnb_widen.h"
 
 namespace xnb {
+
+// the reference roundings shared with the public pair-functor API
+using pair::image_coord;
+using pair::image_coord_f;
+using pair::norm2_rn;
 
 constexpr int kImageCenter = 13;  // image code of the unshifted image: (0+1) + 3*(0+1) + 9*(0+1)
 
@@ -128,10 +134,8 @@ struct DevArrays {
 
 // ----------------------------------------------------------------------------
 // Exact FP64 helpers: the reference's arithmetic written with explicit rounding
-// so the compiler cannot contract to FMA.
-__device__ __forceinline__ double norm2_rn(double x, double y, double z) {
-  return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
-}
+// so the compiler cannot contract to FMA (norm2_rn and image_coord come from the
+// pair-functor header).
 
 // restore_u32_double (core/include/exanb/core/backup_r.h:31-34)
 __device__ __forceinline__ double restore_u32(uint32_t x, double o, double r) {
@@ -207,16 +211,6 @@ __device__ __forceinline__ void make_pf2(const SysDesc& s, double x, double y, d
   hi = make_float4(narrow_f64(rx), narrow_f64(ry), narrow_f64(rz), 0.f);
   lo = make_float4(narrow_f64(rx - widen_f32(hi.x)), narrow_f64(ry - widen_f32(hi.y)), narrow_f64(rz - widen_f32(hi.z)),
                    0.f);
-}
-
-__device__ __forceinline__ float image_coord_f(float x, float period, int d) {
-  return d == 1 ? x : (d == 2 ? x + period : x - period);
-}
-
-// Image offset along one axis for image code digit d in {0,1,2} (-1, 0, +1).
-__device__ __forceinline__ double image_coord(double x, double period, int d) {
-  // apply_coord_modifier: x + (SIDE ? 1.0 : -1.0) * (rmax - rmin) when shifted, x otherwise
-  return d == 1 ? x : __dadd_rn(x, __dmul_rn(d == 2 ? 1.0 : -1.0, period));
 }
 
 __device__ __forceinline__ double widen_f32(float f) {

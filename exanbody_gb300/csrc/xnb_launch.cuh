@@ -48,8 +48,16 @@ int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevA
 // block-per-cell build of the cells too large for it: three kernels). lbuf: the
 // largest slot rounded up to 32 entries, 0 above 1024 or when no system has a
 // slot yet; it sizes the shared-memory list buffers.
+// form: kBuildRows (lane per particle, rows of three cells bulk-copied into
+// shared memory, xnb_build_rows.cu) or kBuildWarp (lane per candidate, the
+// 27-cell block staged per warp); cells neither handles go to the
+// block-per-cell build.
+constexpr int kBuildRows = 0;
+constexpr int kBuildWarp = 1;
 int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int stage_cap,
-                     int lbuf, cudaStream_t stream);
+                     int lbuf, cudaStream_t stream, int form = kBuildRows);
+// the lane-per-particle build alone (cells it cannot take are appended to a.nbr_wide)
+int launch_neighbors_rows(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream);
 
 // Reference-format chunk-neighbour streams of system sid (xnb_stream.cu):
 // per-cell lengths (u16 units), the streams at cell_off, and the checker

@@ -203,8 +203,9 @@ __device__ __forceinline__ void mixed_pair(const SysDesc& S, uint32_t e, double 
 }
 
 // ---------------------------------------------------------------------------
-// zero_particle_force + lennard_jones_force over the neighbour lists.
-// compute_cell_particle_pairs_cell (compute/include/exanb/compute/
+// zero_particle_force + lennard_jones_force over the neighbour lists, as a
+// functor of the pair-functor API (include/xnb_pair.cuh) run through the batch
+// traversal. compute_cell_particle_pairs_cell (compute/include/exanb/compute/
 // compute_cell_particle_pairs_impl_default.h:148-238) walks each particle's
 // stream in (cell_enc, p_b) order with dr = r_b - r_a and keeps 0 < d2 <= rc^2;
 // LennardJonesForceFunctor (contribs/md/lennard_jones/lennard_jones.cu:67-102)
@@ -214,122 +215,74 @@ __device__ __forceinline__ void mixed_pair(const SysDesc& S, uint32_t e, double 
 //                    no contraction): bit-identical to the CPU restatement.
 //   P = kFp64      : same selection of pairs (exact d2 test), force from
 //                    1/d2 by Newton-Raphson, FMA accumulation.
-//   P = kMixed     : FP64 displacement and FP64 accumulation; r^2, r^-6 and the
-//                    force magnitude in FP32; the cutoff decision is made in FP32
-//                    where a proven margin allows and in FP64 otherwise, so the
-//                    pair set is the FP64 one. The displacement is applied
+//   P = kMixed     : raw entries (the functor forms the displacement): FP64
+//                    displacement and FP64 accumulation; r^2, r^-6 and the
+//                    force magnitude in FP32; the cutoff decision is made in
+//                    FP32 where a proven margin allows and in FP64 otherwise, so
+//                    the pair set is the FP64 one. The displacement is applied
 //                    once per particle (sum pd*r_b - r_a*sum pd, all in FP64)
 //                    and the FP32 factor is widened on the integer pipes: a
 //                    pair costs 3 DFMA + 1 DADD on the FP64 pipe.
 template <int P, bool PE, bool KICK>
-// 72 registers: 7 blocks of 128 threads per SM (measured faster than the
-// unconstrained 79 despite a few spilled bytes).
-__global__ void __maxnreg__(72)
-    k_force(uint32_t n_part, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a,
-            int sys_only) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x) {
-    const uint32_t c = a.pcell[i];
-    if (c == kInvalid) continue;
-    const uint32_t s = a.cell_sys[c];
-    if (sys_only >= 0 && s != static_cast<uint32_t>(sys_only)) continue;
-    if (st[s].error) continue;  // lists of a failed system are not trusted
-    const SysDesc& S = sys[s];
-    const double xa = a.rx[i], ya = a.ry[i], za = a.rz[i];
-    const uint32_t* __restrict__ L = a.nbr + S.list_base + a.nbr_start[i];
-    const uint32_t n = a.nbr_cnt[i];
-    const uint32_t pbase = S.part_base;
-    const double px = S.period[0], py = S.period[1], pz = S.period[2];
-    const double rcut2 = S.rcut2;
-    const float4 paf = a.pf[i];
-    const float4 pal = (P == kMixed) ? a.pflo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float pre_hi = S.rc2_f + S.pre_margin_f;
-    const float pfx = S.period_f[0], pfy = S.period_f[1], pfz = S.period_f[2];
-    double fx = 0.0, fy = 0.0, fz = 0.0, pe = 0.0, psum = 0.0;
-    const uint32_t self_e = ((i - pbase) << 5) | static_cast<uint32_t>(kImageCenter);
-    // Windows of 128 entries: the FP32 prefilter marks the entries that may lie
-    // within rc, then the FP64 block runs for the marked ones in list order, so
-    // a warp executes it as often as its busiest lane has marked entries.
-    if (P == kMixed) {
-      // Two marked entries per iteration: their list entries, then their five
-      // gathers each, are in flight together (list order is kept: b0 < b1).
-      for (uint32_t kw = 0; kw < n; kw += 128) {
-        Marks mk = prefilter_window(L, kw, min(n, kw + 128u), a.pf, pbase, self_e, paf, pfx, pfy, pfz, pre_hi);
-        uint32_t b0 = 0, b1 = 0;
-        bool h0 = next_mark(mk, b0);
-        while (h0) {
-          const bool h1 = next_mark(mk, b1);
-          const uint32_t e0 = __ldg(L + kw + b0);
-          const uint32_t e1 = __ldg(L + kw + (h1 ? b1 : b0));
-          const uint32_t j0 = pbase + (e0 >> 5), j1 = pbase + (e1 >> 5);
-          const double x0 = __ldg(a.rx + j0), y0 = __ldg(a.ry + j0), z0 = __ldg(a.rz + j0);
-          const double x1 = __ldg(a.rx + j1), y1 = __ldg(a.ry + j1), z1 = __ldg(a.rz + j1);
-          const float4 hi0 = __ldg(a.pf + j0), lo0 = __ldg(a.pflo + j0);
-          const float4 hi1 = __ldg(a.pf + j1), lo1 = __ldg(a.pflo + j1);
-          mixed_pair<PE>(S, e0, x0, y0, z0, hi0, lo0, xa, ya, za, paf, pal, rcut2, fx, fy, fz, psum, pe);
-          if (h1) mixed_pair<PE>(S, e1, x1, y1, z1, hi1, lo1, xa, ya, za, paf, pal, rcut2, fx, fy, fz, psum, pe);
-          h0 = h1 && next_mark(mk, b0);
-        }
+struct LJForce {
+  const SysDesc* __restrict__ sys;
+  DevArrays a;
+  struct Acc {
+    double fx, fy, fz, pe, psum;
+  };
+
+  __device__ __forceinline__ double rcut2(const pair::ParticleContext& c) const { return sys[c.sys].rcut2; }
+  __device__ __forceinline__ float prefilter_hi(const pair::ParticleContext& c) const {
+    const SysDesc& S = sys[c.sys];
+    return S.rc2_f + S.pre_margin_f;
+  }
+  __device__ __forceinline__ bool start(Acc& q, const pair::ParticleContext&) const {
+    q.fx = q.fy = q.fz = q.pe = q.psum = 0.0;
+    return true;
+  }
+  __device__ __forceinline__ void pair(Acc& q, const pair::ParticleContext& c, const pair::PairData& p) const {
+    const SysDesc& S = sys[c.sys];
+    if (P == kFp64Exact) {
+      // lj_compute_energy (lennard_jones.cu:46-56) then pair_de *= w / r with w = 1
+      const double r = __dsqrt_rn(p.d2);
+      const double inv_r = __ddiv_rn(1.0, r);
+      const double ratio = __dmul_rn(S.sigma, inv_r);
+      const double ratio2 = __dmul_rn(ratio, ratio);
+      const double ratio6 = __dmul_rn(__dmul_rn(ratio2, ratio2), ratio2);
+      const double ratio12 = __dmul_rn(ratio6, ratio6);
+      double de = __dmul_rn(__dmul_rn(S.m24eps, __dsub_rn(__dmul_rn(2.0, ratio12), ratio6)), inv_r);
+      de = __dmul_rn(de, inv_r);
+      q.fx = __dadd_rn(q.fx, __dmul_rn(de, p.dx));
+      q.fy = __dadd_rn(q.fy, __dmul_rn(de, p.dy));
+      q.fz = __dadd_rn(q.fz, __dmul_rn(de, p.dz));
+      if (PE) {
+        const double en = __dmul_rn(S.eps4, __dsub_rn(ratio12, ratio6));
+        q.pe = __dadd_rn(q.pe, __dmul_rn(0.5, __dsub_rn(en, S.e_shift)));
       }
     } else {
-      for (uint32_t kw = 0; kw < n; kw += 128) {
-       Marks mk = prefilter_window(L, kw, min(n, kw + 128u), a.pf, pbase, self_e, paf, pfx, pfy, pfz, pre_hi);
-       uint32_t b;
-       while (next_mark(mk, b)) {
-        const uint32_t e = __ldg(L + kw + b);
-        const uint32_t j = pbase + (e >> 5);
-        const uint32_t code = e & 31u;
-        double xb = __ldg(a.rx + j), yb = __ldg(a.ry + j), zb = __ldg(a.rz + j);
-        if (code != static_cast<uint32_t>(kImageCenter)) {
-          xb = image_coord(xb, px, static_cast<int>(code % 3u));
-          yb = image_coord(yb, py, static_cast<int>((code / 3u) % 3u));
-          zb = image_coord(zb, pz, static_cast<int>(code / 9u));
-        }
-        if (P == kFp64Exact) {
-          const double dx = __dsub_rn(xb, xa);
-          const double dy = __dsub_rn(yb, ya);
-          const double dz = __dsub_rn(zb, za);
-          const double d2 = norm2_rn(dx, dy, dz);
-          if (d2 > 0.0 && d2 <= rcut2) {
-            // lj_compute_energy (lennard_jones.cu:46-56) then pair_de *= w / r with w = 1
-            const double r = __dsqrt_rn(d2);
-            const double inv_r = __ddiv_rn(1.0, r);
-            const double ratio = __dmul_rn(S.sigma, inv_r);
-            const double ratio2 = __dmul_rn(ratio, ratio);
-            const double ratio6 = __dmul_rn(__dmul_rn(ratio2, ratio2), ratio2);
-            const double ratio12 = __dmul_rn(ratio6, ratio6);
-            double de = __dmul_rn(__dmul_rn(S.m24eps, __dsub_rn(__dmul_rn(2.0, ratio12), ratio6)), inv_r);
-            de = __dmul_rn(de, inv_r);
-            fx = __dadd_rn(fx, __dmul_rn(de, dx));
-            fy = __dadd_rn(fy, __dmul_rn(de, dy));
-            fz = __dadd_rn(fz, __dmul_rn(de, dz));
-            if (PE) {
-              const double en = __dmul_rn(S.eps4, __dsub_rn(ratio12, ratio6));
-              pe = __dadd_rn(pe, __dmul_rn(0.5, __dsub_rn(en, S.e_shift)));
-            }
-          }
-        } else if (P == kFp64) {
-          const double dx = __dsub_rn(xb, xa);
-          const double dy = __dsub_rn(yb, ya);
-          const double dz = __dsub_rn(zb, za);
-          const double d2 = norm2_rn(dx, dy, dz);
-          if (d2 > 0.0 && d2 <= rcut2) {
-            const double ir2 = rcp_nr(d2);
-            const double s2 = S.sig2 * ir2;
-            const double s6 = s2 * s2 * s2;
-            const double pd = S.eps24 * s6 * fma(-2.0, s6, 1.0) * ir2;
-            fx = fma(pd, dx, fx);
-            fy = fma(pd, dy, fy);
-            fz = fma(pd, dz, fz);
-            if (PE) pe += 0.5 * fma(S.eps4 * s6, s6 - 1.0, -S.e_shift);
-          }
-        }
-       }
-      }
+      const double ir2 = rcp_nr(p.d2);
+      const double s2 = S.sig2 * ir2;
+      const double s6 = s2 * s2 * s2;
+      const double pd = S.eps24 * s6 * fma(-2.0, s6, 1.0) * ir2;
+      q.fx = fma(pd, p.dx, q.fx);
+      q.fy = fma(pd, p.dy, q.fy);
+      q.fz = fma(pd, p.dz, q.fz);
+      if (PE) q.pe += 0.5 * fma(S.eps4 * s6, s6 - 1.0, -S.e_shift);
     }
+  }
+  __device__ __forceinline__ void entry(Acc& q, const pair::ParticleContext& c, const pair::RawEntry& r) const {
+    const SysDesc& S = sys[c.sys];
+    mixed_pair<PE>(S, r.e, r.xb, r.yb, r.zb, r.hb, r.lb, c.x, c.y, c.z, c.hi, c.lo, S.rcut2, q.fx, q.fy, q.fz,
+                   q.psum, q.pe);
+  }
+  __device__ __forceinline__ void stop(Acc& q, const pair::ParticleContext& c) const {
+    const SysDesc& S = sys[c.sys];
+    const uint32_t i = c.i;
+    double fx = q.fx, fy = q.fy, fz = q.fz;
     if (P == kMixed) {
-      fx = fma(-xa, psum, fx);
-      fy = fma(-ya, psum, fy);
-      fz = fma(-za, psum, fz);
+      fx = fma(-c.x, q.psum, fx);
+      fy = fma(-c.y, q.psum, fy);
+      fz = fma(-c.z, q.psum, fz);
     }
     // the force field was zeroed (zero_particle_force.cu:39-46) and receives the
     // sum; 0 + s differs from s only for s = -0, which the exact path keeps
@@ -347,7 +300,7 @@ __global__ void __maxnreg__(72)
     a.fx[i] = fx;
     a.fy[i] = fy;
     a.fz[i] = fz;
-    if (PE) a.pe[i] = pe;
+    if (PE) a.pe[i] = q.pe;
     if (KICK) {
       // verlet_second_half: push_f_v with dt_scale 0.5 (numerical-scheme.msp:17-18)
       const double h = S.dt_half;
@@ -362,6 +315,34 @@ __global__ void __maxnreg__(72)
       }
     }
   }
+};
+
+}  // namespace
+}  // namespace xnb
+
+namespace xnb {
+namespace pair {
+// The mixed path takes raw entries with both mirrors, two per iteration (both
+// entries' gathers in flight together; list order unchanged); the FP64 paths
+// take the traversal's FP64 pairs within rc.
+template <int P, bool PE, bool KICK>
+struct ComputePairTraits<LJForce<P, PE, KICK>> : DefaultPairTraits {
+  static constexpr bool RawEntries = (P == kMixed);
+  static constexpr bool GatherMirrors = (P == kMixed);
+  static constexpr int EntriesPerIteration = (P == kMixed) ? 2 : 1;
+};
+}  // namespace pair
+}  // namespace xnb
+
+namespace xnb {
+namespace {
+
+// 72 registers: 7 blocks of 128 threads per SM (measured faster than the
+// unconstrained 79 despite a few spilled bytes).
+template <int P, bool PE, bool KICK>
+__global__ void __maxnreg__(72) k_force(uint32_t n_part, BatchSource src, LJForce<P, PE, KICK> f) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x)
+    pair::traverse_particle(src, i, f);
 }
 
 // ---------------------------------------------------------------------------
@@ -417,11 +398,47 @@ __global__ void __launch_bounds__(256)
         }
       }
       if (!found) break;
-      double xb = __ldg(a.rx + j), yb = __ldg(a.ry + j), zb = __ldg(a.rz + j);
+      const double xbr = __ldg(a.rx + j), ybr = __ldg(a.ry + j), zbr = __ldg(a.rz + j);
+      double xb = xbr, yb = ybr, zb = zbr;
       if (code != static_cast<uint32_t>(kImageCenter)) {
         xb = image_coord(xb, px, static_cast<int>(code % 3u));
         yb = image_coord(yb, py, static_cast<int>((code / 3u) % 3u));
         zb = image_coord(zb, pz, static_cast<int>(code / 9u));
+      }
+      if (P == kFp64 && code != static_cast<uint32_t>(kImageCenter)) {
+        // The partner's reaction through a periodic image is evaluated as the
+        // partner's own full-list traversal would: b sees a through the
+        // opposite image (digits 2 - d) and rounds its own image coordinate
+        // x_a +- period, whose rounding differs from x_b -+ period far from the
+        // coordinate origin. Each side keeps its own cutoff decision.
+        const double xai = image_coord(xa, px, 2 - static_cast<int>(code % 3u));
+        const double yai = image_coord(ya, py, 2 - static_cast<int>((code / 3u) % 3u));
+        const double zai = image_coord(za, pz, 2 - static_cast<int>(code / 9u));
+        const double dxa = __dsub_rn(xb, xa), dya = __dsub_rn(yb, ya), dza = __dsub_rn(zb, za);
+        const double dxb = __dsub_rn(xai, xbr), dyb = __dsub_rn(yai, ybr), dzb = __dsub_rn(zai, zbr);
+        const double d2a = norm2_rn(dxa, dya, dza);
+        const double d2b = norm2_rn(dxb, dyb, dzb);
+        if (d2a > 0.0 && d2a <= rcut2) {
+          const double ir2 = rcp_nr(d2a);
+          const double s2 = S.sig2 * ir2;
+          const double s6 = s2 * s2 * s2;
+          const double pd = S.eps24 * s6 * fma(-2.0, s6, 1.0) * ir2;
+          fx += pd * dxa;
+          fy += pd * dya;
+          fz += pd * dza;
+          if (PE) pe += 0.5 * fma(S.eps4 * s6, s6 - 1.0, -S.e_shift);
+        }
+        if (d2b > 0.0 && d2b <= rcut2) {
+          const double ir2 = rcp_nr(d2b);
+          const double s2 = S.sig2 * ir2;
+          const double s6 = s2 * s2 * s2;
+          const double pd = S.eps24 * s6 * fma(-2.0, s6, 1.0) * ir2;
+          atomicAdd(a.fx + j, pd * dxb);
+          atomicAdd(a.fy + j, pd * dyb);
+          atomicAdd(a.fz + j, pd * dzb);
+          if (PE) atomicAdd(a.pe + j, 0.5 * fma(S.eps4 * s6, s6 - 1.0, -S.e_shift));
+        }
+        continue;
       }
       bool in;
       double pd = 0.0, en = 0.0;
@@ -577,8 +594,8 @@ template <int P, bool PE, bool KICK>
 void force_dispatch(const Extent& ex, const SysDesc* sys, const SysState* st, const DevArrays& a, int sys_only,
                     cudaStream_t stream) {
   const int threads = ex.force_block > 0 ? ex.force_block : 128;
-  k_force<P, PE, KICK><<<grid_for(ex.n_part, threads), threads, 0, stream>>>(ex.n_part, sys, st, a,
-                                                                                           sys_only);
+  k_force<P, PE, KICK><<<grid_for(ex.n_part, threads), threads, 0, stream>>>(
+      ex.n_part, BatchSource(sys, st, a, sys_only), LJForce<P, PE, KICK>{sys, a});
 }
 
 }  // namespace

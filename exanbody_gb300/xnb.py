@@ -18,6 +18,9 @@ PREC_NEWTON = 0x10
 PRECISIONS = {"fp64_exact": PREC_FP64_EXACT, "fp64": PREC_FP64, "mixed": PREC_MIXED,
               "fp64_newton": PREC_FP64 | PREC_NEWTON, "mixed_newton": PREC_MIXED | PREC_NEWTON}
 
+BUILD_ROWS = 0
+BUILD_WARP = 1
+
 STEP_HOST_SYNC = 1
 STEP_ENERGY = 2
 
@@ -40,7 +43,7 @@ EXPORTED = [
     "xnb_check_errors", "xnb_stats_kernel_launches", "xnb_chunk_neighbors_noalloc", "xnb_chunk_neighbors_stream",
     "xnb_verify_chunk_neighbors", "xnb_simulation_stats", "xnb_sample_particles", "xnb_system_set_types",
     "xnb_gravitational_force", "xnb_batch_set_tuning", "xnb_autotune", "xnb_snap_create", "xnb_snap_destroy",
-    "xnb_snap_force", "xnb_system_pairs_range",
+    "xnb_snap_force", "xnb_system_pairs_range", "xnb_system_pair_view", "xnb_batch_set_build_form",
 ]
 
 FORCE_ENERGY = 1
@@ -87,6 +90,8 @@ class Tuning(C.Structure):
         ("newton", C.c_int32),
         ("trials", C.c_int32),
         ("atom_steps_per_s", C.c_double),
+        ("build_form", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -114,6 +119,15 @@ class SystemInfo(C.Structure):
         ("active", C.c_int32),
         ("max_nbr", C.c_uint32),
     ]
+
+
+class PairView(C.Structure):
+    """xnb_pair_view: device pointers of one system for pair functors (include/xnb_pair.cuh)."""
+    _fields_ = [("n_particles", C.c_int64)] + [(k, C.c_void_p) for k in (
+        "rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz", "pe", "id", "type", "mirror", "mirror_lo", "nbr",
+        "nbr_start", "nbr_count", "nbr_half")] + [
+        ("origin", C.c_double * 3), ("period", C.c_double * 3), ("nbh_dist", C.c_double),
+        ("max_period", C.c_double), ("mass", C.c_double), ("divide_by_mass", C.c_int32), ("sys", C.c_int32)]
 
 
 class SnapParams(C.Structure):
@@ -161,6 +175,8 @@ def load(build_if_missing=True):
     lib.xnb_system_download.argtypes = [vp, i32] + [P(d)] * 9 + [P(u64), P(i32), P(d), vp]
     lib.xnb_system_pairs.argtypes = [vp, i32, P(u64), P(u64), P(i32), i64, P(i64), vp]
     lib.xnb_system_pairs_range.argtypes = [vp, i32, i64, i64, P(u64), P(i32), i64, P(i64), vp]
+    lib.xnb_system_pair_view.argtypes = [vp, i32, P(PairView)]
+    lib.xnb_batch_set_build_form.argtypes = [vp, i32]
     lib.xnb_system_energy.argtypes = [vp, i32, P(d), P(d), vp]
     lib.xnb_init_particles.argtypes = [vp, i32, i32, vp]
     lib.xnb_push_f_v_r.argtypes = [vp, i32, d, vp]
@@ -327,6 +343,12 @@ class Batch:
             raise XnbError(-4, "pairs_range: %d entries, %d requested" % (nout.value, len(b)))
         return b[: nout.value], cnt
 
+    def pair_view(self, s):
+        """The system's xnb_pair_view (for functors compiled against include/xnb_pair.cuh)."""
+        v = PairView()
+        _ck(self.lib.xnb_system_pair_view(self.h, s, C.byref(v)))
+        return v
+
     def energy(self, s):
         ke, pe = C.c_double(), C.c_double()
         _ck(self.lib.xnb_system_energy(self.h, s, C.byref(ke), C.byref(pe), self.stream))
@@ -425,6 +447,10 @@ class Batch:
 
     def set_tuning(self, stage_cap, force_block):
         _ck(self.lib.xnb_batch_set_tuning(self.h, int(stage_cap), int(force_block)))
+
+    def set_build_form(self, form):
+        """BUILD_ROWS (lane per particle, bulk-copied rows) or BUILD_WARP (lane per candidate)."""
+        _ck(self.lib.xnb_batch_set_build_form(self.h, int(form)))
 
     def autotune(self, trial_steps=20, precision=PREC_MIXED):
         """Online autotuner (xnb_autotune): the batch advances while it is timed and is

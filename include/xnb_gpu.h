@@ -194,12 +194,29 @@ typedef struct xnb_tuning {
   int32_t newton;             /* 1: XNB_PREC_NEWTON traversal */
   int32_t trials;             /* configurations timed */
   double atom_steps_per_s;    /* the chosen configuration's measured rate */
+  int32_t build_form;         /* XNB_BUILD_ROWS or XNB_BUILD_WARP */
+  int32_t reserved;
 } xnb_tuning;
+
+/* Neighbour-build kernels (both give the same lists, the reference's):
+ * XNB_BUILD_ROWS: one warp per cell, one lane per particle (two for cells of
+ *   33-64 particles); the 27 neighbour cells staged as 9 rows of three
+ *   x-adjacent cells, each cell's mirrors one bulk copy (cp.async.bulk) into
+ *   shared memory, the next row's copy in flight while the current row is tested.
+ * XNB_BUILD_WARP: one warp per cell, one lane per candidate; the whole 27-cell
+ *   block (up to stage_cap candidates) staged by the warp, four particles tested
+ *   per staged load with a ballot each.
+ * Cells neither form takes (more than 64 particles, or candidates over the
+ * stage) are built block-per-cell. */
+#define XNB_BUILD_ROWS 0
+#define XNB_BUILD_WARP 1
+int xnb_batch_set_build_form(xnb_batch* b, int32_t form);
 
 /* Changes the launch configuration of a live batch (same limits as at creation). */
 int xnb_batch_set_tuning(xnb_batch* b, int32_t stage_cap, int32_t force_block);
-/* Online autotuner: coordinate search over stage_cap {384, 640, 1024},
- * force_block {128, 256} and the Newton traversal, each configuration timed
+/* Online autotuner: coordinate search over the neighbour-build form
+ * {ROWS, WARP}, stage_cap {384, 640, 1024}, force_block {128, 256} and the
+ * Newton traversal, each configuration timed
  * (CUDA events on `stream`) over trial_steps of xnb_step without host sync
  * after one untimed step. The trials are real MD steps: the batch advances
  * (1 + trial_steps) x trials steps. The batch is left on the fastest
@@ -259,6 +276,42 @@ int xnb_system_set_types(xnb_batch* b, int32_t sys, const uint64_t* ids, const u
 #define XNB_FORCE_MIXED 4 /* xnb_snap_force: FP32 arithmetic for U, Z, Y and the adjoint */
 int xnb_gravitational_force(xnb_batch* b, int32_t sys, double G, const double* type_mass, int32_t ntypes,
                             double rcut, int32_t precision, int32_t flags, void* stream);
+
+/* ---- pair-functor API (include/xnb_pair.cuh) ---- */
+
+/* Device-side view of one resident system for pair functors compiled against
+ * include/xnb_pair.cuh: the arrays the traversal of compute_cell_particle_pairs
+ * (compute/include/exanb/compute/compute_cell_particle_pairs.h:119-245) reads
+ * and writes, over the lists built here. Particles are in storage order
+ * (0 .. n_particles-1); a list entry is (particle index << 5) | periodic image
+ * code. Pointers are device addresses into the batch's pools: valid until the
+ * system is removed or the batch destroyed; positions and lists change with
+ * every step and rebuild. */
+typedef struct xnb_pair_view {
+  int64_t n_particles;
+  const double *rx, *ry, *rz;
+  double *vx, *vy, *vz;
+  double *fx, *fy, *fz;
+  double* pe;                /* per-particle energy field */
+  const uint64_t* id;
+  const uint8_t* type;       /* field::type */
+  const void* mirror;        /* float4 per particle: fl32(r - origin) per axis, 0 */
+  const void* mirror_lo;     /* float4 per particle: fl32((r - origin) - mirror) per axis, 0 */
+  const uint32_t* nbr;       /* the system's list entries */
+  const uint32_t* nbr_start; /* per particle: its first entry in nbr */
+  const uint32_t* nbr_count; /* per particle: its list length */
+  const uint32_t* nbr_half;  /* per particle: entries ahead of the particle itself in the reference's
+                                (cell_enc, p_b) order, the lower half of the symmetric split */
+  double origin[3];
+  double period[3];          /* extent - origin: the periodic image offsets */
+  double nbh_dist;           /* rcut + rcut_inc the lists were built with */
+  double max_period;         /* largest period (the FP32 prefilter's error bound uses it) */
+  double mass;               /* the system's particle mass and its divide_by_mass flag */
+  int32_t divide_by_mass;
+  int32_t sys;
+} xnb_pair_view;
+/* Fills *out for system sys (no GPU work). */
+int xnb_system_pair_view(xnb_batch* b, int32_t sys, xnb_pair_view* out);
 
 /* ---- on-device observables ---- */
 

@@ -57,6 +57,7 @@ def _lib(kind="parity"):
     lib.xo_get_particles.argtypes = [C.c_void_p] + [P(d)] * 9 + [P(u64), P(i32), P(d)]
     lib.xo_set_types.argtypes = [C.c_void_p, P(u64), P(C.c_uint8), i64]
     lib.xo_gravitational_force.argtypes = [C.c_void_p, d, P(d), C.c_int32, d]
+    lib.xo_morse_force.argtypes = [C.c_void_p, d, d, d, d]
     lib.xo_get_cell_counts.argtypes = [C.c_void_p, P(i64)]
     lib.xo_get_pairs.argtypes = [C.c_void_p, P(u64), P(u64), P(i32)]
     lib.xo_pair_count_cells.restype = i64
@@ -219,6 +220,11 @@ class OracleSystem:
         rc = self.lib.xo_gravitational_force(self.h, float(G), _ptr(masses, C.c_double), len(masses), float(rcut))
         if rc != 0:
             raise RuntimeError("oracle gravitational_force failed: %d" % rc)
+
+    def morse_force(self, D, alpha, r0, rcut):
+        rc = self.lib.xo_morse_force(self.h, float(D), float(alpha), float(r0), float(rcut))
+        if rc != 0:
+            raise RuntimeError("oracle morse_force failed: %d" % rc)
 
     def energy(self):
         ke, pe = C.c_double(), C.c_double()

@@ -738,6 +738,68 @@ struct xo_sys {
     return err ? -4 : 0;
   }
 
+  /* zero_particle_force + a Morse pair potential as a buffer-less functor over
+   * the streams (the reference has no Morse functor; this restates the
+   * published form V(r) = D (exp(-2a(r-r0)) - 2 exp(-a(r-r0))) for the
+   * pair-functor API test): per stream entry inside rcut, in stream order
+   * (compute_cell_particle_pairs_impl_default.h:186-205), with dr = r_b - r_a,
+   * e1 = exp(-a(r-r0)), e2 = e1*e1, dV/dr = 2aD(e1 - e2), f_a += (dV/dr / r) dr,
+   * and 0.5 (V(r) - V(rcut)) per entry as the particle's energy. */
+  int morse_forces(double D, double alpha, double r0, double rcut_m) {
+    const double rc2 = rcut_m * rcut_m;
+    const double ec1 = std::exp(-alpha * (rcut_m - r0));
+    const double e_shift = D * (ec1 * ec1 - 2.0 * ec1);
+#pragma omp parallel for schedule(dynamic)
+    for (long c = 0; c < static_cast<long>(cells.size()); ++c) {
+      Cell& A = cells[c];
+      const L3 la = gloc(c);
+      for (size_t q = 0; q < A.size(); ++q) { A.fx[q] = 0.0; A.fy[q] = 0.0; A.fz[q] = 0.0; A.pe[q] = 0.0; }
+      if (is_ghost(la)) continue;
+      const size_t na = A.size();
+      if (na == 0) continue;
+      const uint16_t* base = streams[c].data();
+      const uint16_t* stream_base = base + (na + 1) * 2;
+      const uint32_t* offset = reinterpret_cast<const uint32_t*>(base);
+      for (size_t pa = 0; pa < na; ++pa) {
+        const uint16_t* st = stream_base + offset[pa] - 1;
+        int groups = *(st++);
+        double fx = 0.0, fy = 0.0, fz = 0.0, e_sum = 0.0;
+        while (groups > 0) {
+          const uint16_t enc = *(st++);
+          int nch = *(st++);
+          const long ri = static_cast<long>(enc & 31) - 16;
+          const long rj = static_cast<long>((enc >> 5) & 31) - 16;
+          const long rk = static_cast<long>((enc >> 10) & 31) - 16;
+          const Cell& B = cells[c + ((rk * G[1]) + rj) * G[0] + ri];
+          --groups;
+          while (nch > 0) {
+            const unsigned pb = *(st++);
+            --nch;
+            const double drx = B.rx[pb] - A.rx[pa];
+            const double dry = B.ry[pb] - A.ry[pa];
+            const double drz = B.rz[pb] - A.rz[pa];
+            const double d2 = norm2(drx, dry, drz);
+            if (d2 > 0.0 && d2 <= rc2) {
+              const double r = std::sqrt(d2);
+              const double e1 = std::exp(-alpha * (r - r0));
+              const double e2 = e1 * e1;
+              const double s = 2.0 * alpha * D * (e1 - e2) / r;
+              fx += s * drx;
+              fy += s * dry;
+              fz += s * drz;
+              e_sum += 0.5 * (D * (e2 - 2.0 * e1) - e_shift);
+            }
+          }
+        }
+        A.fx[pa] = fx;
+        A.fy[pa] = fy;
+        A.fz[pa] = fz;
+        A.pe[pa] = e_sum;
+      }
+    }
+    return 0;
+  }
+
   /* type of each particle by id; ghost copies follow their owner */
   int set_types(const uint64_t* ids, const uint8_t* types, int64_t n) {
     std::vector<std::pair<uint64_t, uint8_t>> t(static_cast<size_t>(n));
@@ -1149,6 +1211,10 @@ int xo_set_snap(xo_sys* s, int32_t twojmax, double rcutfac, double rfac0, double
 
 int xo_gravitational_force(xo_sys* s, double G, const double* type_mass, int32_t ntypes, double rcut) {
   return s->gravitational_forces(G, type_mass, ntypes, rcut);
+}
+
+int xo_morse_force(xo_sys* s, double D, double alpha, double r0, double rcut) {
+  return s->morse_forces(D, alpha, r0, rcut);
 }
 
 int xo_energy(const xo_sys* s, double* ke, double* pe) {

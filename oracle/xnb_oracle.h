@@ -97,6 +97,10 @@ int xo_set_types(xo_sys* s, const uint64_t* ids, const uint8_t* types, int64_t n
 /* zero_particle_force + gravitational_force (contribs/pi/gravitational_force.cu:42-141)
  * over the current streams with cutoff rcut (<= the neighbour distance); masses per type. */
 int xo_gravitational_force(xo_sys* s, double G, const double* type_mass, int32_t ntypes, double rcut);
+/* zero_particle_force + a Morse pair potential D (exp(-2a(r-r0)) - 2 exp(-a(r-r0))),
+ * shifted to 0 at rcut (<= the neighbour distance), over the current streams:
+ * the user-written functor of the pair-functor API test. */
+int xo_morse_force(xo_sys* s, double D, double alpha, double r0, double rcut);
 /* From now on the force chain is snap_force_generic (linear SNAP, one element
  * set: chemflag, bnormflag, quadraticflag, switchinnerflag off), followed by
  * update_force_from_ghost and, when the system divides by mass, the division.
