@@ -100,6 +100,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--force-block", type=int, default=0, help="threads per block of the force kernel (0: library default)")
     ap.add_argument("--stage-cap", type=int, default=0, help="neighbour-build staging candidates (0: library default)")
+    ap.add_argument("--build-form", default="", choices=["", "rows", "warp"],
+                    help="neighbour-build kernel (empty: library default)")
     ap.add_argument("--workload", default="lj", choices=["lj", "snap_ni", "snap_mo"],
                     help="lj: the 4M-atom LJ headline; snap_*: the reference's SNAP benchmark decks")
     return ap.parse_args()
@@ -270,6 +272,8 @@ def run_ours(args):
         b = xnb.Batch(N + 64, ncell + 64, int(N * 160) + 4096, max_systems=1, device=local,
                       stage_cap=args.stage_cap, force_block=args.force_block)
         b.stream = sp
+        if args.build_form:
+            b.set_build_form({"rows": xnb.BUILD_ROWS, "warp": xnb.BUILD_WARP}[args.build_form])
         return b
 
     def timed(fn, reps=1):

@@ -189,6 +189,14 @@ SysDesc make_desc(const xnb_lj_params& p) {
                    !std::signbit(p.origin[1]) && p.origin[2] == 0.0 && !std::signbit(p.origin[2]))
                       ? 1
                       : 0;
+  {
+    double P = 0.0, X = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      P = std::max(P, std::fabs(p.extent[a] - p.origin[a]));
+      X = std::max(X, std::max(std::fabs(p.origin[a]), std::fabs(p.extent[a])));
+    }
+    d.far_coords = X > 4.0 * P ? 1 : 0;
+  }
   d.cell_size = p.cell_size;
   const double ghost_dist = (p.rcut + p.rcut_inc) / 1.0;  // nbh_dist.cpp:63-65
   for (int a = 0; a < 3; ++a) {

@@ -233,7 +233,7 @@ __device__ __forceinline__ void test_row(RowsWarp& w, const SysDesc& S, const De
           const uint32_t idx = k + static_cast<uint32_t>(j);
           if (pi[q] == kInvalid) {
             hit[q][j] = false;
-          } else if (idx == pself[q]) {
+          } else if (self_here && idx == pself[q]) {
             hit[q][j] = false;
             // the particle's own position in (cell_enc, p_b) order: the entries
             // before it are the lower half of the symmetric split
@@ -343,7 +343,7 @@ __device__ __forceinline__ bool rows_cell(RowsWarp& w, const SysDesc& S, SysStat
       }
     }
     __syncwarp();
-    uint32_t self_lo = 0, self_hi = 0;
+    uint32_t self_lo = 0, self_hi = 0;  // outside the centre row no candidate is the particle itself
     if (r == 4) {
       // the centre cell is group 1 of the centre row: its particles' own entries
       self_lo = n0;

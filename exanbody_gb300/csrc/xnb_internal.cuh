@@ -74,6 +74,9 @@ struct SysDesc {
   int32_t divide_by_mass;
   int32_t amr_enabled;
   int32_t origin_zero;  // origin is (+0, +0, +0): x - origin is x itself, no subtraction needed
+  int32_t far_coords;   // coordinates beyond 4 periods: image coordinates x +- period round coarser than
+                        // the displacements they form (the Newton FP64 traversal then evaluates each
+                        // reaction across an image from the partner's own side)
   uint32_t cell_base, ncells;
   uint32_t part_base, npart;
   uint64_t list_base;  // first entry of the system's list segment

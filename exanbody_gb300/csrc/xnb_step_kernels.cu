@@ -405,12 +405,15 @@ __global__ void __launch_bounds__(256)
         yb = image_coord(yb, py, static_cast<int>((code / 3u) % 3u));
         zb = image_coord(zb, pz, static_cast<int>(code / 9u));
       }
-      if (P == kFp64 && code != static_cast<uint32_t>(kImageCenter)) {
-        // The partner's reaction through a periodic image is evaluated as the
+      if (P == kFp64 && code != static_cast<uint32_t>(kImageCenter) && S.far_coords) {
+        // Far from the coordinate origin (coordinates beyond 4 periods) the
+        // partner's reaction through a periodic image is evaluated as the
         // partner's own full-list traversal would: b sees a through the
         // opposite image (digits 2 - d) and rounds its own image coordinate
-        // x_a +- period, whose rounding differs from x_b -+ period far from the
-        // coordinate origin. Each side keeps its own cutoff decision.
+        // x_a +- period, whose rounding there exceeds the displacements'
+        // resolution and differs from that of x_b -+ period. Each side keeps
+        // its own cutoff decision. (A per-system flag: the branch is uniform,
+        // and domains near the origin keep the single evaluation.)
         const double xai = image_coord(xa, px, 2 - static_cast<int>(code % 3u));
         const double yai = image_coord(ya, py, 2 - static_cast<int>((code / 3u) % 3u));
         const double zai = image_coord(za, pz, 2 - static_cast<int>(code / 9u));

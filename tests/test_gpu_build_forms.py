@@ -27,7 +27,7 @@ CASES = [
 @pytest.mark.parametrize("n,rho,T,seed,steps", CASES)
 def test_build_form_lists_equal_the_oracle(form, n, rho, T, seed, steps):
     w = workloads.lj_fcc_system(n, rho, T, seed)
-    b = new_batch([w["n_atoms"]], [ncells(w["geom"])])
+    b = new_batch([w["n_atoms"]], [ncells(w["geom"])], list_per_atom=max(170.0, 220.0 * rho))
     s = b.add_system(xnb.lj_params(w["geom"]), w["r"], w["v"], w["id"])
     b.set_build_form(form)
     b.init_particles(s, xnb.PREC_FP64_EXACT)
