@@ -102,6 +102,8 @@ def parse():
     ap.add_argument("--stage-cap", type=int, default=0, help="neighbour-build staging candidates (0: library default)")
     ap.add_argument("--build-form", default="", choices=["", "rows", "warp"],
                     help="neighbour-build kernel (empty: library default)")
+    ap.add_argument("--force-lanes", type=int, default=0, choices=[0, 1, 2, 4],
+                    help="threads per particle of the FP64 / mixed force traversal (0: library default)")
     ap.add_argument("--workload", default="lj", choices=["lj", "snap_ni", "snap_mo"],
                     help="lj: the 4M-atom LJ headline; snap_*: the reference's SNAP benchmark decks")
     return ap.parse_args()
@@ -274,6 +276,8 @@ def run_ours(args):
         b.stream = sp
         if args.build_form:
             b.set_build_form({"rows": xnb.BUILD_ROWS, "warp": xnb.BUILD_WARP}[args.build_form])
+        if args.force_lanes:
+            b.set_force_lanes(args.force_lanes)
         return b
 
     def timed(fn, reps=1):

@@ -97,6 +97,7 @@ struct xnb_batch {
   xnb_batch_config cfg{};
   int stage_cap = 640;
   int force_block = 128;
+  int force_lanes = 1;          // threads per particle of the FP64 / mixed force traversal
   int build_form = kBuildWarp;  // neighbour-build kernel (xnb_batch_set_build_form)
   DevArrays a{};
   SysDesc* d_sys = nullptr;
@@ -119,6 +120,7 @@ struct xnb_batch {
     e.nsys = hw;
     e.sm_count = sm_count;
     e.force_block = force_block;
+    e.force_lanes = force_lanes;
     return e;
   }
 };
@@ -127,6 +129,10 @@ struct xnb_graph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   xnb_batch* batch = nullptr;
+  // what the captured launches depend on besides device memory: the batch's
+  // work extent and launch configuration at capture
+  uint32_t n_part = 0, n_cells = 0;
+  int nsys = 0, lbuf = 0, stage_cap = 0, force_block = 0, force_lanes = 0, build_form = 0;
 };
 
 namespace {
@@ -1058,6 +1064,15 @@ int xnb_step_graph_create(xnb_batch* b, int32_t nsteps, int32_t precision, int32
   xnb_graph* G = new xnb_graph();
   G->graph = g;
   G->batch = b;
+  const Extent ex = b->extent();
+  G->n_part = ex.n_part;
+  G->n_cells = ex.n_cells;
+  G->nsys = ex.nsys;
+  G->lbuf = list_buf(b);
+  G->stage_cap = b->stage_cap;
+  G->force_block = b->force_block;
+  G->force_lanes = b->force_lanes;
+  G->build_form = b->build_form;
   const cudaError_t ie = cudaGraphInstantiate(&G->exec, g, 0);
   if (ie != cudaSuccess) {
     cudaGraphDestroy(g);
@@ -1068,8 +1083,23 @@ int xnb_step_graph_create(xnb_batch* b, int32_t nsteps, int32_t precision, int32
   return XNB_OK;
 }
 
+int xnb_graph_is_current(const xnb_graph* g) {
+  if (!g || !g->batch) return 0;
+  const xnb_batch* b = g->batch;
+  const Extent ex = b->extent();
+  return (ex.n_part == g->n_part && ex.n_cells == g->n_cells && ex.nsys == g->nsys && list_buf(b) == g->lbuf &&
+          b->stage_cap == g->stage_cap && b->force_block == g->force_block && b->force_lanes == g->force_lanes &&
+          b->build_form == g->build_form)
+             ? 1
+             : 0;
+}
+
 int xnb_graph_launch(xnb_graph* g, void* stream) {
   if (!g) return fail(XNB_ERR_ARG, "null graph");
+  // a graph captured for a smaller extent would skip the particles and cells of
+  // systems added beyond it: refuse instead of stepping part of the batch
+  if (!xnb_graph_is_current(g))
+    return fail(XNB_ERR_ARG, "the batch's extent or launch configuration changed since the graph was captured");
   XCK(cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream)));
   return XNB_OK;
 }
@@ -1106,6 +1136,13 @@ int xnb_batch_set_tuning(xnb_batch* b, int32_t stage_cap, int32_t force_block) {
   return XNB_OK;
 }
 
+int xnb_batch_set_force_lanes(xnb_batch* b, int32_t lanes) {
+  if (!b) return fail(XNB_ERR_ARG, "null batch");
+  if (lanes != 1 && lanes != 2 && lanes != 4) return fail(XNB_ERR_ARG, "force lanes per particle must be 1, 2 or 4");
+  b->force_lanes = lanes;
+  return XNB_OK;
+}
+
 int xnb_batch_set_build_form(xnb_batch* b, int32_t form) {
   if (!b) return fail(XNB_ERR_ARG, "null batch");
   if (form != XNB_BUILD_ROWS && form != XNB_BUILD_WARP) return fail(XNB_ERR_ARG, "unknown neighbour-build form");
@@ -1128,10 +1165,12 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
   XCK(cudaEventCreate(&e0));
   XCK(cudaEventCreate(&e1));
   int trials = 0;
-  auto rate_of = [&](int sc, int fb, int nw, int bf, double* rate) -> int {
+  auto rate_of = [&](int sc, int fb, int nw, int bf, int fl, double* rate) -> int {
     int rc = xnb_batch_set_tuning(b, sc, fb);
     if (rc) return rc;
     rc = xnb_batch_set_build_form(b, bf);
+    if (rc) return rc;
+    rc = xnb_batch_set_force_lanes(b, fl);
     if (rc) return rc;
     const int32_t prec = precision | (nw ? XNB_PREC_NEWTON : 0);
     rc = xnb_step(b, 1, prec, 0, stream);
@@ -1147,31 +1186,35 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
     *rate = static_cast<double>(atoms) * trial_steps / (static_cast<double>(ms) * 1e-3);
     return xnb_check_errors(b, stream);
   };
-  const int caps[3] = {384, 640, 1024}, blocks[2] = {128, 256}, forms[2] = {XNB_BUILD_ROWS, XNB_BUILD_WARP};
-  int best_sc = b->stage_cap, best_fb = b->force_block, best_nw = 0;
+  const int caps[3] = {384, 640, 1024}, blocks[2] = {128, 256}, forms[2] = {XNB_BUILD_ROWS, XNB_BUILD_WARP},
+            lanes[3] = {1, 2, 4};
+  int best_sc = b->stage_cap, best_fb = b->force_block, best_nw = 0, best_fl = b->force_lanes;
   int best_bf = b->build_form == kBuildRows ? XNB_BUILD_ROWS : XNB_BUILD_WARP;
   double best = 0.0;
-  int rc = rate_of(best_sc, best_fb, best_nw, best_bf, &best);
+  int rc = rate_of(best_sc, best_fb, best_nw, best_bf, best_fl, &best);
   // coordinate search: one parameter at a time, the others at their best so far
-  // (neighbour-build form, then the stage cap of the forms that stage whole
-  // neighbourhoods, the force block size and the Newton traversal)
-  const int nvals[4] = {2, 3, 2, 2};
-  for (int pass = 0; pass < 4 && rc == 0; ++pass) {
+  // (neighbour-build form, the stage cap of the forms that stage whole
+  // neighbourhoods, the force block size, threads per particle of the force
+  // traversal and the Newton traversal)
+  const int nvals[5] = {2, 3, 2, 3, 2};
+  for (int pass = 0; pass < 5 && rc == 0; ++pass) {
     for (int v = 0; v < nvals[pass] && rc == 0; ++v) {
-      int sc = best_sc, fb = best_fb, nw = best_nw, bf = best_bf;
+      int sc = best_sc, fb = best_fb, nw = best_nw, bf = best_bf, fl = best_fl;
       if (pass == 0) bf = forms[v];
       else if (pass == 1) sc = caps[v];
       else if (pass == 2) fb = blocks[v];
+      else if (pass == 3) fl = lanes[v];
       else nw = v;
-      if (sc == best_sc && fb == best_fb && nw == best_nw && bf == best_bf) continue;
+      if (sc == best_sc && fb == best_fb && nw == best_nw && bf == best_bf && fl == best_fl) continue;
       double r = 0.0;
-      rc = rate_of(sc, fb, nw, bf, &r);
+      rc = rate_of(sc, fb, nw, bf, fl, &r);
       if (rc == 0 && r > best) {
         best = r;
         best_sc = sc;
         best_fb = fb;
         best_nw = nw;
         best_bf = bf;
+        best_fl = fl;
       }
     }
   }
@@ -1182,9 +1225,12 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
   if (rc) return rc;
   rc = xnb_batch_set_build_form(b, best_bf);
   if (rc) return rc;
+  rc = xnb_batch_set_force_lanes(b, best_fl);
+  if (rc) return rc;
   out->stage_cap = best_sc;
   out->force_block = best_fb;
   out->build_form = best_bf;
+  out->force_lanes = best_fl;
   out->newton = best_nw;
   out->trials = trials;
   out->atom_steps_per_s = best;

@@ -275,6 +275,13 @@ struct LJForce {
     mixed_pair<PE>(S, r.e, r.xb, r.yb, r.zb, r.hb, r.lb, c.x, c.y, c.z, c.hi, c.lo, S.rcut2, q.fx, q.fy, q.fz,
                    q.psum, q.pe);
   }
+  __device__ __forceinline__ void combine(Acc& q, const Acc& o) const {
+    q.fx += o.fx;
+    q.fy += o.fy;
+    q.fz += o.fz;
+    q.pe += o.pe;
+    q.psum += o.psum;
+  }
   __device__ __forceinline__ void stop(Acc& q, const pair::ParticleContext& c) const {
     const SysDesc& S = sys[c.sys];
     const uint32_t i = c.i;
@@ -343,6 +350,21 @@ template <int P, bool PE, bool KICK>
 __global__ void __maxnreg__(72) k_force(uint32_t n_part, BatchSource src, LJForce<P, PE, KICK> f) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x)
     pair::traverse_particle(src, i, f);
+}
+
+// LANES threads per particle (FP64 and mixed): each takes every LANES-th
+// 8-entry block of the particle's list and the partial sums are combined in a
+// fixed order, so the result is reproducible (it agrees with the one-lane
+// traversal to rounding). The whole warp iterates together: the shuffles of
+// the combination span it.
+template <int P, bool PE, bool KICK, int LANES>
+__global__ void __maxnreg__(72) k_force_lanes(uint32_t n_part, BatchSource src, LJForce<P, PE, KICK> f) {
+  const uint64_t total = static_cast<uint64_t>(n_part) * LANES;
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t base = static_cast<uint64_t>(blockIdx.x) * blockDim.x; base < total; base += stride) {
+    const uint64_t t = base + threadIdx.x;
+    pair::traverse_particle_lanes<LANES>(src, static_cast<uint32_t>(t / LANES), t < total, f);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -597,8 +619,20 @@ template <int P, bool PE, bool KICK>
 void force_dispatch(const Extent& ex, const SysDesc* sys, const SysState* st, const DevArrays& a, int sys_only,
                     cudaStream_t stream) {
   const int threads = ex.force_block > 0 ? ex.force_block : 128;
-  k_force<P, PE, KICK><<<grid_for(ex.n_part, threads), threads, 0, stream>>>(
-      ex.n_part, BatchSource(sys, st, a, sys_only), LJForce<P, PE, KICK>{sys, a});
+  const BatchSource src(sys, st, a, sys_only);
+  const LJForce<P, PE, KICK> f{sys, a};
+  // the bit-exact path keeps one thread per particle (the reference's summation order)
+  if constexpr (P != kFp64Exact) {
+    if (ex.force_lanes == 2) {
+      k_force_lanes<P, PE, KICK, 2><<<grid_for(ex.n_part * 2u, threads), threads, 0, stream>>>(ex.n_part, src, f);
+      return;
+    }
+    if (ex.force_lanes == 4) {
+      k_force_lanes<P, PE, KICK, 4><<<grid_for(ex.n_part * 4u, threads), threads, 0, stream>>>(ex.n_part, src, f);
+      return;
+    }
+  }
+  k_force<P, PE, KICK><<<grid_for(ex.n_part, threads), threads, 0, stream>>>(ex.n_part, src, f);
 }
 
 }  // namespace

@@ -6,11 +6,12 @@ included), and the step sequence is captured as a CUDA graph
 (xnb_step_graph_create) so a chunk of steps costs one launch on the host.
 
 The autotuner times short trials of the batch over the tunables the library
-exposes -- neighbour-build staging capacity (candidates per warp chunk),
-force-traversal threads per block, the force traversal itself (full lists or
-Newton half lists) and, when asked, the Verlet skin -- and keeps the fastest.
+exposes -- the neighbour-build kernel (lane per candidate or lane per particle
+with bulk-copied rows), its staging capacity, force-traversal threads per
+block and threads per particle, the force traversal itself (full lists or
+Newton half lists) and the Verlet skin -- and keeps the fastest.
 
-  python -m exanbody_gb300.ensemble [--count 1024] [--steps 500] [--autotune]
+  python -m exanbody_gb300.ensemble [--count 1024] [--steps 500] [--autotune] [--no-tune-skin]
 """
 import argparse
 import ctypes
@@ -22,7 +23,8 @@ import numpy as np
 
 from . import replicas, workloads, xnb
 
-DEFAULTS = dict(stage_cap=640, force_block=128, skin=0.3, newton=False)
+DEFAULTS = dict(build_form="warp", stage_cap=640, force_block=128, force_lanes=1, skin=0.3, newton=False)
+FORMS = {"warp": xnb.BUILD_WARP, "rows": xnb.BUILD_ROWS}
 
 
 def make_systems(specs, rcut=2.5, skin=0.3):
@@ -30,7 +32,7 @@ def make_systems(specs, rcut=2.5, skin=0.3):
 
 
 def build_batch(systems, stage_cap=640, force_block=128, skin=0.3, rcut=2.5, dt=0.005, stream=None,
-                precision=xnb.PREC_MIXED, list_per_atom=None):
+                precision=xnb.PREC_MIXED, list_per_atom=None, build_form="warp", force_lanes=1):
     n_atoms = sum(w["n_atoms"] for w in systems)
     n_cells = sum(int(np.prod(w["geom"]["dims"])) for w in systems)
     if list_per_atom is None:
@@ -41,6 +43,8 @@ def build_batch(systems, stage_cap=640, force_block=128, skin=0.3, rcut=2.5, dt=
                   max_systems=len(systems), stage_cap=stage_cap, force_block=force_block)
     if stream is not None:
         b.stream = ctypes.c_void_p(stream)
+    b.set_build_form(FORMS[build_form])
+    b.set_force_lanes(force_lanes)
     ids = [b.add_system(xnb.lj_params(w["geom"], rcut=rcut, rcut_inc=skin, dt=dt), w["r"], w["v"], w["id"],
                         list_factor=1.25) for w in systems]
     b.init_particles(-1, precision)
@@ -69,7 +73,7 @@ def timed_steps(batch, stream, steps, precision, chunk=10):
 def trial(systems, cfg, steps, precision, stream):
     prec = precision | (xnb.PREC_NEWTON if cfg["newton"] else 0)
     b, ids, n = build_batch(systems, cfg["stage_cap"], cfg["force_block"], cfg["skin"], stream=stream.cuda_stream,
-                            precision=prec)
+                            precision=prec, build_form=cfg["build_form"], force_lanes=cfg["force_lanes"])
     try:
         secs, done = timed_steps(b, stream, steps, prec)
     finally:
@@ -83,15 +87,17 @@ def autotune(systems, precision=xnb.PREC_MIXED, steps=40, tune_skin=False, strea
 
     stream = stream or torch.cuda.Stream()
     space = {
+        "build_form": ["warp", "rows"],
         "stage_cap": [384, 640, 1024],
         "force_block": [128, 256],
+        "force_lanes": [1, 2, 4],
         "newton": [False, True],
         "skin": [0.3, 0.4, 0.5] if tune_skin else [0.3],
     }
     best = dict(DEFAULTS)
     best_rate = trial(systems, best, steps, precision, stream)
     log = [dict(best, rate=best_rate)]
-    for key in ("stage_cap", "force_block", "newton", "skin"):
+    for key in ("build_form", "stage_cap", "force_block", "force_lanes", "newton", "skin"):
         for v in space[key]:
             if v == best[key]:
                 continue
@@ -109,7 +115,7 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--autotune", action="store_true")
-    ap.add_argument("--tune-skin", action="store_true")
+    ap.add_argument("--no-tune-skin", action="store_true", help="keep the Verlet skin at 0.3")
     ap.add_argument("--tune-sample", type=int, default=128, help="systems used for the autotuner trials")
     args = ap.parse_args()
     import torch
@@ -131,7 +137,7 @@ def main():
     t0 = time.perf_counter()
     if args.autotune:
         sample = systems[: args.tune_sample]
-        cfg, _, tune_log = autotune(sample, xnb.PREC_MIXED, tune_skin=args.tune_skin, stream=stream)
+        cfg, _, tune_log = autotune(sample, xnb.PREC_MIXED, tune_skin=not args.no_tune_skin, stream=stream)
     tune_s = time.perf_counter() - t0
     out = {"workload": "ensemble_%d_fcc_n4-25_rho0.70-1.00_T0.7-1.5" % args.count, "gpus": world,
            "atoms": int(replicas.gather_values([sum(w["n_atoms"] for w in systems)], device=dev).sum()),
@@ -143,7 +149,8 @@ def main():
             ("fp64_full", xnb.PREC_FP64), ("fp64_newton", xnb.PREC_FP64 | xnb.PREC_NEWTON)]
     for name, prec in runs:
         b, ids, n = build_batch(systems, cfg["stage_cap"], cfg["force_block"], cfg["skin"],
-                                stream=stream.cuda_stream, precision=prec)
+                                stream=stream.cuda_stream, precision=prec, build_form=cfg["build_form"],
+                                force_lanes=cfg["force_lanes"])
         secs, done = timed_steps(b, stream, args.steps, prec)
         rebuilds = sum(b.info(s).rebuilds for s in ids)
         b.close()

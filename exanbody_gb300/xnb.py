@@ -44,6 +44,7 @@ EXPORTED = [
     "xnb_verify_chunk_neighbors", "xnb_simulation_stats", "xnb_sample_particles", "xnb_system_set_types",
     "xnb_gravitational_force", "xnb_batch_set_tuning", "xnb_autotune", "xnb_snap_create", "xnb_snap_destroy",
     "xnb_snap_force", "xnb_system_pairs_range", "xnb_system_pair_view", "xnb_batch_set_build_form",
+    "xnb_graph_is_current", "xnb_batch_set_force_lanes",
 ]
 
 FORCE_ENERGY = 1
@@ -91,7 +92,7 @@ class Tuning(C.Structure):
         ("trials", C.c_int32),
         ("atom_steps_per_s", C.c_double),
         ("build_form", C.c_int32),
-        ("reserved", C.c_int32),
+        ("force_lanes", C.c_int32),
     ]
 
 
@@ -177,6 +178,8 @@ def load(build_if_missing=True):
     lib.xnb_system_pairs_range.argtypes = [vp, i32, i64, i64, P(u64), P(i32), i64, P(i64), vp]
     lib.xnb_system_pair_view.argtypes = [vp, i32, P(PairView)]
     lib.xnb_batch_set_build_form.argtypes = [vp, i32]
+    lib.xnb_graph_is_current.argtypes = [vp]
+    lib.xnb_batch_set_force_lanes.argtypes = [vp, i32]
     lib.xnb_system_energy.argtypes = [vp, i32, P(d), P(d), vp]
     lib.xnb_init_particles.argtypes = [vp, i32, i32, vp]
     lib.xnb_push_f_v_r.argtypes = [vp, i32, d, vp]
@@ -448,6 +451,10 @@ class Batch:
     def set_tuning(self, stage_cap, force_block):
         _ck(self.lib.xnb_batch_set_tuning(self.h, int(stage_cap), int(force_block)))
 
+    def set_force_lanes(self, lanes):
+        """Threads per particle (1, 2 or 4) of the FP64 / mixed full-list force traversal."""
+        _ck(self.lib.xnb_batch_set_force_lanes(self.h, int(lanes)))
+
     def set_build_form(self, form):
         """BUILD_ROWS (lane per particle, bulk-copied rows) or BUILD_WARP (lane per candidate)."""
         _ck(self.lib.xnb_batch_set_build_form(self.h, int(form)))
@@ -489,6 +496,10 @@ class Graph:
 
     def launch(self):
         _ck(self.batch.lib.xnb_graph_launch(self.g, self.batch.stream))
+
+    def current(self):
+        """False once systems were added beyond the captured extent (capture again)."""
+        return bool(self.batch.lib.xnb_graph_is_current(self.g))
 
     def close(self):
         if self.g:

@@ -178,7 +178,13 @@ int xnb_step(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, voi
 /* Captures nsteps of the fused step (device-side trigger, no host sync) as a CUDA graph. */
 int xnb_step_graph_create(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, void* stream,
                           xnb_graph** out);
+/* Launches the captured steps; XNB_ERR_ARG when the batch's extent (the
+ * high-water marks of its particle and cell pools, the number of system slots)
+ * or launch configuration changed since capture: systems added beyond the
+ * captured extent would not be stepped, so the graph must be captured again. */
 int xnb_graph_launch(xnb_graph* g, void* stream);
+/* 1 when the graph still covers the batch as it is (xnb_graph_launch accepts it), else 0. */
+int xnb_graph_is_current(const xnb_graph* g);
 int xnb_graph_destroy(xnb_graph* g);
 /* Any device error bit set on any system -> XNB_ERR_DEVICE / XNB_ERR_CAPACITY (synchronises). */
 int xnb_check_errors(xnb_batch* b, void* stream);
@@ -195,8 +201,15 @@ typedef struct xnb_tuning {
   int32_t trials;             /* configurations timed */
   double atom_steps_per_s;    /* the chosen configuration's measured rate */
   int32_t build_form;         /* XNB_BUILD_ROWS or XNB_BUILD_WARP */
-  int32_t reserved;
+  int32_t force_lanes;        /* threads per particle of the FP64 / mixed full-list force traversal */
 } xnb_tuning;
+
+/* Threads per particle (1, 2 or 4) of the FP64 and mixed full-list force
+ * traversals: the particle's list is split in 8-entry blocks dealt round-robin
+ * to the threads and their partial sums combined in a fixed order, so results
+ * are reproducible and agree with one thread per particle to rounding.
+ * FP64_EXACT always runs one thread per particle. */
+int xnb_batch_set_force_lanes(xnb_batch* b, int32_t lanes);
 
 /* Neighbour-build kernels (both give the same lists, the reference's):
  * XNB_BUILD_ROWS: one warp per cell, one lane per particle (two for cells of
@@ -215,8 +228,8 @@ int xnb_batch_set_build_form(xnb_batch* b, int32_t form);
 /* Changes the launch configuration of a live batch (same limits as at creation). */
 int xnb_batch_set_tuning(xnb_batch* b, int32_t stage_cap, int32_t force_block);
 /* Online autotuner: coordinate search over the neighbour-build form
- * {ROWS, WARP}, stage_cap {384, 640, 1024}, force_block {128, 256} and the
- * Newton traversal, each configuration timed
+ * {ROWS, WARP}, stage_cap {384, 640, 1024}, force_block {128, 256}, force
+ * threads per particle {1, 2, 4} and the Newton traversal, each configuration timed
  * (CUDA events on `stream`) over trial_steps of xnb_step without host sync
  * after one untimed step. The trials are real MD steps: the batch advances
  * (1 + trial_steps) x trials steps. The batch is left on the fastest

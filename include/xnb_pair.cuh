@@ -34,6 +34,7 @@
  *     __device__ void buffer(Acc&, const ParticleContext&, int n, const PairData*) const;  compute buffer
  *     __device__ void entry(Acc&, const ParticleContext&, const RawEntry&) const;  raw entries
  *     __device__ void stop(Acc&, const ParticleContext&) const;
+ *     __device__ void combine(Acc&, const Acc&) const;   (lane groups: add a partial state)
  * and a ComputePairTraits<F> specialisation (derived from DefaultPairTraits)
  * choosing which of pair / buffer / entry the traversal calls:
  *   BufferLessCompatible  pair() per neighbour within the cutoff (default);
@@ -160,11 +161,14 @@ struct Marks {
   uint32_t w[4];
 };
 
+// With lanes > 1 the caller is lane `sub` of a group sharing the particle and
+// marks only the 8-entry blocks kw + 8 (sub + lanes k) of the window.
 __device__ __forceinline__ Marks prefilter_window(const uint32_t* __restrict__ L, uint32_t kw, uint32_t kend,
                                                   const float4* __restrict__ pf, uint32_t pbase, uint32_t self_e,
-                                                  float4 paf, float pfx, float pfy, float pfz, float pre_hi) {
+                                                  float4 paf, float pfx, float pfy, float pfz, float pre_hi,
+                                                  uint32_t sub = 0, uint32_t lanes = 1) {
   Marks m{{0u, 0u, 0u, 0u}};
-  for (uint32_t kb = kw; kb < kend; kb += 8) {
+  for (uint32_t kb = kw + 8u * sub; kb < kend; kb += 8u * lanes) {
     const uint4 ea = __ldg(reinterpret_cast<const uint4*>(L + kb));
     const uint4 eb = __ldg(reinterpret_cast<const uint4*>(L + kb + 4));
     const uint32_t ev[8] = {ea.x, ea.y, ea.z, ea.w, eb.x, eb.y, eb.z, eb.w};
@@ -323,6 +327,85 @@ __device__ __forceinline__ void traverse_particle(const Src& src, uint32_t i, co
     }
   }
   f.stop(acc, c);
+}
+
+// ---------------------------------------------------------------------------
+// The same walk with LANES threads per particle (2, 4 or 8 consecutive lanes
+// of a warp): lane `sub` of the group takes the 8-entry blocks sub, sub +
+// LANES, ... of every window, in list order, and the partial states are
+// combined in a fixed order (F::combine, a shuffle tree within the group), so
+// results are reproducible from run to run; they agree with the one-lane walk
+// to rounding. Every lane of the warp must call it (the shuffles span the
+// warp): `active` is false for lanes past the last particle. Raw-entry and
+// buffer-less functors; stop() runs on the group's first lane.
+template <int LANES, class F, class Src>
+__device__ __forceinline__ void traverse_particle_lanes(const Src& src, uint32_t i, bool active, const F& f) {
+  using T = ComputePairTraits<F>;
+  static_assert(LANES == 2 || LANES == 4 || LANES == 8, "2, 4 or 8 lanes per particle");
+  static_assert(T::RawEntries || T::BufferLessCompatible, "lane groups take raw entries or buffer-less pairs");
+  static_assert(sizeof(typename F::Acc) % 4 == 0, "the per-particle state is combined 32 bits at a time");
+  const uint32_t sub = threadIdx.x & (LANES - 1);
+  ParticleContext c;
+  typename F::Acc acc{};
+  bool ok = active && src.begin(i, T::Symmetric, T::GatherMirrors, c);
+  if (ok) ok = f.start(acc, c);
+  if (ok) {
+    const float pre_hi = f.prefilter_hi(c);
+    const uint32_t self_e = ((c.i - c.pbase) << 5) | kImageCenter;
+    const uint32_t n = c.n;
+    const uint32_t* __restrict__ L = c.list;
+    const double rc2 = T::RawEntries ? 0.0 : f.rcut2(c);
+    for (uint32_t kw = 0; kw < n; kw += 128) {
+      Marks mk = prefilter_window(L, kw, min(n, kw + 128u), src.pf, c.pbase, self_e, c.hi, c.period_f[0],
+                                  c.period_f[1], c.period_f[2], pre_hi, sub, LANES);
+      uint32_t b;
+      while (next_mark(mk, b)) {
+        const uint32_t e = __ldg(L + kw + b);
+        const uint32_t j = c.pbase + (e >> 5);
+        if constexpr (T::RawEntries) {
+          RawEntry r;
+          r.e = e;
+          r.j = j;
+          r.xb = __ldg(src.rx + j);
+          r.yb = __ldg(src.ry + j);
+          r.zb = __ldg(src.rz + j);
+          r.hb = __ldg(src.pf + j);
+          r.lb = T::GatherMirrors ? __ldg(src.pflo + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+          f.entry(acc, c, r);
+        } else {
+          const uint32_t code = e & 31u;
+          double xb = __ldg(src.rx + j), yb = __ldg(src.ry + j), zb = __ldg(src.rz + j);
+          if (code != kImageCenter) {
+            xb = image_coord(xb, c.period[0], static_cast<int>(code % 3u));
+            yb = image_coord(yb, c.period[1], static_cast<int>((code / 3u) % 3u));
+            zb = image_coord(zb, c.period[2], static_cast<int>(code / 9u));
+          }
+          PairData p;
+          p.dx = __dsub_rn(xb, c.x);
+          p.dy = __dsub_rn(yb, c.y);
+          p.dz = __dsub_rn(zb, c.z);
+          p.d2 = norm2_rn(p.dx, p.dy, p.dz);
+          if (p.d2 > 0.0 && p.d2 <= rc2) {
+            p.j = j;
+            p.code = code;
+            f.pair(acc, c, p);
+          }
+        }
+      }
+    }
+  }
+  // fixed-order tree over the group: lane sub takes lane sub + off's partial
+  constexpr int kWords = static_cast<int>(sizeof(typename F::Acc) / 4);
+#pragma unroll
+  for (int off = LANES / 2; off > 0; off >>= 1) {
+    typename F::Acc other;
+    uint32_t* ow = reinterpret_cast<uint32_t*>(&other);
+    const uint32_t* aw = reinterpret_cast<const uint32_t*>(&acc);
+#pragma unroll
+    for (int w = 0; w < kWords; ++w) ow[w] = __shfl_down_sync(0xffffffffu, aw[w], off, LANES);
+    if (ok && sub < static_cast<uint32_t>(off)) f.combine(acc, other);
+  }
+  if (ok && sub == 0) f.stop(acc, c);
 }
 
 // ---------------------------------------------------------------------------
