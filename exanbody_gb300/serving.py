@@ -15,7 +15,7 @@ Latency of a request = completion time - arrival time (host clock, seconds).
 The baseline serves the same requests one at a time through the plain FP64
 path (a fresh single-system batch per request, in arrival order).
 
-  python -m exanbody_gb300.serving [--requests 200] [--rate R] [--budget-gb 150]
+  python -m exanbody_gb300.serving [--requests 10000] [--rate R] [--budget-gb 150] [--baseline-requests 1000]
 """
 import argparse
 import collections
@@ -40,7 +40,16 @@ def footprint(w):
 
 
 class Server:
-    def __init__(self, budget_bytes, max_systems=4096, precision=xnb.PREC_MIXED, chunk=50, stream=None):
+    """One resident batch serving requests by continuous batching.
+
+    Each chunk of steps runs as a CUDA graph (xnb_step_graph_create), cached per
+    chunk length and captured again only when an admission grew the batch's
+    extent (xnb_graph_is_current). While the GPU runs a chunk, the host builds
+    the initial states of the requests that arrive next, so that their upload
+    and initialisation at the next chunk boundary do not wait for it."""
+
+    def __init__(self, budget_bytes, max_systems=4096, precision=xnb.PREC_MIXED, chunk=50, stream=None,
+                 use_graphs=True, lookahead_s=2.0, lookahead_max=64):
         import torch
 
         self.stream = stream or torch.cuda.Stream()
@@ -51,20 +60,66 @@ class Server:
         self.batch.stream = ctypes.c_void_p(self.stream.cuda_stream)
         self.budget = budget_bytes
         self.used = 0
+        self.peak_used = 0
         self.max_systems = max_systems
         self.precision = precision
         self.chunk = chunk
+        self.use_graphs = use_graphs
+        self.lookahead_s = lookahead_s
+        self.lookahead_max = lookahead_max
+        self.graphs = {}  # chunk length -> captured graph
+        self.captures = 0
+        self.chunks = 0
 
     def close(self):
+        for g in self.graphs.values():
+            g.close()
+        self.graphs = {}
         self.batch.close()
 
+    def _launch_chunk(self, nsteps):
+        if not self.use_graphs:
+            self.batch.step(nsteps, self.precision, 0)
+            return
+        g = self.graphs.get(nsteps)
+        if g is None or not g.current():
+            if g is not None:
+                g.close()
+            g = self.batch.graph(nsteps, self.precision, 0)
+            self.graphs[nsteps] = g
+            self.captures += 1
+        g.launch()
+
     def serve(self, requests, prebuilt=None, time_limit=None, keep_results=False):
-        """Serve requests in real time; returns per-request records."""
-        pending = collections.deque(sorted(range(len(requests)), key=lambda k: requests[k]["arrival"]))
-        active = {}  # sys id -> [req index, remaining steps, bytes]
+        """Serve requests in real time; returns (records, wall seconds, atom-steps).
+        records[k]: arrival, admit, done, latency (done - arrival), wait (admit - arrival)."""
+        order = sorted(range(len(requests)), key=lambda k: requests[k]["arrival"])
+        pending = collections.deque(order)
+        pending_set = set(order)
+        ready = {}  # request -> initial state built on the host ahead of its admission
+        upcoming = collections.deque(order)  # requests whose state is not built yet
+
+        def system_of(k):
+            if prebuilt is not None:
+                return prebuilt[k]
+            w = ready.pop(k, None)
+            return w if w is not None else request_system(requests[k])
+
+        def prepare(now):
+            # host work overlapped with the running chunk: the states of the next arrivals
+            if prebuilt is not None:
+                return
+            while upcoming and len(ready) < self.lookahead_max:
+                k = upcoming[0]
+                if requests[k]["arrival"] > now + self.lookahead_s:
+                    break
+                upcoming.popleft()
+                if k in pending_set and k not in ready:
+                    ready[k] = request_system(requests[k])
+
+        active = {}  # sys id -> [req index, remaining steps, bytes, atoms]
         records = {}
         t0 = time.perf_counter()
-        steps_done = 0
         atom_steps = 0
         while pending or active:
             now = time.perf_counter() - t0
@@ -73,32 +128,43 @@ class Server:
             admitted = []
             while pending and requests[pending[0]]["arrival"] <= now and len(active) < self.max_systems:
                 k = pending[0]
-                w = prebuilt[k] if prebuilt else request_system(requests[k])
+                w = system_of(k)
                 fb = footprint(w)
                 if self.used + fb > self.budget:
+                    if prebuilt is None:
+                        ready[k] = w
                     break
                 pending.popleft()
+                pending_set.discard(k)
                 try:
                     s = self.batch.add_system(xnb.lj_params(w["geom"]), w["r"], w["v"], w["id"], list_factor=1.25)
                 except xnb.XnbError:
                     pending.appendleft(k)  # pool fragmentation: retry after a retirement
+                    pending_set.add(k)
+                    if prebuilt is None:
+                        ready[k] = w
                     break
                 self.used += fb
+                self.peak_used = max(self.peak_used, self.used)
                 active[s] = [k, requests[k]["steps"], fb, w["n_atoms"]]
-                records[k] = {"admit": time.perf_counter() - t0}
+                t_admit = time.perf_counter() - t0
+                records[k] = {"arrival": requests[k]["arrival"], "admit": t_admit,
+                              "wait": t_admit - requests[k]["arrival"]}
                 admitted.append(s)
             for s in admitted:
                 self.batch.init_particles(s, self.precision)
             if not active:
+                prepare(time.perf_counter() - t0)
                 if pending:
                     wait = requests[pending[0]]["arrival"] - (time.perf_counter() - t0)
                     if wait > 0:
                         time.sleep(min(wait, 0.05))
                 continue
             nsteps = min(self.chunk, min(v[1] for v in active.values()))
-            self.batch.step(nsteps, self.precision, 0)
+            self._launch_chunk(nsteps)  # asynchronous on self.stream
+            self.chunks += 1
+            prepare(time.perf_counter() - t0)
             self.stream.synchronize()
-            steps_done += nsteps
             atom_steps += nsteps * sum(v[3] for v in active.values())
             finished = [s for s, v in active.items() if v[1] - nsteps <= 0]
             for s in active:
@@ -150,26 +216,37 @@ def serve_sequential(requests, prebuilt=None, precision=xnb.PREC_FP64, time_limi
 
 
 def summarize(records, wall, atom_steps, device=None):
-    """Completion-latency percentiles and throughput; under torchrun the latencies
-    of all ranks are gathered and the wall time is the slowest rank's."""
+    """Completion-latency percentiles and throughput (and the admission waits
+    where recorded); under torchrun the values of all ranks are gathered and the
+    wall time is the slowest rank's."""
     lat = np.array([r["latency"] for r in records.values() if "latency" in r])
     lat = replicas.gather_values(lat, device=device)
     wall = replicas.max_over_ranks(wall, device=device)
     atom_steps = replicas.gather_values([atom_steps], device=device).sum()
-    return {"completed": int(len(lat)), "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
-            "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
-            "mean_s": float(lat.mean()) if len(lat) else None, "wall_s": wall,
-            "atom_steps_per_s": float(atom_steps) / wall}
+    out = {"completed": int(len(lat)), "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+           "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+           "mean_s": float(lat.mean()) if len(lat) else None, "max_s": float(lat.max()) if len(lat) else None,
+           "wall_s": wall, "atom_steps_per_s": float(atom_steps) / wall}
+    waits = np.array([r["wait"] for r in records.values() if "wait" in r])
+    if len(waits):
+        waits = replicas.gather_values(waits, device=device)
+        out["admission_wait_s"] = {"p50": float(np.percentile(waits, 50)), "p90": float(np.percentile(waits, 90)),
+                                   "p99": float(np.percentile(waits, 99)), "max": float(waits.max()),
+                                   "mean": float(waits.mean()), "zero_fraction": float(np.mean(waits < 1e-3))}
+    return out
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--requests", type=int, default=10000)
     ap.add_argument("--rate", type=float, default=0.0, help="arrivals per second (0: 0.8 x measured capacity)")
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--chunk", type=int, default=50)
     ap.add_argument("--seed", type=int, default=4242)
-    ap.add_argument("--no-baseline", action="store_true")
+    ap.add_argument("--baseline-requests", type=int, default=1000,
+                    help="the sequential FP64 baseline serves this prefix of the stream (0: none)")
+    ap.add_argument("--no-graphs", action="store_true", help="eager xnb_step chunks instead of captured graphs")
+    ap.add_argument("--out", default="", help="also write the JSON result to this file")
     args = ap.parse_args()
     import torch
 
@@ -184,15 +261,15 @@ def main():
         dev = torch.device("cuda", local)
     torch.cuda.init()
     reqs = replicas.shard(workloads.serving_stream(args.requests, seed=args.seed, rate=1.0), rank, world)
-    prebuilt = [request_system(r) for r in reqs]
-    work = sum(w["n_atoms"] * r["steps"] for w, r in zip(prebuilt, reqs))
+    # FCC n^3 holds 4 n^3 atoms: the work is known without building the systems
+    work = sum(4 * r["n"] ** 3 * r["steps"] for r in reqs)
     rate = args.rate
     capacity = None
     if rate <= 0:
         # capacity: a batch of the first requests, all admitted at once
         probe = [dict(r, arrival=0.0) for r in reqs[: min(64, len(reqs))]]
         srv = Server(args.budget_gb * 1e9, precision=xnb.PREC_MIXED, chunk=args.chunk)
-        rec, wall, ast = srv.serve(probe, prebuilt[: len(probe)])
+        rec, wall, ast = srv.serve(probe, [request_system(r) for r in probe])
         srv.close()
         mean_work = work / len(reqs)
         capacity = ast / wall / mean_work  # requests per second of one GPU
@@ -202,19 +279,36 @@ def main():
     # rescale the unit-rate arrival times of the seeded stream to the chosen rate
     for r in reqs:
         r["arrival"] = r["arrival"] / rate
-    srv = Server(args.budget_gb * 1e9, precision=xnb.PREC_MIXED, chunk=args.chunk)
-    rec, wall, ast = srv.serve(reqs, prebuilt)
+    srv = Server(args.budget_gb * 1e9, precision=xnb.PREC_MIXED, chunk=args.chunk, use_graphs=not args.no_graphs)
+    rec_b, wall, ast = srv.serve(reqs)
+    batched = summarize(rec_b, wall, ast, dev)
+    batched.update(peak_admitted_gb=srv.peak_used / 1e9, chunks=srv.chunks, graph_captures=srv.captures,
+                   chunk_runs="eager xnb_step" if args.no_graphs else "captured CUDA graphs")
     srv.close()
     out = {"workload": "serving_%d_requests_fcc_n5-40_steps200-2000" % args.requests,
            "arrival_rate_per_s": rate, "capacity_req_per_s": capacity, "budget_gb": args.budget_gb,
            "chunk_steps": args.chunk, "total_atom_steps": int(replicas.gather_values([work], device=dev).sum()),
-           "gpus": world, "batched_mixed": summarize(rec, wall, ast, dev)}
-    if not args.no_baseline:
-        # the plain FP64 path at its faster traversal on one system at a time (Newton half lists)
-        rec, wall, ast = serve_sequential(reqs, prebuilt, precision=xnb.PREC_FP64 | xnb.PREC_NEWTON)
-        out["sequential_fp64"] = dict(summarize(rec, wall, ast, dev), traversal="newton")
+           "gpus": world, "batched_mixed": batched}
+    nb = min(args.baseline_requests, len(reqs))
+    if nb > 0:
+        # the plain FP64 path at its faster traversal (Newton half lists) on one
+        # system at a time, over the first nb requests of the same stream
+        first = sorted(range(len(reqs)), key=lambda k: reqs[k]["arrival"])[:nb]
+        sub = [reqs[k] for k in first]
+        rec, wall, ast = serve_sequential(sub, precision=xnb.PREC_FP64 | xnb.PREC_NEWTON)
+        out["sequential_fp64"] = dict(summarize(rec, wall, ast, dev), traversal="newton",
+                                      requests="the first %d of the stream, same arrival times" % nb)
+        # the batched loop's latencies over the same requests, for a like-for-like comparison
+        pre = [rec_b[k]["latency"] for k in first if "latency" in rec_b.get(k, {})]
+        if pre:
+            out["batched_mixed_same_prefix"] = {"completed": len(pre), "p50_s": float(np.percentile(pre, 50)),
+                                                "p99_s": float(np.percentile(pre, 99)), "mean_s": float(np.mean(pre))}
     if rank == 0:
-        print(json.dumps(out))
+        line = json.dumps(out)
+        print(line)
+        if args.out:
+            with open(args.out, "w") as f:
+                f.write(line + "\n")
 
 
 if __name__ == "__main__":
