@@ -31,6 +31,13 @@ def make_systems(specs, rcut=2.5, skin=0.3):
     return [workloads.lj_fcc_system(sp["n"], sp["rho"], sp["T"], sp["seed"], rcut, skin) for sp in specs]
 
 
+def geometry_for(w, rcut, skin):
+    """The system's periodic box with the cell grid of neighbour distance rcut + skin
+    (the same box and positions; the cell size follows the skin)."""
+    g = w["geom"]
+    return workloads.geometry(tuple(e - o for e, o in zip(g["extent"], g["origin"])), rcut, skin)
+
+
 def build_batch(systems, stage_cap=640, force_block=128, skin=0.3, rcut=2.5, dt=0.005, stream=None,
                 precision=xnb.PREC_MIXED, list_per_atom=None, build_form="warp", force_lanes=1):
     n_atoms = sum(w["n_atoms"] for w in systems)
@@ -45,8 +52,8 @@ def build_batch(systems, stage_cap=640, force_block=128, skin=0.3, rcut=2.5, dt=
         b.stream = ctypes.c_void_p(stream)
     b.set_build_form(FORMS[build_form])
     b.set_force_lanes(force_lanes)
-    ids = [b.add_system(xnb.lj_params(w["geom"], rcut=rcut, rcut_inc=skin, dt=dt), w["r"], w["v"], w["id"],
-                        list_factor=1.25) for w in systems]
+    ids = [b.add_system(xnb.lj_params(geometry_for(w, rcut, skin), rcut=rcut, rcut_inc=skin, dt=dt), w["r"], w["v"],
+                        w["id"], list_factor=1.25) for w in systems]
     b.init_particles(-1, precision)
     return b, ids, n_atoms
 
