@@ -115,8 +115,12 @@ struct xnb_batch {
     e.n_part = static_cast<uint32_t>(parts.high_water());
     e.n_cells = static_cast<uint32_t>(cells.high_water());
     int hw = 0;
+    e.far_coords = 0;
     for (size_t s = 0; s < sys.size(); ++s)
-      if (sys[s].active) hw = static_cast<int>(s) + 1;
+      if (sys[s].active) {
+        hw = static_cast<int>(s) + 1;
+        if (sys[s].d.far_coords) e.far_coords = 1;
+      }
     e.nsys = hw;
     e.sm_count = sm_count;
     e.force_block = force_block;
@@ -132,7 +136,7 @@ struct xnb_graph {
   // what the captured launches depend on besides device memory: the batch's
   // work extent and launch configuration at capture
   uint32_t n_part = 0, n_cells = 0;
-  int nsys = 0, lbuf = 0, stage_cap = 0, force_block = 0, force_lanes = 0, build_form = 0;
+  int nsys = 0, lbuf = 0, stage_cap = 0, force_block = 0, force_lanes = 0, build_form = 0, far_coords = 0;
 };
 
 namespace {
@@ -1068,6 +1072,7 @@ int xnb_step_graph_create(xnb_batch* b, int32_t nsteps, int32_t precision, int32
   G->n_part = ex.n_part;
   G->n_cells = ex.n_cells;
   G->nsys = ex.nsys;
+  G->far_coords = ex.far_coords;
   G->lbuf = list_buf(b);
   G->stage_cap = b->stage_cap;
   G->force_block = b->force_block;
@@ -1087,7 +1092,8 @@ int xnb_graph_is_current(const xnb_graph* g) {
   if (!g || !g->batch) return 0;
   const xnb_batch* b = g->batch;
   const Extent ex = b->extent();
-  return (ex.n_part == g->n_part && ex.n_cells == g->n_cells && ex.nsys == g->nsys && list_buf(b) == g->lbuf &&
+  return (ex.n_part == g->n_part && ex.n_cells == g->n_cells && ex.nsys == g->nsys && ex.far_coords == g->far_coords &&
+          list_buf(b) == g->lbuf &&
           b->stage_cap == g->stage_cap && b->force_block == g->force_block && b->force_lanes == g->force_lanes &&
           b->build_form == g->build_form)
              ? 1

@@ -18,6 +18,7 @@ struct Extent {
   int sm_count;
   int force_block;   // threads per block of the force traversal (multiple of 32, <= 256)
   int force_lanes;   // threads per particle of the FP64 / mixed full-list traversal (1, 2 or 4)
+  int far_coords;    // some resident system lies far from the coordinate origin (SysDesc::far_coords)
 };
 
 // Fused first half of velocity Verlet plus the displacement trigger:

@@ -375,7 +375,10 @@ __global__ void __maxnreg__(72) k_force_lanes(uint32_t n_part, BatchSource src, 
 // reduction in L2. Each pair inside rc is evaluated once. The order in which
 // reactions arrive varies from run to run, so results agree to rounding, not
 // bit for bit; FP64_EXACT always uses the full-list kernel above.
-template <int P, bool PE>
+// FAR: instantiated only when a system of the batch lies far from the
+// coordinate origin (Extent::far_coords), so the common kernel carries no
+// partner-side evaluation.
+template <int P, bool PE, bool FAR = false>
 __global__ void __launch_bounds__(256)
     k_force_half(uint32_t n_part, const SysDesc* __restrict__ sys, const SysState* __restrict__ st, DevArrays a,
                  int sys_only) {
@@ -427,7 +430,7 @@ __global__ void __launch_bounds__(256)
         yb = image_coord(yb, py, static_cast<int>((code / 3u) % 3u));
         zb = image_coord(zb, pz, static_cast<int>(code / 9u));
       }
-      if (P == kFp64 && code != static_cast<uint32_t>(kImageCenter) && S.far_coords) {
+      if (FAR && P == kFp64 && code != static_cast<uint32_t>(kImageCenter) && S.far_coords) {
         // Far from the coordinate origin (coordinates beyond 4 periods) the
         // partner's reaction through a periodic image is evaluated as the
         // partner's own full-list traversal would: b sees a through the
@@ -660,8 +663,13 @@ int launch_force(const Extent& ex, const SysDesc* sys, SysState* st, const DevAr
     const int g = grid_capped(ex.n_part, threads, ex.sm_count, 8);
     k_zero_force<<<g, threads, 0, stream>>>(ex.n_part, st, a, sys_only, with_pe);
     if (precision == kFp64) {
-      if (with_pe) k_force_half<kFp64, true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);
-      else k_force_half<kFp64, false><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);
+      if (ex.far_coords) {
+        if (with_pe) k_force_half<kFp64, true, true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);
+        else k_force_half<kFp64, false, true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);
+      } else {
+        if (with_pe) k_force_half<kFp64, true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);
+        else k_force_half<kFp64, false><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);
+      }
     } else {
       if (with_pe) k_force_half<kMixed, true><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);
       else k_force_half<kMixed, false><<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only);
