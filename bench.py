@@ -104,6 +104,8 @@ def parse():
                     help="neighbour-build kernel (empty: library default)")
     ap.add_argument("--force-lanes", type=int, default=0, choices=[0, 1, 2, 4],
                     help="threads per particle of the FP64 / mixed force traversal (0: library default)")
+    ap.add_argument("--force-form", default="", choices=["", "thread", "staged"],
+                    help="mixed full-list force traversal form (empty: library default)")
     ap.add_argument("--workload", default="lj", choices=["lj", "snap_ni", "snap_mo"],
                     help="lj: the 4M-atom LJ headline; snap_*: the reference's SNAP benchmark decks")
     return ap.parse_args()
@@ -278,6 +280,8 @@ def run_ours(args):
             b.set_build_form({"rows": xnb.BUILD_ROWS, "warp": xnb.BUILD_WARP}[args.build_form])
         if args.force_lanes:
             b.set_force_lanes(args.force_lanes)
+        if args.force_form:
+            b.set_force_form({"thread": xnb.FORCE_THREAD, "staged": xnb.FORCE_STAGED}[args.force_form])
         return b
 
     def timed(fn, reps=1):

@@ -98,6 +98,8 @@ struct xnb_batch {
   int stage_cap = 640;
   int force_block = 128;
   int force_lanes = 1;          // threads per particle of the FP64 / mixed force traversal
+  int force_form = kForceThread;  // mixed full-list traversal form (xnb_batch_set_force_form)
+  std::vector<uint4> segs;      // cell segments of the staged traversal (host copy of a.seg)
   int build_form = kBuildWarp;  // neighbour-build kernel (xnb_batch_set_build_form)
   DevArrays a{};
   SysDesc* d_sys = nullptr;
@@ -125,6 +127,8 @@ struct xnb_batch {
     e.sm_count = sm_count;
     e.force_block = force_block;
     e.force_lanes = force_lanes;
+    e.force_form = force_form;
+    e.n_seg = a.seg ? static_cast<uint32_t>(segs.size()) : 0u;
     return e;
   }
 };
@@ -137,6 +141,8 @@ struct xnb_graph {
   // work extent and launch configuration at capture
   uint32_t n_part = 0, n_cells = 0;
   int nsys = 0, lbuf = 0, stage_cap = 0, force_block = 0, force_lanes = 0, build_form = 0, far_coords = 0;
+  int force_form = 0;
+  uint32_t n_seg = 0;
 };
 
 namespace {
@@ -335,6 +341,29 @@ int pull_states(xnb_batch* b, cudaStream_t st) {
   const Extent ex = b->extent();
   if (ex.nsys == 0) return XNB_OK;
   XCK(cudaMemcpyAsync(b->h_st, b->d_st, sizeof(SysState) * ex.nsys, cudaMemcpyDeviceToHost, st));
+  XCK(cudaStreamSynchronize(st));
+  return XNB_OK;
+}
+
+// Cell segments of the staged force traversal: every row (j, k) of every
+// resident system cut into runs of kStagedSegCells x-adjacent cells; uploaded
+// whenever the set of systems changes (and the staged form is allocated).
+int upload_segments(xnb_batch* b, cudaStream_t st) {
+  b->segs.clear();
+  for (size_t q = 0; q < b->sys.size(); ++q) {
+    const SysHost& h = b->sys[q];
+    if (!h.active) continue;
+    const SysDesc& d = h.d;
+    for (int k = 0; k < d.dims[2]; ++k)
+      for (int j = 0; j < d.dims[1]; ++j)
+        for (int i = 0; i < d.dims[0]; i += kStagedSegCells) {
+          const uint32_t first = d.cell_base + static_cast<uint32_t>((k * d.dims[1] + j) * d.dims[0] + i);
+          const uint32_t n = static_cast<uint32_t>(std::min(kStagedSegCells, d.dims[0] - i));
+          b->segs.push_back(make_uint4(first, n, static_cast<uint32_t>(q), 0u));
+        }
+  }
+  if (!b->a.seg || b->segs.empty()) return XNB_OK;
+  XCK(cudaMemcpyAsync(b->a.seg, b->segs.data(), b->segs.size() * sizeof(uint4), cudaMemcpyHostToDevice, st));
   XCK(cudaStreamSynchronize(st));
   return XNB_OK;
 }
@@ -597,6 +626,10 @@ int xnb_system_add(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double
   // the caller's arrays and the host staging are pageable: finish the copies before returning
   XCK(cudaStreamSynchronize(st));
   *sys_out = slot;
+  {
+    const int urc = upload_segments(b, st);
+    if (urc) return urc;
+  }
   return XNB_OK;
 }
 
@@ -735,6 +768,10 @@ int xnb_system_remove(xnb_batch* b, int32_t s, void* stream) {
   b->cells.release(h.d.cell_base);
   if (h.list_off >= 0) b->lists.release(static_cast<uint64_t>(h.list_off));
   h = SysHost{};
+  {
+    const int urc = upload_segments(b, st);
+    if (urc) return urc;
+  }
   return XNB_OK;
 }
 
@@ -1073,6 +1110,8 @@ int xnb_step_graph_create(xnb_batch* b, int32_t nsteps, int32_t precision, int32
   G->n_cells = ex.n_cells;
   G->nsys = ex.nsys;
   G->far_coords = ex.far_coords;
+  G->force_form = ex.force_form;
+  G->n_seg = ex.n_seg;
   G->lbuf = list_buf(b);
   G->stage_cap = b->stage_cap;
   G->force_block = b->force_block;
@@ -1093,6 +1132,7 @@ int xnb_graph_is_current(const xnb_graph* g) {
   const xnb_batch* b = g->batch;
   const Extent ex = b->extent();
   return (ex.n_part == g->n_part && ex.n_cells == g->n_cells && ex.nsys == g->nsys && ex.far_coords == g->far_coords &&
+          ex.force_form == g->force_form && ex.n_seg == g->n_seg &&
           list_buf(b) == g->lbuf &&
           b->stage_cap == g->stage_cap && b->force_block == g->force_block && b->force_lanes == g->force_lanes &&
           b->build_form == g->build_form)
@@ -1149,6 +1189,30 @@ int xnb_batch_set_force_lanes(xnb_batch* b, int32_t lanes) {
   return XNB_OK;
 }
 
+int xnb_batch_set_force_form(xnb_batch* b, int32_t form) {
+  if (!b) return fail(XNB_ERR_ARG, "null batch");
+  if (form != XNB_FORCE_THREAD && form != XNB_FORCE_STAGED) return fail(XNB_ERR_ARG, "unknown force traversal form");
+  if (form == XNB_FORCE_STAGED && b->force_form != kForceStaged) {
+    XCK(cudaSetDevice(b->device));
+    if (!b->a.nbr16) {
+      int rc = dalloc(b, &b->a.nbr16, b->lists.cap);
+      if (rc) return rc;
+      rc = dalloc(b, &b->a.seg, static_cast<uint64_t>(b->cells.cap) + 1);
+      if (rc) return rc;
+      rc = upload_segments(b, nullptr);
+      if (rc) return rc;
+    }
+    // the current lists get their compact entries now; later builds write them as they go
+    XCK(cudaDeviceSynchronize());
+    Extent ex = b->extent();
+    ex.force_form = kForceStaged;
+    b->launches += launch_compact_lists(ex, b->d_sys, b->d_st, b->a, nullptr, true);
+    XCK(cudaDeviceSynchronize());
+  }
+  b->force_form = form == XNB_FORCE_STAGED ? kForceStaged : kForceThread;
+  return check_launch();
+}
+
 int xnb_batch_set_build_form(xnb_batch* b, int32_t form) {
   if (!b) return fail(XNB_ERR_ARG, "null batch");
   if (form != XNB_BUILD_ROWS && form != XNB_BUILD_WARP) return fail(XNB_ERR_ARG, "unknown neighbour-build form");
@@ -1171,8 +1235,10 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
   XCK(cudaEventCreate(&e0));
   XCK(cudaEventCreate(&e1));
   int trials = 0;
-  auto rate_of = [&](int sc, int fb, int nw, int bf, int fl, double* rate) -> int {
+  auto rate_of = [&](int sc, int fb, int nw, int bf, int fl, int ff, double* rate) -> int {
     int rc = xnb_batch_set_tuning(b, sc, fb);
+    if (rc) return rc;
+    rc = xnb_batch_set_force_form(b, ff);
     if (rc) return rc;
     rc = xnb_batch_set_build_form(b, bf);
     if (rc) return rc;
@@ -1193,27 +1259,30 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
     return xnb_check_errors(b, stream);
   };
   const int caps[3] = {384, 640, 1024}, blocks[2] = {128, 256}, forms[2] = {XNB_BUILD_ROWS, XNB_BUILD_WARP},
-            lanes[3] = {1, 2, 4};
+            lanes[3] = {1, 2, 4}, fforms[2] = {XNB_FORCE_THREAD, XNB_FORCE_STAGED};
   int best_sc = b->stage_cap, best_fb = b->force_block, best_nw = 0, best_fl = b->force_lanes;
   int best_bf = b->build_form == kBuildRows ? XNB_BUILD_ROWS : XNB_BUILD_WARP;
+  int best_ff = b->force_form == kForceStaged ? XNB_FORCE_STAGED : XNB_FORCE_THREAD;
   double best = 0.0;
-  int rc = rate_of(best_sc, best_fb, best_nw, best_bf, best_fl, &best);
+  int rc = rate_of(best_sc, best_fb, best_nw, best_bf, best_fl, best_ff, &best);
   // coordinate search: one parameter at a time, the others at their best so far
   // (neighbour-build form, the stage cap of the forms that stage whole
   // neighbourhoods, the force block size, threads per particle of the force
   // traversal and the Newton traversal)
-  const int nvals[5] = {2, 3, 2, 3, 2};
-  for (int pass = 0; pass < 5 && rc == 0; ++pass) {
+  const int nvals[6] = {2, 3, 2, 3, 2, 2};
+  for (int pass = 0; pass < 6 && rc == 0; ++pass) {
     for (int v = 0; v < nvals[pass] && rc == 0; ++v) {
-      int sc = best_sc, fb = best_fb, nw = best_nw, bf = best_bf, fl = best_fl;
+      int sc = best_sc, fb = best_fb, nw = best_nw, bf = best_bf, fl = best_fl, ff = best_ff;
       if (pass == 0) bf = forms[v];
       else if (pass == 1) sc = caps[v];
       else if (pass == 2) fb = blocks[v];
       else if (pass == 3) fl = lanes[v];
+      else if (pass == 4) ff = fforms[v];
       else nw = v;
-      if (sc == best_sc && fb == best_fb && nw == best_nw && bf == best_bf && fl == best_fl) continue;
+      if (sc == best_sc && fb == best_fb && nw == best_nw && bf == best_bf && fl == best_fl && ff == best_ff)
+        continue;
       double r = 0.0;
-      rc = rate_of(sc, fb, nw, bf, fl, &r);
+      rc = rate_of(sc, fb, nw, bf, fl, ff, &r);
       if (rc == 0 && r > best) {
         best = r;
         best_sc = sc;
@@ -1221,6 +1290,7 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
         best_nw = nw;
         best_bf = bf;
         best_fl = fl;
+        best_ff = ff;
       }
     }
   }
@@ -1233,6 +1303,9 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
   if (rc) return rc;
   rc = xnb_batch_set_force_lanes(b, best_fl);
   if (rc) return rc;
+  rc = xnb_batch_set_force_form(b, best_ff);
+  if (rc) return rc;
+  out->force_form = best_ff;
   out->stage_cap = best_sc;
   out->force_block = best_fb;
   out->build_form = best_bf;

@@ -880,6 +880,7 @@ __global__ void k_nbr_reset(int nsys, SysState* st, const unsigned int* any, uns
   st[s].list_used = 0;
   st[s].max_nbr = 0;
   st[s].lists_fresh = 1;  // the build that follows reads the current positions
+  st[s].compact_bad = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1049,7 +1050,9 @@ int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const D
   if (form == kBuildRows) launch_neighbors_rows(ex, sys, st, a, stream);
   else k_neighbors_warp<<<grid_w, 128, smem_w, stream>>>(ex.n_cells, sys, st, a, cap, lbuf_w);
   k_neighbors<<<warp_grid(ex.n_cells, 1, ex.sm_count), 128, smem, stream>>>(ex.n_cells, sys, st, a, cap, lbuf);
-  return 3;
+  // compact entries for the staged force traversal
+  const int nc = ex.force_form == kForceStaged ? launch_compact_lists(ex, sys, st, a, stream) : 0;
+  return 3 + nc;
 }
 
 }  // namespace xnb

@@ -93,6 +93,7 @@ struct SysState {
   uint32_t rebuild_armed;        // 1 once backup_r has run (the trigger needs a backup)
   uint32_t max_nbr;              // largest per-particle list count of the last build
   uint32_t lists_fresh;          // 1 from a neighbour build until positions next change
+  uint32_t compact_bad;          // the last build's lists could not be compacted (staged force traversal)
   unsigned long long rebuilds;
 };
 
@@ -129,6 +130,8 @@ struct DevArrays {
   uint32_t* nbr_half;              // per particle: entries before it in the reference order
                                    // ((cell_b, p_b) < (cell_a, p_a)), the Newton half list
   uint32_t* nbr;                   // all segments
+  uint16_t* nbr16;                 // compact entries (g << 11) | p_b beside nbr (staged force traversal; or null)
+  uint4* seg;                      // cell segments of the staged force traversal: first cell, cells, system
   uint32_t* nbr_wide;              // cells whose candidates or slot exceed the warp-per-cell build's buffers
   unsigned int* nbr_wide_n;        // number of them (reset by each build)
   // scan scratch

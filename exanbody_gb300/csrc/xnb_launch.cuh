@@ -19,7 +19,15 @@ struct Extent {
   int force_block;   // threads per block of the force traversal (multiple of 32, <= 256)
   int force_lanes;   // threads per particle of the FP64 / mixed full-list traversal (1, 2 or 4)
   int far_coords;    // some resident system lies far from the coordinate origin (SysDesc::far_coords)
+  int force_form;    // kForceThread or kForceStaged (mixed full-list traversal)
+  uint32_t n_seg;    // cell segments of the staged traversal (DevArrays::seg)
 };
+
+// Mixed-precision force traversal forms: one thread per particle over global
+// memory, or cell segments staged in shared memory (xnb_force_staged.cu).
+constexpr int kForceThread = 0;
+constexpr int kForceStaged = 1;
+constexpr int kStagedSegCells = 8;  // x-adjacent cells of one row per staged segment
 
 // Fused first half of velocity Verlet plus the displacement trigger:
 // push_f_v_r(dt_scale 1) ; push_f_v(dt_scale 0.5) ; particle_displ_over.
@@ -33,6 +41,15 @@ int launch_first_half(const Extent& ex, const SysDesc* sys, SysState* st, const 
 // reactions with FP64 reductions (three kernels: zero, traverse, finish).
 int launch_force(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int precision,
                  bool with_pe, bool second_half, int sys_only, cudaStream_t stream, bool newton = false);
+
+// Compact list entries of the flagged systems after a build, and the staged
+// mixed force traversal (+ kick) over the cell segments (xnb_force_staged.cu).
+// all = true: every resident system's current lists (when the staged form is switched on)
+int launch_compact_lists(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream,
+                         bool all = false);
+int launch_force_staged(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, bool with_pe,
+                        bool second_half, int sys_only, cudaStream_t stream);
+size_t staged_smem_bytes();
 
 // Marks systems for rebuild: all of them (init), or those with moved > 0.
 int launch_mark_rebuild(const Extent& ex, SysState* st, int mode, int sys_only, unsigned int* any,

@@ -31,7 +31,7 @@ struct BatchSource {
   const uint32_t* __restrict__ nbr_half;
   int sys_only;
 
-  __host__ BatchSource(const SysDesc* s_, const SysState* st_, const DevArrays& a, int sys_only_)
+  __host__ __device__ BatchSource(const SysDesc* s_, const SysState* st_, const DevArrays& a, int sys_only_)
       : sys(s_), st(st_), rx(a.rx), ry(a.ry), rz(a.rz), pf(a.pf), pflo(a.pflo), pcell(a.pcell),
         cell_sys(a.cell_sys), nbr(a.nbr), nbr_start(a.nbr_start), nbr_cnt(a.nbr_cnt), nbr_half(a.nbr_half),
         sys_only(sys_only_) {}

@@ -20,6 +20,8 @@ PRECISIONS = {"fp64_exact": PREC_FP64_EXACT, "fp64": PREC_FP64, "mixed": PREC_MI
 
 BUILD_ROWS = 0
 BUILD_WARP = 1
+FORCE_THREAD = 0
+FORCE_STAGED = 1
 
 STEP_HOST_SYNC = 1
 STEP_ENERGY = 2
@@ -44,7 +46,7 @@ EXPORTED = [
     "xnb_verify_chunk_neighbors", "xnb_simulation_stats", "xnb_sample_particles", "xnb_system_set_types",
     "xnb_gravitational_force", "xnb_batch_set_tuning", "xnb_autotune", "xnb_snap_create", "xnb_snap_destroy",
     "xnb_snap_force", "xnb_system_pairs_range", "xnb_system_pair_view", "xnb_batch_set_build_form",
-    "xnb_graph_is_current", "xnb_batch_set_force_lanes",
+    "xnb_graph_is_current", "xnb_batch_set_force_lanes", "xnb_batch_set_force_form",
 ]
 
 FORCE_ENERGY = 1
@@ -93,6 +95,8 @@ class Tuning(C.Structure):
         ("atom_steps_per_s", C.c_double),
         ("build_form", C.c_int32),
         ("force_lanes", C.c_int32),
+        ("force_form", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -180,6 +184,7 @@ def load(build_if_missing=True):
     lib.xnb_batch_set_build_form.argtypes = [vp, i32]
     lib.xnb_graph_is_current.argtypes = [vp]
     lib.xnb_batch_set_force_lanes.argtypes = [vp, i32]
+    lib.xnb_batch_set_force_form.argtypes = [vp, i32]
     lib.xnb_system_energy.argtypes = [vp, i32, P(d), P(d), vp]
     lib.xnb_init_particles.argtypes = [vp, i32, i32, vp]
     lib.xnb_push_f_v_r.argtypes = [vp, i32, d, vp]
@@ -454,6 +459,11 @@ class Batch:
     def set_force_lanes(self, lanes):
         """Threads per particle (1, 2 or 4) of the FP64 / mixed full-list force traversal."""
         _ck(self.lib.xnb_batch_set_force_lanes(self.h, int(lanes)))
+
+    def set_force_form(self, form):
+        """FORCE_THREAD (one thread per particle, default) or FORCE_STAGED (cell
+        segments staged in shared memory) for the mixed full-list traversal."""
+        _ck(self.lib.xnb_batch_set_force_form(self.h, int(form)))
 
     def set_build_form(self, form):
         """BUILD_ROWS (lane per particle, bulk-copied rows) or BUILD_WARP (lane per candidate)."""
