@@ -1259,30 +1259,31 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
     return xnb_check_errors(b, stream);
   };
   const int caps[3] = {384, 640, 1024}, blocks[2] = {128, 256}, forms[2] = {XNB_BUILD_ROWS, XNB_BUILD_WARP},
-            lanes[3] = {1, 2, 4}, fforms[2] = {XNB_FORCE_THREAD, XNB_FORCE_STAGED};
+            lanes[3] = {1, 2, 4};
   int best_sc = b->stage_cap, best_fb = b->force_block, best_nw = 0, best_fl = b->force_lanes;
   int best_bf = b->build_form == kBuildRows ? XNB_BUILD_ROWS : XNB_BUILD_WARP;
-  int best_ff = b->force_form == kForceStaged ? XNB_FORCE_STAGED : XNB_FORCE_THREAD;
+  // the batch's force form is kept: the staged form allocates 2 bytes per list
+  // entry when switched on, and it measured slower than the one-thread
+  // traversal at every size tried
+  const int best_ff = b->force_form == kForceStaged ? XNB_FORCE_STAGED : XNB_FORCE_THREAD;
   double best = 0.0;
   int rc = rate_of(best_sc, best_fb, best_nw, best_bf, best_fl, best_ff, &best);
   // coordinate search: one parameter at a time, the others at their best so far
   // (neighbour-build form, the stage cap of the forms that stage whole
   // neighbourhoods, the force block size, threads per particle of the force
   // traversal and the Newton traversal)
-  const int nvals[6] = {2, 3, 2, 3, 2, 2};
-  for (int pass = 0; pass < 6 && rc == 0; ++pass) {
+  const int nvals[5] = {2, 3, 2, 3, 2};
+  for (int pass = 0; pass < 5 && rc == 0; ++pass) {
     for (int v = 0; v < nvals[pass] && rc == 0; ++v) {
-      int sc = best_sc, fb = best_fb, nw = best_nw, bf = best_bf, fl = best_fl, ff = best_ff;
+      int sc = best_sc, fb = best_fb, nw = best_nw, bf = best_bf, fl = best_fl;
       if (pass == 0) bf = forms[v];
       else if (pass == 1) sc = caps[v];
       else if (pass == 2) fb = blocks[v];
       else if (pass == 3) fl = lanes[v];
-      else if (pass == 4) ff = fforms[v];
       else nw = v;
-      if (sc == best_sc && fb == best_fb && nw == best_nw && bf == best_bf && fl == best_fl && ff == best_ff)
-        continue;
+      if (sc == best_sc && fb == best_fb && nw == best_nw && bf == best_bf && fl == best_fl) continue;
       double r = 0.0;
-      rc = rate_of(sc, fb, nw, bf, fl, ff, &r);
+      rc = rate_of(sc, fb, nw, bf, fl, best_ff, &r);
       if (rc == 0 && r > best) {
         best = r;
         best_sc = sc;
@@ -1290,7 +1291,6 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
         best_nw = nw;
         best_bf = bf;
         best_fl = fl;
-        best_ff = ff;
       }
     }
   }
@@ -1302,8 +1302,6 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
   rc = xnb_batch_set_build_form(b, best_bf);
   if (rc) return rc;
   rc = xnb_batch_set_force_lanes(b, best_fl);
-  if (rc) return rc;
-  rc = xnb_batch_set_force_form(b, best_ff);
   if (rc) return rc;
   out->force_form = best_ff;
   out->stage_cap = best_sc;

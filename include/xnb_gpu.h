@@ -202,7 +202,7 @@ typedef struct xnb_tuning {
   double atom_steps_per_s;    /* the chosen configuration's measured rate */
   int32_t build_form;         /* XNB_BUILD_ROWS or XNB_BUILD_WARP */
   int32_t force_lanes;        /* threads per particle of the FP64 / mixed full-list force traversal */
-  int32_t force_form;         /* XNB_FORCE_THREAD or XNB_FORCE_STAGED */
+  int32_t force_form;         /* the batch's force form (XNB_FORCE_THREAD or XNB_FORCE_STAGED; not searched) */
   int32_t reserved;
 } xnb_tuning;
 
@@ -219,7 +219,9 @@ int xnb_batch_set_force_lanes(xnb_batch* b, int32_t lanes);
  *   neighbourhood (9 rows of 10 cells, periodic images included) is copied into
  *   shared memory first; the lists are read in a compact (cell group, index in
  *   cell) form written after each build. Forces, energies and velocities are
- *   bitwise equal to XNB_FORCE_THREAD. Switching it on allocates 2 bytes per
+ *   bitwise equal to XNB_FORCE_THREAD, and slower (4.65 against 2.62 ms per
+ *   4M-atom force call, plus 3 ms per rebuild for the compact entries, on
+ *   GB300). Switching it on allocates 2 bytes per
  *   list entry of the batch and a segment table, and compacts the current lists
  *   (synchronises the device). FP64 and Newton traversals are unaffected. */
 #define XNB_FORCE_THREAD 0
@@ -244,8 +246,8 @@ int xnb_batch_set_build_form(xnb_batch* b, int32_t form);
 int xnb_batch_set_tuning(xnb_batch* b, int32_t stage_cap, int32_t force_block);
 /* Online autotuner: coordinate search over the neighbour-build form
  * {ROWS, WARP}, stage_cap {384, 640, 1024}, force_block {128, 256}, force
- * threads per particle {1, 2, 4}, the mixed traversal form {THREAD, STAGED}
- * and the Newton traversal, each configuration timed
+ * threads per particle {1, 2, 4} and the Newton traversal (the batch's force
+ * form is kept), each configuration timed
  * (CUDA events on `stream`) over trial_steps of xnb_step without host sync
  * after one untimed step. The trials are real MD steps: the batch advances
  * (1 + trial_steps) x trials steps. The batch is left on the fastest
