@@ -106,6 +106,10 @@ def parse():
                     help="threads per particle of the FP64 / mixed force traversal (0: library default)")
     ap.add_argument("--force-form", default="", choices=["", "thread", "staged"],
                     help="mixed full-list force traversal form (empty: library default)")
+    ap.add_argument("--cell-factor", type=float, default=1.0,
+                    help="cells of at least this many times rcut + skin (> 1: dense cells with AMR sub-grids)")
+    ap.add_argument("--no-subcell-pruning", action="store_true",
+                    help="build dense cells' lists without the sub-cell pair pruning")
     ap.add_argument("--workload", default="lj", choices=["lj", "snap_ni", "snap_mo"],
                     help="lj: the 4M-atom LJ headline; snap_*: the reference's SNAP benchmark decks")
     return ap.parse_args()
@@ -171,11 +175,11 @@ class Clocks:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_workload(n):
+def make_workload(n, cell_factor=1.0):
     from exanbody_gb300 import workloads
 
     return workloads.lj_fcc_system(n, WORKLOAD["rho"], WORKLOAD["T"], WORKLOAD["seed"], WORKLOAD["rcut"],
-                                   WORKLOAD["skin"])
+                                   WORKLOAD["skin"], cell_factor)
 
 
 def cpu_oracle_run(w, steps, threads):
@@ -196,7 +200,7 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    w = make_workload(args.n)
+    w = make_workload(args.n, args.cell_factor)
     threads = os.cpu_count() or 1
     s, used = cpu_oracle_run(w, args.steps, threads)
     for _ in range(args.warmup):
@@ -266,7 +270,7 @@ def run_ours(args):
     stream = torch.cuda.Stream(device=dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
 
-    w = make_workload(args.n)
+    w = make_workload(args.n, args.cell_factor)
     N = w["n_atoms"]
     g = w["geom"]
     ncell = g["dims"][0] * g["dims"][1] * g["dims"][2]
@@ -282,6 +286,8 @@ def run_ours(args):
             b.set_force_lanes(args.force_lanes)
         if args.force_form:
             b.set_force_form({"thread": xnb.FORCE_THREAD, "staged": xnb.FORCE_STAGED}[args.force_form])
+        if args.no_subcell_pruning:
+            b.set_subcell_pruning(False)
         return b
 
     def timed(fn, reps=1):
@@ -479,7 +485,10 @@ def run_ours(args):
             "dtype": "f64+f32",
             "data": "synthetic",
             "config": config_of(args.n, N, parallelism="replicas" if world > 1 else "single",
-                                precision="mixed", rebuilds_in_timed_steps=rebuilds),
+                                precision="mixed", rebuilds_in_timed_steps=rebuilds,
+                                **({"cell_size": g["cell_size"], "atoms_per_cell": N / ncell,
+                                    "subcell_pruning": not args.no_subcell_pruning}
+                                   if args.cell_factor != 1.0 else {})),
             "fp64": {"value": value64, "unit": "atom-steps/s", "steps": k64,
                      "speedup_mixed_vs_fp64": value / world / value64},
             "traversals": dict(trials, unit="atom-steps/s", steps=k64,

@@ -101,6 +101,7 @@ struct xnb_batch {
   int force_form = kForceThread;  // mixed full-list traversal form (xnb_batch_set_force_form)
   std::vector<uint4> segs;      // cell segments of the staged traversal (host copy of a.seg)
   int build_form = kBuildWarp;  // neighbour-build kernel (xnb_batch_set_build_form)
+  int subcell_prune = 1;        // sub-cell pruned build of dense cells after a rebin (xnb_batch_set_subcell_pruning)
   DevArrays a{};
   SysDesc* d_sys = nullptr;
   SysState* d_st = nullptr;
@@ -141,7 +142,7 @@ struct xnb_graph {
   // work extent and launch configuration at capture
   uint32_t n_part = 0, n_cells = 0;
   int nsys = 0, lbuf = 0, stage_cap = 0, force_block = 0, force_lanes = 0, build_form = 0, far_coords = 0;
-  int force_form = 0;
+  int force_form = 0, subcell_prune = 0;
   uint32_t n_seg = 0;
 };
 
@@ -279,6 +280,11 @@ SysDesc make_desc(const xnb_lj_params& p) {
     while (n > 1 && static_cast<double>(n - 1) / d.sub_grid_density >= 8.0) --n;
     d.amr_min_n = static_cast<uint32_t>(n);
   }
+  // sub-cell pair pruning: two sub-cell boxes are searched together when their
+  // distance, in cells, is at most this (nbh / cell_size rounded up, then
+  // widened by 1e-5 so that rounding of positions, keys and images never drops a
+  // neighbour)
+  d.sub_reach_f = std::nextafter(static_cast<float>(nbh / p.cell_size * (1.0 + 1e-5)), 2.0f);
   d.dt = p.dt;
   d.dt_full = p.dt * 1.0;
   d.dt_sq_half = d.dt_full * d.dt_full * 0.5;
@@ -426,7 +432,8 @@ int size_lists(xnb_batch* b, int s, uint32_t need, cudaStream_t st) {
 int neighbors_sync(xnb_batch* b, cudaStream_t st) {
   const Extent ex = b->extent();
   for (int pass = 0; pass < 3; ++pass) {
-    b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, list_buf(b), st, b->build_form);
+    b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, list_buf(b), st, b->build_form,
+                                    b->subcell_prune != 0);
     int rc = pull_states(b, st);
     if (rc) return rc;
     bool again = false;
@@ -476,9 +483,10 @@ int xnb_version(void) { return 10000; }
 
 int64_t xnb_system_bytes(int64_t n, int64_t ncells, double list_per_particle) {
   // doubles r v f pe, restored backup, rebin scratch (22); ids (2); u32 cell, backup,
-  // rebin and list bookkeeping (10); FP32 hi/lo mirrors; types (2)
-  const int64_t per_part = 22 * 8 + 2 * 8 + 10 * 4 + 3 * 16 + 2;
-  const int64_t per_cell = 4 * 6 + 8 + 4;
+  // rebin and list bookkeeping (10); FP32 hi/lo mirrors; types (2); sub-cell key;
+  // per cell: u32 tables (6), scan, the two build lists and the sub-grid side
+  const int64_t per_part = 22 * 8 + 2 * 8 + 10 * 4 + 3 * 16 + 2 + 2;
+  const int64_t per_cell = 4 * 6 + 8 + 4 + 4 + 1;
   return n * per_part + ncells * per_cell + static_cast<int64_t>(static_cast<double>(n) * list_per_particle) * 4;
 }
 
@@ -531,6 +539,10 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   rc = rc ? rc : dalloc(b, &a.cell_scan, Cc + 1);
   rc = rc ? rc : dalloc(b, &a.nbr_wide, Cc + 1);
   rc = rc ? rc : dalloc(b, &a.nbr_wide_n, 1);
+  rc = rc ? rc : dalloc(b, &a.nbr_sub, Cc + 1);
+  rc = rc ? rc : dalloc(b, &a.nbr_sub_n, 1);
+  rc = rc ? rc : dalloc(b, &a.skey, P);
+  rc = rc ? rc : dalloc(b, &a.cside, Cc + 1);
   rc = rc ? rc : dalloc(b, &a.scan_blocks, scan_scratch_elems(static_cast<uint32_t>(Cc + 1)) + 8);
   rc = rc ? rc : dalloc(b, &a.nbr, L);
   rc = rc ? rc : dalloc(b, &b->d_sys, static_cast<uint64_t>(cfg->max_systems));
@@ -551,6 +563,8 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   cudaMemset(b->d_st, 0, sizeof(SysState) * cfg->max_systems);
   cudaMemset(a.any_rebuild, 0, sizeof(unsigned int));
   cudaMemset(a.nbr_wide_n, 0, sizeof(unsigned int));
+  cudaMemset(a.nbr_sub_n, 0, sizeof(unsigned int));
+  cudaMemset(a.cside, 1, Cc + 1);
   if (cudaDeviceSynchronize() != cudaSuccess) {
     xnb_batch_destroy(b);
     return fail(XNB_ERR_CUDA, "initialisation failed");
@@ -1078,7 +1092,8 @@ int xnb_step(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, voi
         int rc = neighbors_sync(b, st);
         if (rc) return rc;
       } else {
-        b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, list_buf(b), st, b->build_form);
+        b->launches += launch_neighbors(ex, b->d_sys, b->d_st, b->a, b->stage_cap, list_buf(b), st, b->build_form,
+                                        b->subcell_prune != 0);
       }
     }
     // compute_all_forces_energy + verlet_second_half
@@ -1117,6 +1132,7 @@ int xnb_step_graph_create(xnb_batch* b, int32_t nsteps, int32_t precision, int32
   G->force_block = b->force_block;
   G->force_lanes = b->force_lanes;
   G->build_form = b->build_form;
+  G->subcell_prune = b->subcell_prune;
   const cudaError_t ie = cudaGraphInstantiate(&G->exec, g, 0);
   if (ie != cudaSuccess) {
     cudaGraphDestroy(g);
@@ -1135,7 +1151,7 @@ int xnb_graph_is_current(const xnb_graph* g) {
           ex.force_form == g->force_form && ex.n_seg == g->n_seg &&
           list_buf(b) == g->lbuf &&
           b->stage_cap == g->stage_cap && b->force_block == g->force_block && b->force_lanes == g->force_lanes &&
-          b->build_form == g->build_form)
+          b->build_form == g->build_form && b->subcell_prune == g->subcell_prune)
              ? 1
              : 0;
 }
@@ -1217,6 +1233,13 @@ int xnb_batch_set_build_form(xnb_batch* b, int32_t form) {
   if (!b) return fail(XNB_ERR_ARG, "null batch");
   if (form != XNB_BUILD_ROWS && form != XNB_BUILD_WARP) return fail(XNB_ERR_ARG, "unknown neighbour-build form");
   b->build_form = form == XNB_BUILD_ROWS ? kBuildRows : kBuildWarp;
+  return XNB_OK;
+}
+
+int xnb_batch_set_subcell_pruning(xnb_batch* b, int32_t on) {
+  if (!b) return fail(XNB_ERR_ARG, "null batch");
+  if (on != 0 && on != 1) return fail(XNB_ERR_ARG, "subcell pruning is 0 or 1");
+  b->subcell_prune = on;
   return XNB_OK;
 }
 

@@ -295,6 +295,7 @@ __global__ void __launch_bounds__(128)
     // (a warp-wide FP64 instruction costs the same for one lane as for 32)
     const int side = (S.amr_enabled && n >= S.amr_min_n) ? sub_grid_side(n, S.sub_grid_density) : 1;
     // backup_r runs afterwards in k_backup, one thread per particle
+    if (lane == 0) a.cside[c] = static_cast<uint8_t>(side);
     if (side > 1) {
       cell_ijk(S, c - S.cell_base, ci, cj, ck);
       const double lo[3] = {cell_lo(S, 0, ci), cell_lo(S, 1, cj), cell_lo(S, 2, ck)};
@@ -338,6 +339,7 @@ __global__ void __launch_bounds__(128)
       a.pf[dst] = mhi;
       a.pflo[dst] = mlo;
       a.pcell[dst] = c;
+      if (side > 1) a.skey[dst] = static_cast<uint16_t>(a.pdest[src]);
     }
     if (lane == 0) {
       a.cell_start[c] = ns;
@@ -387,10 +389,15 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-__global__ void k_arm(int nsys, SysState* st, const unsigned int* any) {
+// backup_r done for the flagged systems; after a rebin their sub-cell keys
+// (k_rebin_finalize) also describe the current positions
+__global__ void k_arm(int nsys, SysState* st, const unsigned int* any, bool rebinned) {
   if (*any == 0) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < nsys && st[s].rebuild) st[s].rebuild_armed = 1;
+  if (s < nsys && st[s].rebuild) {
+    st[s].rebuild_armed = 1;
+    if (rebinned) st[s].keys_fresh = 1;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -643,70 +650,9 @@ __global__ void __launch_bounds__(128, 8)
 // warp-uniform branches: a chunk holding a candidate whose ghost filter is
 // undecided in FP32, and an FP32 distance inside the error band around nbh^2
 // (both then take the reference's FP64 decision, as in k_neighbors).
-constexpr int kNbrP = 4;  // particles tested per staged candidate load (even: FP32x2 pairs)
-
-template <bool AMB, bool SELF>
-__device__ __forceinline__ void nbr_chunk(const SysDesc& S, const DevArrays& a, const float4 b, const float (&px)[kNbrP],
-                                          const float (&py)[kNbrP], const float (&pz)[kNbrP], uint32_t i0,
-                                          uint32_t self0, uint32_t t0, uint32_t low0, float nb_lo, float nb_hi,
-                                          float nb_zero, unsigned lt, uint32_t* sbuf, uint32_t lbuf,
-                                          uint32_t (&cur)[kNbrP], uint32_t (&half)[kNbrP]) {
-  const uint32_t ent = __float_as_uint(b.w);
-  const bool amb = AMB && (ent & kAmbiguousBit) != 0;
-  bool hit[kNbrP], may[kNbrP];
-  bool any_may = false;
-  // squared FP32 distances two particles at a time on the packed FP32x2 path:
-  // per particle the roundings of fmaf(dx, dx, fmaf(dy, dy, dz * dz)) exactly
-  float dd[kNbrP];
-  {
-    unsigned long long bx2, by2, bz2;
-    asm("mov.b64 %0, {%1, %1};" : "=l"(bx2) : "f"(b.x));
-    asm("mov.b64 %0, {%1, %1};" : "=l"(by2) : "f"(b.y));
-    asm("mov.b64 %0, {%1, %1};" : "=l"(bz2) : "f"(b.z));
-#pragma unroll
-    for (int k = 0; k < kNbrP; k += 2) {
-      unsigned long long x2, y2, z2, dx, dy, dz, d;
-      asm("mov.b64 %0, {%1, %2};" : "=l"(x2) : "f"(px[k]), "f"(px[k + 1]));
-      asm("mov.b64 %0, {%1, %2};" : "=l"(y2) : "f"(py[k]), "f"(py[k + 1]));
-      asm("mov.b64 %0, {%1, %2};" : "=l"(z2) : "f"(pz[k]), "f"(pz[k + 1]));
-      asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(dx) : "l"(x2), "l"(bx2));
-      asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(dy) : "l"(y2), "l"(by2));
-      asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(dz) : "l"(z2), "l"(bz2));
-      asm("mul.rn.f32x2 %0, %1, %1;" : "=l"(d) : "l"(dz));
-      asm("fma.rn.f32x2 %0, %1, %1, %2;" : "=l"(d) : "l"(dy), "l"(d));
-      asm("fma.rn.f32x2 %0, %1, %1, %2;" : "=l"(d) : "l"(dx), "l"(d));
-      asm("mov.b64 {%0, %1}, %2;" : "=f"(dd[k]), "=f"(dd[k + 1]) : "l"(d));
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < kNbrP; ++k) {
-    const float d = dd[k];
-    hit[k] = d < nb_lo && d > nb_zero && !amb;
-    // the particle's own entry only sits in a SELF chunk (d = 0 there: no hit)
-    may[k] = !hit[k] && d <= nb_hi && (!SELF || ent != self0 + (static_cast<uint32_t>(k) << 5));
-    any_may |= may[k];
-  }
-  if (__any_sync(0xffffffffu, any_may)) {
-#pragma unroll
-    for (int k = 0; k < kNbrP; ++k)
-      if (may[k]) hit[k] = exact_neighbor_test(S, a, i0 + k, ent);
-  }
-  const uint32_t e = AMB ? (ent & ~kAmbiguousBit) : ent;
-#pragma unroll
-  for (int k = 0; k < kNbrP; ++k) {
-    const unsigned m = __ballot_sync(0xffffffffu, hit[k]);
-    // entries past the slot land in the buffer's last word, which is never written out
-    if (hit[k]) sbuf[k * lbuf + min(cur[k] + __popc(m & lt), lbuf - 1u)] = e;
-    if (SELF) {
-      const uint32_t w = low0 + static_cast<uint32_t>(k) - t0;
-      if (w < 32u) half[k] = cur[k] + __popc(m & ((1u << w) - 1u));
-    }
-    cur[k] += __popc(m);
-  }
-}
-
 __global__ void __launch_bounds__(128)
-    k_neighbors_warp(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap, int lbuf) {
+    k_neighbors_warp(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap, int lbuf,
+                     bool prune) {
   if (*a.any_rebuild == 0) return;
   extern __shared__ float4 stage_w[];
   const uint32_t lane = threadIdx.x & 31;
@@ -724,6 +670,10 @@ __global__ void __launch_bounds__(128)
     if (s == kInvalid || !sys_flagged(st, s)) continue;
     const uint32_t na = a.cell_n[c];
     if (na == 0) continue;
+    if (prune && a.cside[c] >= 2 && st[s].keys_fresh) {
+      if (lane == 0) a.nbr_sub[atomicAdd(a.nbr_sub_n, 1u)] = c;
+      continue;
+    }
     const SysDesc& S = sys[s];
     const uint32_t sa = a.cell_start[c];
     int ci, cj, ck;
@@ -872,8 +822,12 @@ __global__ void __launch_bounds__(128)
 }
 
 // Clears the per-build list statistics of the flagged systems.
-__global__ void k_nbr_reset(int nsys, SysState* st, const unsigned int* any, unsigned int* wide_n) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) *wide_n = 0;
+__global__ void k_nbr_reset(int nsys, SysState* st, const unsigned int* any, unsigned int* wide_n,
+                            unsigned int* sub_n) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *wide_n = 0;
+    *sub_n = 0;
+  }
   if (*any == 0) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsys || !st[s].rebuild) return;
@@ -1019,19 +973,19 @@ int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevAr
   k_rebin_finalize<<<wg, 128, 0, stream>>>(ex.n_cells, sys, st, a);
   if (exact_backup) k_backup<true><<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
   else k_backup<false><<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
-  k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild);
+  k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild, true);
   return 7 + ns;
 }
 
 int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream) {
   if (ex.n_part == 0) return 0;
   k_backup<true><<<thread_grid(ex.n_part, 256, ex.sm_count), 256, 0, stream>>>(ex.n_part, sys, st, a);
-  k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild);
+  k_arm<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild, false);
   return 2;
 }
 
 int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int cap, int lbuf,
-                     cudaStream_t stream, int form) {
+                     cudaStream_t stream, int form, bool prune) {
   if (ex.n_cells == 0) return 0;
   const size_t smem = static_cast<size_t>(cap) * sizeof(float4) + static_cast<size_t>(4) * 2 * lbuf * sizeof(uint32_t);
   // warp-per-cell buffers: one slot of each of kNbrP particles plus a spill word
@@ -1046,13 +1000,15 @@ int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const D
     per_sm = 1;
   const long long want_w = (static_cast<long long>(ex.n_cells) + 3) / 4;
   const int grid_w = static_cast<int>(std::max(1ll, std::min(want_w, static_cast<long long>(per_sm) * ex.sm_count)));
-  k_nbr_reset<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild, a.nbr_wide_n);
-  if (form == kBuildRows) launch_neighbors_rows(ex, sys, st, a, stream);
-  else k_neighbors_warp<<<grid_w, 128, smem_w, stream>>>(ex.n_cells, sys, st, a, cap, lbuf_w);
+  k_nbr_reset<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild, a.nbr_wide_n, a.nbr_sub_n);
+  if (form == kBuildRows) launch_neighbors_rows(ex, sys, st, a, stream, prune);
+  else k_neighbors_warp<<<grid_w, 128, smem_w, stream>>>(ex.n_cells, sys, st, a, cap, lbuf_w, prune);
+  // dense cells (sub-grid side >= 2), before the block-per-cell build, which takes the ones it passes on
+  const int nsub = prune ? launch_neighbors_sub(ex, sys, st, a, cap, stream) : 0;
   k_neighbors<<<warp_grid(ex.n_cells, 1, ex.sm_count), 128, smem, stream>>>(ex.n_cells, sys, st, a, cap, lbuf);
   // compact entries for the staged force traversal
   const int nc = ex.force_form == kForceStaged ? launch_compact_lists(ex, sys, st, a, stream) : 0;
-  return 3 + nc;
+  return 3 + nsub + nc;
 }
 
 }  // namespace xnb

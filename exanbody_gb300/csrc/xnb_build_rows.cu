@@ -374,7 +374,7 @@ __device__ __forceinline__ bool rows_cell(RowsWarp& w, const SysDesc& S, SysStat
 }
 
 __global__ void __launch_bounds__(128)
-    k_neighbors_rows(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a) {
+    k_neighbors_rows(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, bool prune) {
   if (*a.any_rebuild == 0) return;
   extern __shared__ __align__(16) unsigned char rows_smem[];
   const uint32_t lane = threadIdx.x & 31;
@@ -396,6 +396,10 @@ __global__ void __launch_bounds__(128)
     if (s == kInvalid || !sys_flagged(st, s)) continue;
     const uint32_t na = a.cell_n[c];
     if (na == 0) continue;
+    if (prune && a.cside[c] >= 2 && st[s].keys_fresh) {
+      if (lane == 0) a.nbr_sub[atomicAdd(a.nbr_sub_n, 1u)] = c;
+      continue;
+    }
     const SysDesc& S = sys[s];
     int ci, cj, ck;
     cell_ijk(S, c - S.cell_base, ci, cj, ck);
@@ -438,7 +442,8 @@ __global__ void __launch_bounds__(128)
 
 }  // namespace
 
-int launch_neighbors_rows(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream) {
+int launch_neighbors_rows(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream,
+                          bool prune) {
   if (ex.n_cells == 0) return 0;
   const size_t smem = 4 * sizeof(RowsWarp);
   cudaFuncSetAttribute(k_neighbors_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -447,7 +452,7 @@ int launch_neighbors_rows(const Extent& ex, const SysDesc* sys, SysState* st, co
     per_sm = 1;
   const long long want = (static_cast<long long>(ex.n_cells) + 3) / 4;
   const int grid = static_cast<int>(std::max(1ll, std::min(want, static_cast<long long>(per_sm) * ex.sm_count)));
-  k_neighbors_rows<<<grid, 128, smem, stream>>>(ex.n_cells, sys, st, a);
+  k_neighbors_rows<<<grid, 128, smem, stream>>>(ex.n_cells, sys, st, a, prune);
   return 1;
 }
 

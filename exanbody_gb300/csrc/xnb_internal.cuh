@@ -68,6 +68,7 @@ struct SysDesc {
   // the position and of its backup is above trig_hi_f only when the FP64 |d|^2
   // reaches max_displ2, below trig_lo_f only when it does not
   float trig_lo_f, trig_hi_f;
+  float sub_reach_f;             // nbh_dist / cell_size widened by 1e-5: reach of the sub-cell box test (cells)
   double inv_cell;               // fl(1/cell_size): reciprocal pre-decision of the backup encoding
   double m24eps, eps4, sig2, eps24;  // -24*eps, 4*eps (lennard_jones.cu:54-55), sigma^2, 24*eps
   int32_t dims[3];
@@ -94,6 +95,7 @@ struct SysState {
   uint32_t max_nbr;              // largest per-particle list count of the last build
   uint32_t lists_fresh;          // 1 from a neighbour build until positions next change
   uint32_t compact_bad;          // the last build's lists could not be compacted (staged force traversal)
+  uint32_t keys_fresh;           // 1 from a rebin until positions next change: the sub-cell keys fit them
   unsigned long long rebuilds;
 };
 
@@ -134,6 +136,10 @@ struct DevArrays {
   uint4* seg;                      // cell segments of the staged force traversal: first cell, cells, system
   uint32_t* nbr_wide;              // cells whose candidates or slot exceed the warp-per-cell build's buffers
   unsigned int* nbr_wide_n;        // number of them (reset by each build)
+  uint32_t* nbr_sub;               // dense cells (sub-grid side >= 2) for the sub-cell pruned build
+  unsigned int* nbr_sub_n;         // number of them (reset by each build)
+  uint16_t* skey;                  // sub-cell key of each particle of a cell with side >= 2 (k_rebin_finalize)
+  uint8_t* cside;                  // sub-grid side of each cell at the last rebin (1: no sub-grid)
   // scan scratch
   unsigned long long* scan_blocks;
 };

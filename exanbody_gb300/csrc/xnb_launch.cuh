@@ -71,12 +71,20 @@ int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevA
 // shared memory, xnb_build_rows.cu) or kBuildWarp (lane per candidate, the
 // 27-cell block staged per warp); cells neither handles go to the
 // block-per-cell build.
+// prune: cells with a sub-grid go to the sub-cell pruned build (xnb_build_sub.cu)
+// when their system's sub-cell keys still describe its positions (keys_fresh:
+// set by the rebin, cleared when positions are pushed).
 constexpr int kBuildRows = 0;
 constexpr int kBuildWarp = 1;
 int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int stage_cap,
-                     int lbuf, cudaStream_t stream, int form = kBuildRows);
+                     int lbuf, cudaStream_t stream, int form = kBuildRows, bool prune = false);
 // the lane-per-particle build alone (cells it cannot take are appended to a.nbr_wide)
-int launch_neighbors_rows(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream);
+int launch_neighbors_rows(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream,
+                          bool prune);
+// the sub-cell pruned build of the cells listed in a.nbr_sub (cells with a
+// neighbour of sub-grid side above 3 are passed on to a.nbr_wide)
+int launch_neighbors_sub(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int stage_cap,
+                         cudaStream_t stream);
 
 // Reference-format chunk-neighbour streams of system sid (xnb_stream.cu):
 // per-cell lengths (u16 units), the streams at cell_off, and the checker

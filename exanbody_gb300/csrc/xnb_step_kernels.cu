@@ -25,9 +25,12 @@ __global__ void __launch_bounds__(256)
                  bool push_r, bool push_v, bool trigger, double scale_r, double scale_v, int sys_only) {
   const bool canonical = (scale_r == 1.0 && scale_v == 0.5);
   if (push_r && blockIdx.x == 0) {
-    // positions change: lists no longer describe the current positions exactly
+    // positions change: lists and sub-cell keys no longer describe them exactly
     for (int s = static_cast<int>(threadIdx.x); s < nsys; s += static_cast<int>(blockDim.x))
-      if (sys_only < 0 || s == sys_only) st[s].lists_fresh = 0;
+      if (sys_only < 0 || s == sys_only) {
+        st[s].lists_fresh = 0;
+        st[s].keys_fresh = 0;
+      }
   }
   // every lane of a warp runs the same number of iterations, so full-warp
   // collectives below see all 32 lanes

@@ -18,8 +18,10 @@ import numpy as np
 FCC_BASIS = np.array([[0.0, 0.0, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0]])
 
 
-def geometry(lengths, rcut=2.5, skin=0.3):
-    nbh = rcut + skin
+def geometry(lengths, rcut=2.5, skin=0.3, cell_factor=1.0):
+    """Periodic box of the given lengths cut into cubic cells of at least
+    cell_factor * (rcut + skin) (cell_factor >= 1: denser cells, AMR sub-grids)."""
+    nbh = (rcut + skin) * cell_factor
     lengths = [float(x) for x in lengths]
     dmin = [int(math.floor(L / nbh)) for L in lengths]
     # one cubic cell size for all axes: the smallest L/D over axes
@@ -49,21 +51,21 @@ def maxwell_boltzmann(nparticles, temperature, seed, mass=1.0):
     return v
 
 
-def lj_fcc_system(n, rho=0.8442, temperature=1.44, seed=12345, rcut=2.5, skin=0.3):
+def lj_fcc_system(n, rho=0.8442, temperature=1.44, seed=12345, rcut=2.5, skin=0.3, cell_factor=1.0):
     """Periodic FCC n^3 system: positions, velocities, ids, geometry."""
     r, a = fcc_lattice(n, rho)
     L = n * a
-    geom = geometry((L, L, L), rcut, skin)
+    geom = geometry((L, L, L), rcut, skin, cell_factor)
     v = maxwell_boltzmann(len(r), temperature, seed)
     ids = np.arange(len(r), dtype=np.uint64)
     return {"r": r, "v": v, "id": ids, "geom": geom, "a": a, "n_atoms": len(r), "rho": rho, "T": temperature}
 
 
-def lj_slab_system(n, rho=0.8442, temperature=0.8, seed=12345, rcut=2.5, skin=0.3):
+def lj_slab_system(n, rho=0.8442, temperature=0.8, seed=12345, rcut=2.5, skin=0.3, cell_factor=1.0):
     """Liquid-vacuum slab: FCC n^3 filling the middle half of a (L, L, 2L) box."""
     r, a = fcc_lattice(n, rho)
     L = n * a
-    geom = geometry((L, L, 2.0 * L), rcut, skin)
+    geom = geometry((L, L, 2.0 * L), rcut, skin, cell_factor)
     r = r.copy()
     r[:, 2] += 0.5 * geom["extent"][2] * 0.5
     v = maxwell_boltzmann(len(r), temperature, seed)

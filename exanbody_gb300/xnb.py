@@ -47,6 +47,7 @@ EXPORTED = [
     "xnb_gravitational_force", "xnb_batch_set_tuning", "xnb_autotune", "xnb_snap_create", "xnb_snap_destroy",
     "xnb_snap_force", "xnb_system_pairs_range", "xnb_system_pair_view", "xnb_batch_set_build_form",
     "xnb_graph_is_current", "xnb_batch_set_force_lanes", "xnb_batch_set_force_form",
+    "xnb_batch_set_subcell_pruning",
 ]
 
 FORCE_ENERGY = 1
@@ -185,6 +186,7 @@ def load(build_if_missing=True):
     lib.xnb_graph_is_current.argtypes = [vp]
     lib.xnb_batch_set_force_lanes.argtypes = [vp, i32]
     lib.xnb_batch_set_force_form.argtypes = [vp, i32]
+    lib.xnb_batch_set_subcell_pruning.argtypes = [vp, i32]
     lib.xnb_system_energy.argtypes = [vp, i32, P(d), P(d), vp]
     lib.xnb_init_particles.argtypes = [vp, i32, i32, vp]
     lib.xnb_push_f_v_r.argtypes = [vp, i32, d, vp]
@@ -468,6 +470,13 @@ class Batch:
     def set_build_form(self, form):
         """BUILD_ROWS (lane per particle, bulk-copied rows) or BUILD_WARP (lane per candidate)."""
         _ck(self.lib.xnb_batch_set_build_form(self.h, int(form)))
+
+    def set_subcell_pruning(self, on):
+        """Sub-cell pair pruning of the neighbour build (default on): while the
+        positions are those of the last rebin, dense cells (AMR sub-grid side 2
+        or 3) search only the neighbour sub-cells within reach of each sub-cell;
+        the lists are the same."""
+        _ck(self.lib.xnb_batch_set_subcell_pruning(self.h, 1 if on else 0))
 
     def autotune(self, trial_steps=20, precision=PREC_MIXED):
         """Online autotuner (xnb_autotune): the batch advances while it is timed and is

@@ -242,6 +242,18 @@ int xnb_batch_set_force_form(xnb_batch* b, int32_t form);
 #define XNB_BUILD_WARP 1
 int xnb_batch_set_build_form(xnb_batch* b, int32_t form);
 
+/* Sub-cell pair pruning of the neighbour build (on by default), after
+ * max_distance_sub_cell_pairs / AmrSubCellPairCache
+ * (amr/lib/amr_grid_algorithm.cpp:102-218, used at
+ * particle_neighbors/include/exanb/particle_neighbors/chunk_neighbors_execute.h:160-244).
+ * While a system's positions are those of its last rebin (the rebuild steps of
+ * xnb_step, xnb_init_particles, xnb_update_particles_full, and xnb_chunk_neighbors
+ * until positions next change), cells with an AMR sub-grid (side 2 or 3) test
+ * each sub-cell's particles only against the sub-cells of the 27 neighbour cells
+ * whose boxes lie within nbh_dist of it; after positions change, a build without
+ * a rebin searches whole cells. The lists are the same either way. */
+int xnb_batch_set_subcell_pruning(xnb_batch* b, int32_t on);
+
 /* Changes the launch configuration of a live batch (same limits as at creation). */
 int xnb_batch_set_tuning(xnb_batch* b, int32_t stage_cap, int32_t force_block);
 /* Online autotuner: coordinate search over the neighbour-build form
