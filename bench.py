@@ -345,6 +345,15 @@ def run_ours(args):
     g_mixed.close()
     value = world * N * args.steps / (ms * 1e-3)
 
+    # ---- the same mixed steps through the persistent step loop (xnb_step_persistent:
+    # one cooperative launch per run of steps between rebuilds; full lists only) ----
+    persistent = None
+    if not MIXED & xnb.PREC_NEWTON:
+        b.step_persistent(2, MIXED)
+        msp = timed(lambda: b.step_persistent(k64, MIXED))
+        persistent = {"atom_steps_per_s": N * k64 / (msp * 1e-3), "ms_per_step": msp / k64, "steps": k64}
+        b.check_errors()
+
     # ---- plain FP64 path at its faster traversal, from the same state, the same way ----
     b.step(2, FP64, 0)
     g64 = b.graph(k64, FP64, 0)
@@ -384,6 +393,7 @@ def run_ours(args):
         "neighbour_build_ms_per_rebuild": ms_nbr,
         "rebuild_path_ms_per_rebuild": ms_upd,
         "rebuilds_in_timed_steps": rebuilds,
+        "persistent_loop_mixed": persistent,
         "note": "force-only: lennard_jones_force on the post-run state; neighbour build: xnb_chunk_neighbors "
                 "(rebuild mark + one-pass list build); rebuild path: xnb_update_particles_full (rebin, backup, "
                 "list build); CUDA events around each call",

@@ -109,6 +109,7 @@ struct xnb_batch {
   unsigned int* d_flag = nullptr;             // scratch error flag of the stream writer
   unsigned long long* d_counts = nullptr;     // scratch counters of the stream checker
   unsigned char* d_stats = nullptr;           // scratch of the simulation_stats reduction
+  StepCtl* d_ctl = nullptr;                   // control block of the persistent step loop
   std::vector<SysHost> sys;
   RangeAlloc parts, cells, lists;
   std::vector<void*> allocs;
@@ -550,6 +551,7 @@ int xnb_batch_create(const xnb_batch_config* cfg, xnb_batch** out) {
   rc = rc ? rc : dalloc(b, &b->d_flag, 1);
   rc = rc ? rc : dalloc(b, &b->d_counts, 8);
   rc = rc ? rc : dalloc(b, &b->d_stats, stats_scratch_bytes());
+  rc = rc ? rc : dalloc(b, &b->d_ctl, 1);
   if (!rc && cudaMallocHost(&b->h_st, sizeof(SysState) * cfg->max_systems) != cudaSuccess)
     rc = fail(XNB_ERR_NOMEM, "cudaMallocHost failed");
   if (rc) {
@@ -1099,6 +1101,49 @@ int xnb_step(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, voi
     // compute_all_forces_energy + verlet_second_half
     b->launches += launch_force(ex, b->d_sys, b->d_st, b->a, precision, energy, true, -1, st, newton);
     b->launches += launch_clear_moved(ex, b->d_st, st);
+  }
+  return check_launch();
+}
+
+int xnb_step_persistent(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, void* stream) {
+  if (!b) return fail(XNB_ERR_ARG, "null batch");
+  if (nsteps < 0) return fail(XNB_ERR_ARG, "nsteps must be >= 0");
+  if (flags & ~(XNB_STEP_HOST_SYNC | XNB_STEP_ENERGY | XNB_STEP_BARRIER_CHECK)) return fail(XNB_ERR_ARG, "bad flags");
+  int base = 0;
+  bool newton = false;
+  int rc = decode_precision(precision, &base, &newton);
+  if (rc) return rc;
+  if (newton) return fail(XNB_ERR_ARG, "the persistent step loop runs the full-list traversal");
+  for (const SysHost& h : b->sys)
+    if (h.active && !h.initialised) return fail(XNB_ERR_ARG, "call xnb_init_particles first");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  XCK(cudaSetDevice(b->device));
+  const Extent ex = b->extent();
+  const bool exact = base == XNB_PREC_FP64_EXACT;
+  const bool energy = (flags & XNB_STEP_ENERGY) != 0;
+  const bool check = (flags & XNB_STEP_BARRIER_CHECK) != 0;
+  int remaining = nsteps;
+  while (remaining > 0 || check) {
+    XCK(cudaMemsetAsync(b->d_ctl, 0, sizeof(StepCtl), st));
+    b->launches += launch_steps_persistent(ex, b->d_sys, b->d_st, b->a, base, energy, b->d_ctl, remaining, check, st);
+    rc = check_launch();
+    if (rc) return rc;
+    StepCtl h{};
+    XCK(cudaMemcpyAsync(&h, b->d_ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost, st));
+    XCK(cudaStreamSynchronize(st));
+    if (h.error) return fail(XNB_ERR_DEVICE, "a grid barrier of the persistent step loop ran out of time");
+    if (check) return fail(XNB_ERR_ARG, "the barrier check did not run out");
+    remaining -= static_cast<int>(h.steps_done);
+    if (h.stopped) {
+      // the rest of the step whose trigger fired: rebuild path, forces and kick
+      b->launches += launch_mark_rebuild(ex, b->d_st, 1, -1, b->a.any_rebuild, st);
+      b->launches += launch_rebin(ex, b->d_sys, b->d_st, b->a, st, exact);
+      rc = neighbors_sync(b, st);
+      if (rc) return rc;
+      b->launches += launch_force(ex, b->d_sys, b->d_st, b->a, base, energy, true, -1, st, false);
+      b->launches += launch_clear_moved(ex, b->d_st, st);
+      remaining -= 1;
+    }
   }
   return check_launch();
 }

@@ -56,6 +56,25 @@ int launch_mark_rebuild(const Extent& ex, SysState* st, int mode, int sys_only, 
                         cudaStream_t stream);
 int launch_clear_moved(const Extent& ex, SysState* st, cudaStream_t stream);
 
+// Control block of the persistent step loop (device memory, zeroed before each launch).
+struct StepCtl {
+  unsigned int arrive;      // grid barrier: blocks arrived at the current barrier
+  unsigned int generation;  // grid barrier: barriers completed
+  unsigned int fired[2];    // per step parity: an armed system's displacement trigger fired
+  unsigned int steps_done;  // whole steps completed by the launch
+  unsigned int stopped;     // 1: stopped after the first half of step steps_done (the trigger fired)
+  unsigned int error;       // 1: a barrier wait ran out
+  unsigned int pad;
+};
+// Up to max_steps whole MD steps (first half + trigger, grid barrier, forces with
+// the second-half kick, grid barrier) in one cooperative launch, one thread per
+// particle, full lists; it stops after the first half of a step whose trigger
+// fired. check: the first barrier waits for one block more than the launch has,
+// so every wait runs out after wait_ns and the launch returns before changing
+// any state (a test of the timeout path). Returns the number of launches.
+int launch_steps_persistent(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int precision,
+                            bool with_pe, StepCtl* ctl, int max_steps, bool check, cudaStream_t stream);
+
 // move_particles + migrate + rebuild_amr + backup_r for systems with rebuild != 0.
 // exact_backup = false keeps the backup position unencoded (FP64 and mixed paths).
 int launch_rebin(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream,

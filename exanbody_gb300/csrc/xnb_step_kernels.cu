@@ -1,5 +1,7 @@
 // Per-step kernels: velocity-Verlet pushes with the displacement trigger, and the
 // Lennard-Jones pair-force traversal over the neighbour lists.
+#include <algorithm>
+
 #include "xnb_launch.cuh"
 #include "xnb_lj_pair.cuh"
 #include "xnb_traverse.cuh"
@@ -19,10 +21,13 @@ constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 //                norm2(r - restore(backup)) >= max_displ^2, counted per system.
 // EXACT=true keeps the reference's two roundings per product/sum (bit-identical
 // trajectory); EXACT=false lets the compiler fuse them into FMAs.
+// fired (or null): set to 1 when a particle of an armed system is over the
+// displacement threshold (the persistent step loop stops there).
 template <bool EXACT>
-__global__ void __launch_bounds__(256)
-    k_first_half(uint32_t n_part, int nsys, const SysDesc* __restrict__ sys, SysState* __restrict__ st, DevArrays a,
-                 bool push_r, bool push_v, bool trigger, double scale_r, double scale_v, int sys_only) {
+__device__ __forceinline__ void first_half_body(uint32_t n_part, int nsys, const SysDesc* __restrict__ sys,
+                                                SysState* __restrict__ st, const DevArrays& a, bool push_r,
+                                                bool push_v, bool trigger, double scale_r, double scale_v,
+                                                int sys_only, unsigned int* fired) {
   const bool canonical = (scale_r == 1.0 && scale_v == 0.5);
   if (push_r && blockIdx.x == 0) {
     // positions change: lists and sub-cell keys no longer describe them exactly
@@ -121,10 +126,19 @@ __global__ void __launch_bounds__(256)
       const unsigned same = __match_any_sync(0xffffffffu, s);
       const unsigned hits = __ballot_sync(0xffffffffu, over) & same;
       const int leader = __ffs(same) - 1;
-      if (s != kInvalid && static_cast<int>(threadIdx.x & 31) == leader && hits)
+      if (s != kInvalid && static_cast<int>(threadIdx.x & 31) == leader && hits) {
         atomicAdd(&st[s].moved, static_cast<unsigned long long>(__popc(hits)));
+        if (fired) atomicOr(fired, 1u);
+      }
     }
   }
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256)
+    k_first_half(uint32_t n_part, int nsys, const SysDesc* __restrict__ sys, SysState* __restrict__ st, DevArrays a,
+                 bool push_r, bool push_v, bool trigger, double scale_r, double scale_v, int sys_only) {
+  first_half_body<EXACT>(n_part, nsys, sys, st, a, push_r, push_v, trigger, scale_r, scale_v, sys_only, nullptr);
 }
 
 // 72 registers: 7 blocks of 128 threads per SM (measured faster than the
@@ -421,6 +435,115 @@ void force_dispatch(const Extent& ex, const SysDesc* sys, const SysState* st, co
   k_force<P, PE, KICK><<<grid_for(ex.n_part, threads), threads, 0, stream>>>(ex.n_part, src, f);
 }
 
+
+// ---------------------------------------------------------------------------
+// Persistent step loop: one cooperative launch advances the batch step after
+// step, with a grid barrier between the first half (push_f_v_r, push_f_v,
+// trigger) and the forces, and another after the forces. Each phase runs the
+// same per-particle code as k_first_half / k_force, so the states are bitwise
+// those of xnb_step. The loop stops after the first half of a step whose
+// trigger fired (the rebuild path and that step's forces then run as separate
+// launches). The trigger flag alternates between two words by step parity:
+// every block reads step k's word after the first barrier of step k, and block
+// 0 clears the other word during step k's forces, after every block has read it
+// at step k - 1 and before step k + 1 sets it.
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Blocks count in; the last one resets the count and bumps the generation, the
+// others poll the generation for at most wait_ns. A wait that runs out records
+// the error and returns false (the loop then ends without another barrier).
+__device__ bool grid_barrier(StepCtl* ctl, unsigned int nblocks, unsigned long long wait_ns) {
+  __syncthreads();
+  int ok = 1;
+  if (threadIdx.x == 0) {
+    const unsigned int gen = ld_acquire_u32(&ctl->generation);
+    __threadfence();
+    if (atomicAdd(&ctl->arrive, 1u) == nblocks - 1u) {
+      atomicExch(&ctl->arrive, 0u);
+      __threadfence();
+      atomicAdd(&ctl->generation, 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (ld_acquire_u32(&ctl->generation) == gen) {
+        if (global_ns() - t0 > wait_ns) {
+          atomicOr(&ctl->error, 1u);
+          ok = 0;
+          break;
+        }
+        __nanosleep(100);
+      }
+    }
+    __threadfence();
+  }
+  return __syncthreads_and(ok) != 0;
+}
+
+template <bool EXACT, int P, bool PE>
+__global__ void __maxnreg__(72)
+    k_steps_persistent(uint32_t n_part, int nsys, const SysDesc* __restrict__ sys, SysState* __restrict__ st,
+                       DevArrays a, BatchSource src, LJForce<P, PE, true> f, StepCtl* ctl, int max_steps,
+                       unsigned int nblocks, unsigned long long wait_ns, bool check) {
+  if (check && !grid_barrier(ctl, nblocks + 1u, wait_ns)) return;
+  for (int k = 0; k < max_steps; ++k) {
+    first_half_body<EXACT>(n_part, nsys, sys, st, a, true, true, true, 1.0, 0.5, -1, &ctl->fired[k & 1]);
+    if (!grid_barrier(ctl, nblocks, wait_ns)) return;
+    if (ld_acquire_u32(&ctl->fired[k & 1])) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctl->steps_done = static_cast<unsigned int>(k);
+        ctl->stopped = 1u;
+      }
+      return;
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x)
+      pair::traverse_particle(src, i, f);
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->fired[(k + 1) & 1] = 0u;
+    if (!grid_barrier(ctl, nblocks, wait_ns)) return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->steps_done = static_cast<unsigned int>(max_steps);
+    ctl->stopped = 0u;
+  }
+}
+
+template <bool EXACT, int P, bool PE>
+int persistent_launch(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, StepCtl* ctl,
+                      int max_steps, bool check, cudaStream_t stream) {
+  auto kern = k_steps_persistent<EXACT, P, PE>;
+  constexpr int threads = 128;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  const long long want = (static_cast<long long>(ex.n_part) + threads - 1) / threads;
+  const long long cap = static_cast<long long>(per_sm) * ex.sm_count;
+  const unsigned int grid = static_cast<unsigned int>(std::max(1ll, std::min(want, cap)));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  // a barrier waits at most 4 s in a run (a phase of the largest batches lasts
+  // milliseconds), 20 ms in the timeout check
+  const unsigned long long wait_ns = check ? 20000000ull : 4000000000ull;
+  LJForce<P, PE, true> f{sys, a};
+  cudaLaunchKernelEx(&cfg, kern, ex.n_part, ex.nsys, sys, st, a, BatchSource(sys, st, a, -1), f, ctl, max_steps,
+                     grid, wait_ns, check);
+  return 1;
+}
 }  // namespace
 
 int launch_first_half(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, bool do_push_r,
@@ -489,6 +612,19 @@ int launch_clear_moved(const Extent& ex, SysState* st, cudaStream_t stream) {
   if (ex.nsys == 0) return 0;
   k_clear_moved<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st);
   return 1;
+}
+
+int launch_steps_persistent(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int precision,
+                            bool with_pe, StepCtl* ctl, int max_steps, bool check, cudaStream_t stream) {
+  if (ex.n_part == 0) return 0;
+  if (precision == kFp64Exact)
+    return with_pe ? persistent_launch<true, kFp64Exact, true>(ex, sys, st, a, ctl, max_steps, check, stream)
+                   : persistent_launch<true, kFp64Exact, false>(ex, sys, st, a, ctl, max_steps, check, stream);
+  if (precision == kFp64)
+    return with_pe ? persistent_launch<false, kFp64, true>(ex, sys, st, a, ctl, max_steps, check, stream)
+                   : persistent_launch<false, kFp64, false>(ex, sys, st, a, ctl, max_steps, check, stream);
+  return with_pe ? persistent_launch<false, kMixed, true>(ex, sys, st, a, ctl, max_steps, check, stream)
+                 : persistent_launch<false, kMixed, false>(ex, sys, st, a, ctl, max_steps, check, stream);
 }
 
 }  // namespace xnb

@@ -25,6 +25,7 @@ FORCE_STAGED = 1
 
 STEP_HOST_SYNC = 1
 STEP_ENERGY = 2
+STEP_BARRIER_CHECK = 0x100
 
 ERR_ARG = -1
 ERR_CUDA = -2
@@ -47,7 +48,7 @@ EXPORTED = [
     "xnb_gravitational_force", "xnb_batch_set_tuning", "xnb_autotune", "xnb_snap_create", "xnb_snap_destroy",
     "xnb_snap_force", "xnb_system_pairs_range", "xnb_system_pair_view", "xnb_batch_set_build_form",
     "xnb_graph_is_current", "xnb_batch_set_force_lanes", "xnb_batch_set_force_form",
-    "xnb_batch_set_subcell_pruning",
+    "xnb_batch_set_subcell_pruning", "xnb_step_persistent",
 ]
 
 FORCE_ENERGY = 1
@@ -187,6 +188,7 @@ def load(build_if_missing=True):
     lib.xnb_batch_set_force_lanes.argtypes = [vp, i32]
     lib.xnb_batch_set_force_form.argtypes = [vp, i32]
     lib.xnb_batch_set_subcell_pruning.argtypes = [vp, i32]
+    lib.xnb_step_persistent.argtypes = [vp, i32, i32, i32, vp]
     lib.xnb_system_energy.argtypes = [vp, i32, P(d), P(d), vp]
     lib.xnb_init_particles.argtypes = [vp, i32, i32, vp]
     lib.xnb_push_f_v_r.argtypes = [vp, i32, d, vp]
@@ -393,6 +395,11 @@ class Batch:
 
     def step(self, nsteps=1, precision=PREC_FP64_EXACT, flags=STEP_HOST_SYNC):
         _ck(self.lib.xnb_step(self.h, int(nsteps), int(precision), int(flags), self.stream))
+
+    def step_persistent(self, nsteps=1, precision=PREC_FP64_EXACT, flags=0):
+        """xnb_step_persistent: the same steps as one cooperative launch per run
+        of steps between rebuilds (bitwise the states of step())."""
+        _ck(self.lib.xnb_step_persistent(self.h, int(nsteps), int(precision), int(flags), self.stream))
 
     def graph(self, nsteps, precision=PREC_MIXED, flags=0):
         g = C.c_void_p()

@@ -50,6 +50,10 @@ extern "C" {
 /* xnb_step flags */
 #define XNB_STEP_HOST_SYNC 1 /* read the trigger on the host and skip the rebuild launches when idle */
 #define XNB_STEP_ENERGY 2    /* also write per-particle potential energy */
+/* xnb_step_persistent diagnostic: the loop's first grid barrier waits for one
+ * block more than the launch has, so every wait runs out after 20 ms; the call
+ * returns XNB_ERR_DEVICE and no state changes (tests the barrier's time limit) */
+#define XNB_STEP_BARRIER_CHECK 0x100
 
 /* Error bits of xnb_system_info.error_bits */
 #define XNB_ERRBIT_LIST_OVERFLOW 1u
@@ -175,6 +179,16 @@ int xnb_ghost_update_r(xnb_batch* b, int32_t sys, void* stream);
 /* nsteps of numerical_scheme (numerical-scheme.msp:21-25) for every system of
  * the batch, fused into three kernels per step plus the rebuild path. */
 int xnb_step(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, void* stream);
+/* The same nsteps as a persistent step loop: one cooperative launch advances
+ * every system step after step (first half and trigger, a grid barrier, forces
+ * with the second-half kick, a grid barrier), one thread per particle on full
+ * lists, until a step's trigger fires; that step's rebuild path and forces run
+ * as separate launches (host-synchronised, as XNB_STEP_HOST_SYNC), then the loop
+ * resumes. States are bitwise those of xnb_step. The barriers' waits are bounded
+ * (4 s): a wait that runs out ends the launch and the call returns
+ * XNB_ERR_DEVICE. XNB_PREC_NEWTON is refused. Flags: XNB_STEP_ENERGY,
+ * XNB_STEP_BARRIER_CHECK (XNB_STEP_HOST_SYNC is implied). Synchronises. */
+int xnb_step_persistent(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, void* stream);
 /* Captures nsteps of the fused step (device-side trigger, no host sync) as a CUDA graph. */
 int xnb_step_graph_create(xnb_batch* b, int32_t nsteps, int32_t precision, int32_t flags, void* stream,
                           xnb_graph** out);
