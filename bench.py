@@ -100,7 +100,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--force-block", type=int, default=0, help="threads per block of the force kernel (0: library default)")
     ap.add_argument("--stage-cap", type=int, default=0, help="neighbour-build staging candidates (0: library default)")
-    ap.add_argument("--build-form", default="", choices=["", "rows", "warp"],
+    ap.add_argument("--build-form", default="", choices=["", "rows", "warp", "half"],
                     help="neighbour-build kernel (empty: library default)")
     ap.add_argument("--force-lanes", type=int, default=0, choices=[0, 1, 2, 4],
                     help="threads per particle of the FP64 / mixed force traversal (0: library default)")
@@ -281,7 +281,7 @@ def run_ours(args):
                       stage_cap=args.stage_cap, force_block=args.force_block)
         b.stream = sp
         if args.build_form:
-            b.set_build_form({"rows": xnb.BUILD_ROWS, "warp": xnb.BUILD_WARP}[args.build_form])
+            b.set_build_form({"rows": xnb.BUILD_ROWS, "warp": xnb.BUILD_WARP, "half": xnb.BUILD_HALF}[args.build_form])
         if args.force_lanes:
             b.set_force_lanes(args.force_lanes)
         if args.force_form:

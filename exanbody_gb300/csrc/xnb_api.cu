@@ -1276,8 +1276,16 @@ int xnb_batch_set_force_form(xnb_batch* b, int32_t form) {
 
 int xnb_batch_set_build_form(xnb_batch* b, int32_t form) {
   if (!b) return fail(XNB_ERR_ARG, "null batch");
-  if (form != XNB_BUILD_ROWS && form != XNB_BUILD_WARP) return fail(XNB_ERR_ARG, "unknown neighbour-build form");
-  b->build_form = form == XNB_BUILD_ROWS ? kBuildRows : kBuildWarp;
+  if (form != XNB_BUILD_ROWS && form != XNB_BUILD_WARP && form != XNB_BUILD_HALF)
+    return fail(XNB_ERR_ARG, "unknown neighbour-build form");
+  if (form == XNB_BUILD_HALF && !b->a.nmask) {
+    XCK(cudaSetDevice(b->device));
+    const uint64_t P = static_cast<uint64_t>(b->cfg.particle_capacity);
+    int rc = dalloc(b, &b->a.nmask, 27 * P);
+    if (rc) return rc;
+    b->a.nmask_stride = P;
+  }
+  b->build_form = form == XNB_BUILD_ROWS ? kBuildRows : (form == XNB_BUILD_WARP ? kBuildWarp : kBuildHalf);
   return XNB_OK;
 }
 
@@ -1326,10 +1334,12 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
     *rate = static_cast<double>(atoms) * trial_steps / (static_cast<double>(ms) * 1e-3);
     return xnb_check_errors(b, stream);
   };
+  // the half-shell build is not searched: it allocates 27 x 8 bytes per particle
+  // and measured slower than the lane-per-candidate build
   const int caps[3] = {384, 640, 1024}, blocks[2] = {128, 256}, forms[2] = {XNB_BUILD_ROWS, XNB_BUILD_WARP},
             lanes[3] = {1, 2, 4};
   int best_sc = b->stage_cap, best_fb = b->force_block, best_nw = 0, best_fl = b->force_lanes;
-  int best_bf = b->build_form == kBuildRows ? XNB_BUILD_ROWS : XNB_BUILD_WARP;
+  int best_bf = b->build_form;  // kBuild* and XNB_BUILD_* share their values
   // the batch's force form is kept: the staged form allocates 2 bytes per list
   // entry when switched on, and it measured slower than the one-thread
   // traversal at every size tried

@@ -652,7 +652,7 @@ __global__ void __launch_bounds__(128, 8)
 // (both then take the reference's FP64 decision, as in k_neighbors).
 __global__ void __launch_bounds__(128)
     k_neighbors_warp(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap, int lbuf,
-                     bool prune) {
+                     bool prune, bool half_form) {
   if (*a.any_rebuild == 0) return;
   extern __shared__ float4 stage_w[];
   const uint32_t lane = threadIdx.x & 31;
@@ -668,6 +668,7 @@ __global__ void __launch_bounds__(128)
   for (uint32_t c = blockIdx.x * nwarp + wib; c < n_cells; c += nw_all) {
     const uint32_t s = a.cell_sys[c];
     if (s == kInvalid || !sys_flagged(st, s)) continue;
+    if (half_form && !st[s].half_bad) continue;  // built by the half-shell kernels
     const uint32_t na = a.cell_n[c];
     if (na == 0) continue;
     if (prune && a.cside[c] >= 2 && st[s].keys_fresh) {
@@ -835,6 +836,7 @@ __global__ void k_nbr_reset(int nsys, SysState* st, const unsigned int* any, uns
   st[s].max_nbr = 0;
   st[s].lists_fresh = 1;  // the build that follows reads the current positions
   st[s].compact_bad = 0;
+  st[s].half_bad = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1001,14 +1003,18 @@ int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const D
   const long long want_w = (static_cast<long long>(ex.n_cells) + 3) / 4;
   const int grid_w = static_cast<int>(std::max(1ll, std::min(want_w, static_cast<long long>(per_sm) * ex.sm_count)));
   k_nbr_reset<<<(ex.nsys + 127) / 128, 128, 0, stream>>>(ex.nsys, st, a.any_rebuild, a.nbr_wide_n, a.nbr_sub_n);
+  // half-shell form: masks first; systems it cannot take go through the warp-per-cell build
+  const bool half = form == kBuildHalf && a.nmask != nullptr;
+  const int nh = half ? launch_neighbors_half_test(ex, sys, st, a, stream) : 0;
   if (form == kBuildRows) launch_neighbors_rows(ex, sys, st, a, stream, prune);
-  else k_neighbors_warp<<<grid_w, 128, smem_w, stream>>>(ex.n_cells, sys, st, a, cap, lbuf_w, prune);
+  else k_neighbors_warp<<<grid_w, 128, smem_w, stream>>>(ex.n_cells, sys, st, a, cap, lbuf_w, prune, half);
+  const int ne = half ? launch_neighbors_half_emit(ex, sys, st, a, stream) : 0;
   // dense cells (sub-grid side >= 2), before the block-per-cell build, which takes the ones it passes on
   const int nsub = prune ? launch_neighbors_sub(ex, sys, st, a, cap, stream) : 0;
   k_neighbors<<<warp_grid(ex.n_cells, 1, ex.sm_count), 128, smem, stream>>>(ex.n_cells, sys, st, a, cap, lbuf);
   // compact entries for the staged force traversal
   const int nc = ex.force_form == kForceStaged ? launch_compact_lists(ex, sys, st, a, stream) : 0;
-  return 3 + nsub + nc;
+  return 3 + nh + ne + nsub + nc;
 }
 
 }  // namespace xnb

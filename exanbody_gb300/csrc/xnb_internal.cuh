@@ -96,6 +96,7 @@ struct SysState {
   uint32_t lists_fresh;          // 1 from a neighbour build until positions next change
   uint32_t compact_bad;          // the last build's lists could not be compacted (staged force traversal)
   uint32_t keys_fresh;           // 1 from a rebin until positions next change: the sub-cell keys fit them
+  uint32_t half_bad;             // the half-shell build met a cell of more than 64 particles (this build)
   unsigned long long rebuilds;
 };
 
@@ -140,6 +141,8 @@ struct DevArrays {
   unsigned int* nbr_sub_n;         // number of them (reset by each build)
   uint16_t* skey;                  // sub-cell key of each particle of a cell with side >= 2 (k_rebin_finalize)
   uint8_t* cside;                  // sub-grid side of each cell at the last rebin (1: no sub-grid)
+  uint64_t* nmask;                 // half-shell build: per group g, per particle, its bits of cell g's particles
+  uint64_t nmask_stride;           // particles per group plane of nmask (the particle capacity)
   // scan scratch
   unsigned long long* scan_blocks;
 };

@@ -95,11 +95,18 @@ int launch_backup(const Extent& ex, const SysDesc* sys, SysState* st, const DevA
 // set by the rebin, cleared when positions are pushed).
 constexpr int kBuildRows = 0;
 constexpr int kBuildWarp = 1;
+constexpr int kBuildHalf = 2;
 int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int stage_cap,
                      int lbuf, cudaStream_t stream, int form = kBuildRows, bool prune = false);
 // the lane-per-particle build alone (cells it cannot take are appended to a.nbr_wide)
 int launch_neighbors_rows(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, cudaStream_t stream,
                           bool prune);
+// the half-shell build (xnb_build_half.cu): pair masks of the systems whose
+// cells all hold at most 64 particles, then the lists from the masks
+int launch_neighbors_half_test(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a,
+                               cudaStream_t stream);
+int launch_neighbors_half_emit(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a,
+                               cudaStream_t stream);
 // the sub-cell pruned build of the cells listed in a.nbr_sub (cells with a
 // neighbour of sub-grid side above 3 are passed on to a.nbr_wide)
 int launch_neighbors_sub(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, int stage_cap,

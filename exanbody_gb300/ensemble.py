@@ -24,7 +24,7 @@ import numpy as np
 from . import replicas, workloads, xnb
 
 DEFAULTS = dict(build_form="warp", stage_cap=640, force_block=128, force_lanes=1, skin=0.3, newton=False)
-FORMS = {"warp": xnb.BUILD_WARP, "rows": xnb.BUILD_ROWS}
+FORMS = {"warp": xnb.BUILD_WARP, "rows": xnb.BUILD_ROWS, "half": xnb.BUILD_HALF}
 
 
 def make_systems(specs, rcut=2.5, skin=0.3):

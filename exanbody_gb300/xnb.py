@@ -20,6 +20,7 @@ PRECISIONS = {"fp64_exact": PREC_FP64_EXACT, "fp64": PREC_FP64, "mixed": PREC_MI
 
 BUILD_ROWS = 0
 BUILD_WARP = 1
+BUILD_HALF = 2
 FORCE_THREAD = 0
 FORCE_STAGED = 1
 

@@ -254,6 +254,16 @@ int xnb_batch_set_force_form(xnb_batch* b, int32_t form);
  * stage) are built block-per-cell. */
 #define XNB_BUILD_ROWS 0
 #define XNB_BUILD_WARP 1
+/* XNB_BUILD_HALF: each pair of cells once (a cell and the 13 cells after it in
+ *   (dk, dj, di) order, one warp per cell, lanes over the other cell's
+ *   particles): one distance decision per pair sets a bit in both particles'
+ *   per-cell masks (each direction with its own ghost filter and, near nbh, its
+ *   own FP64 test); a second pass writes each list from its 27 masks. Selecting
+ *   it allocates 27 x 8 bytes per particle of capacity. A system with a cell of
+ *   more than 64 particles is built by XNB_BUILD_WARP instead. Slower than
+ *   XNB_BUILD_WARP on GB300 (10.5 against 3.8 ms per 4M-atom rebuild); not
+ *   searched by xnb_autotune. */
+#define XNB_BUILD_HALF 2
 int xnb_batch_set_build_form(xnb_batch* b, int32_t form);
 
 /* Sub-cell pair pruning of the neighbour build (on by default), after

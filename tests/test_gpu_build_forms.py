@@ -1,17 +1,22 @@
-"""Both neighbour-build kernels give the reference's lists.
+"""Every neighbour-build kernel gives the reference's lists.
 
 XNB_BUILD_ROWS (lane per particle, rows of three cells bulk-copied into shared
-memory; two particles per lane for cells of 33-64) and XNB_BUILD_WARP (lane per
-candidate, the 27-cell block staged per warp) against the oracle: neighbour
-lists as ids in stream order at init and after every rebuild, the same rebuild
-steps, and bitwise state after the run (FP64_EXACT). The systems cover a
-uniform liquid, cells of 33-64 particles, cells above 64 particles or with rows
-over the stage (the block-per-cell build) and the 2-cell periodic wrap."""
+memory; two particles per lane for cells of 33-64), XNB_BUILD_WARP (lane per
+candidate, the 27-cell block staged per warp) and XNB_BUILD_HALF (each pair of
+cells once, per-cell pair masks, lists written from the masks) against the
+oracle: neighbour lists as ids in stream order at init and after every
+rebuild, the same rebuild steps, and bitwise state after the run (FP64_EXACT);
+on the final state the Newton traversal over the lower halves agrees with the
+full lists to 1e-12. The systems cover a uniform liquid, cells of 33-64
+particles, cells above 64 particles or with rows over the stage (the
+block-per-cell build; the half-shell form passes the system to the warp build)
+and the 2-cell periodic wrap (a neighbour cell seen through two images)."""
 import numpy as np
 import pytest
 
 from exanbody_gb300 import workloads, xnb
-from helpers import assert_bitwise_equal, compare_pairs_sliced, ncells, new_batch, oracle_from
+from helpers import (assert_bitwise_equal, compare_pairs_sliced, force_error, forces, ncells, new_batch,
+                     oracle_from)
 
 pytestmark = pytest.mark.gpu
 
@@ -23,7 +28,7 @@ CASES = [
 ]
 
 
-@pytest.mark.parametrize("form", [xnb.BUILD_ROWS, xnb.BUILD_WARP])
+@pytest.mark.parametrize("form", [xnb.BUILD_ROWS, xnb.BUILD_WARP, xnb.BUILD_HALF])
 @pytest.mark.parametrize("n,rho,T,seed,steps", CASES)
 def test_build_form_lists_equal_the_oracle(form, n, rho, T, seed, steps):
     w = workloads.lj_fcc_system(n, rho, T, seed)
@@ -47,5 +52,10 @@ def test_build_form_lists_equal_the_oracle(form, n, rho, T, seed, steps):
     if n == 10:
         # the two-particles-per-lane path ran: some cell held 33..64 particles
         assert any(32 < m <= 64 for m in occupancy), occupancy
+    b.lennard_jones_force(s, xnb.PREC_FP64, False)
+    full = forces(b.download(s))
+    b.lennard_jones_force(s, xnb.PREC_FP64 | xnb.PREC_NEWTON, False)
+    e, _ = force_error(forces(b.download(s)), full)
+    assert e <= 1e-12, e
     b.check_errors()
     b.close()
