@@ -316,8 +316,16 @@ SysDesc make_desc(const xnb_lj_params& p) {
   // ghost filter compare: coordinate error 2 (X + P) u, bound conversion (X + nbh) u
   d.filter_margin_f = static_cast<float>(4.0 * (2.0 * (X + P) + X + nbh) * u * 1.01);
   //  force cutoff test of the mixed path: each FP32 axis difference is within
-  //  2u|d| of the FP64 one (converted, or compensated hi/lo), so
-  //  |r2_f32 - d2_f64| <= 6 u d2; margin = 4x at rc^2 (+1 absolute guard so tiny d2 also go to FP64).
+  //  2u|d| + delta of the FP64 one (converted, or compensated hi/lo with the
+  //  residuals packed to lo_step: delta = 2 lo_step), so
+  //  |r2_f32 - d2_f64| <= 6 u d2 + 2 sqrt(3) |d| delta + 3 delta^2; margin = 4x
+  //  at rc^2 (+1 absolute guard so tiny d2 also go to FP64).
+  {
+    int e = 0;
+    std::frexp(X, &e);  // X = m 2^e, m in [0.5, 1): ulp_32(X) = 2^(e - 24)
+    d.lo_step_f = std::ldexp(1.0f, e - 34);
+    d.lo_inv_f = std::ldexp(1.0f, 34 - e);
+  }
   // FP32 cell index of the rebin: the mirror pf = fl32(x - origin) and
   // fl32(1/cell_size) put pf * inv within 3.01 u |q| of the quotient q of the
   // reference's division (|q| <= max dims + 2 before wrapping); a fraction farther
@@ -328,7 +336,11 @@ SysDesc make_desc(const xnb_lj_params& p) {
   d.q_margin_f = static_cast<float>(4.0 * u * (dmax + 2.0));
   d.inv_cell = 1.0 / p.cell_size;
   d.rc2_f = static_cast<float>(d.rcut2);
-  d.rc_margin_f = static_cast<float>(4.0 * 6.0 * u * (d.rcut2 + 1.0));
+  {
+    const double delta = 2.0 * static_cast<double>(d.lo_step_f);
+    d.rc_margin_f = static_cast<float>(
+        4.0 * (6.0 * u * (d.rcut2 + 1.0) + 2.0 * std::sqrt(3.0) * p.rcut * delta + 3.0 * delta * delta));
+  }
   return d;
 }
 

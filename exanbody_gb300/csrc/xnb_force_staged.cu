@@ -37,7 +37,7 @@ constexpr int kStagedThreads = 160;
 
 struct StagedSmem {
   double x[kStageCap], y[kStageCap], z[kStageCap];
-  float4 hi[kStageCap], lo[kStageCap];
+  float4 hi[kStageCap];  // FP32 mirrors, residuals packed in .w
   uint32_t slot_start[kSlots];
   uint32_t slot_base[kSlots + 1];
   uint32_t slot_code[kSlots];
@@ -220,7 +220,6 @@ __global__ void __launch_bounds__(kStagedThreads, 2)
         sm.y[u] = __ldg(a.ry + j);
         sm.z[u] = __ldg(a.rz + j);
         sm.hi[u] = __ldg(a.pf + j);
-        sm.lo[u] = __ldg(a.pflo + j);
       }
     }
     __syncthreads();
@@ -234,7 +233,7 @@ __global__ void __launch_bounds__(kStagedThreads, 2)
         continue;
       }
       pair::ParticleContext c;
-      if (!src.begin(i, false, true, c)) continue;
+      if (!src.begin(i, false, false, c)) continue;
       typename LJForce<kMixed, PE, KICK>::Acc q;
       f.start(q, c);
       const uint32_t m = a.pcell[i] - seg.x;  // the particle's cell within the segment
@@ -255,11 +254,11 @@ __global__ void __launch_bounds__(kStagedThreads, 2)
           const uint32_t s1 = (e1 >> 11) / 3u * kSlotRow + m + (e1 >> 11) % 3u;
           const uint32_t u0 = sm.slot_base[s0] + (e0 & 2047u), u1 = sm.slot_base[s1] + (e1 & 2047u);
           const uint32_t code0 = sm.slot_code[s0], code1 = sm.slot_code[s1];
-          mixed_pair<PE>(S, code0, sm.x[u0], sm.y[u0], sm.z[u0], sm.hi[u0], sm.lo[u0], c.x, c.y, c.z, c.hi, c.lo,
-                         S.rcut2, q.fx, q.fy, q.fz, q.psum, q.pe);
+          mixed_pair<PE>(S, code0, sm.x[u0], sm.y[u0], sm.z[u0], sm.hi[u0], c.x, c.y, c.z, c.hi, S.rcut2, q.fx, q.fy,
+                         q.fz, q.psum, q.pe);
           if (h1)
-            mixed_pair<PE>(S, code1, sm.x[u1], sm.y[u1], sm.z[u1], sm.hi[u1], sm.lo[u1], c.x, c.y, c.z, c.hi, c.lo,
-                           S.rcut2, q.fx, q.fy, q.fz, q.psum, q.pe);
+            mixed_pair<PE>(S, code1, sm.x[u1], sm.y[u1], sm.z[u1], sm.hi[u1], c.x, c.y, c.z, c.hi, S.rcut2, q.fx,
+                           q.fy, q.fz, q.psum, q.pe);
           h0 = h1 && pair::next_mark(mk, b0);
         }
       }

@@ -69,6 +69,7 @@ struct SysDesc {
   // reaches max_displ2, below trig_lo_f only when it does not
   float trig_lo_f, trig_hi_f;
   float sub_reach_f;             // nbh_dist / cell_size widened by 1e-5: reach of the sub-cell box test (cells)
+  float lo_step_f, lo_inv_f;     // quantum of the residual packed in DevArrays::pf.w (ulp(X)/1024) and its inverse
   double inv_cell;               // fl(1/cell_size): reciprocal pre-decision of the backup encoding
   double m24eps, eps4, sig2, eps24;  // -24*eps, 4*eps (lennard_jones.cu:54-55), sigma^2, 24*eps
   int32_t dims[3];
@@ -103,7 +104,8 @@ struct SysState {
 // All device arrays of a batch (pointers into HBM).
 struct DevArrays {
   double *rx, *ry, *rz, *vx, *vy, *vz, *fx, *fy, *fz, *pe;
-  float4* pf;                      // FP32 hi part of (x - origin, y - origin, z - origin), refreshed with r
+  float4* pf;                      // FP32 hi part of (x - origin, y - origin, z - origin), refreshed with r;
+                                   // .w packs the three residuals as 10-bit multiples of lo_step_f (lo_field)
   float4* pflo;                    // FP32 residual (x - origin) - hi, so hi + lo carries ~48 bits
   unsigned int* any_rebuild;       // number of systems flagged for the rebuild path this step
   uint64_t* id;
@@ -209,9 +211,27 @@ __device__ __forceinline__ float narrow_f64(double x) {
 }
 __device__ __forceinline__ double widen_f32(float f);
 
-// FP32 position relative to the system origin, as stored in DevArrays::pf, and
-// its residual (DevArrays::pflo): hi = fl32(x - o), lo = fl32((x - o) - hi).
-// Only the two subtractions per coordinate use the FP64 pipe.
+// The residual of each axis, packed into the fourth word of the mirror: a
+// signed 10-bit multiple of lo_step_f = ulp(X) / 1024, where X bounds
+// |x - origin| for every particle of the system (the residual is at most
+// ulp(X) / 2: the multiple fits [-512, 512] and is clamped to [-511, 511], so
+// the packed residual is within lo_step_f of the FP32 one). Rounded to nearest
+// by the 1.5 * 2^23 addition (|lo * inv| <= 512); lo * inv is exact (inv a power
+// of two).
+__device__ __forceinline__ uint32_t lo_code(float lo, float inv) {
+  int q = __float_as_int(fmaf(lo, inv, 12582912.0f)) - 0x4B400000;
+  q = max(-511, min(511, q));
+  return static_cast<uint32_t>(q) & 1023u;
+}
+// signed 10-bit field k (0: x, 1: y, 2: z) of a packed residual word
+__device__ __forceinline__ int lo_field(uint32_t w, int k) { return static_cast<int>(w << (22 - 10 * k)) >> 22; }
+// small integer |d| < 2^22 to FP32 on the FP32 pipe (exact)
+__device__ __forceinline__ float small_int_f(int d) { return __int_as_float(0x4B400000 + d) - 12582912.0f; }
+
+// FP32 position relative to the system origin, as stored in DevArrays::pf (its
+// residuals packed in .w), and the residual (DevArrays::pflo): hi = fl32(x - o),
+// lo = fl32((x - o) - hi). Only the two subtractions per coordinate use the FP64
+// pipe.
 __device__ __forceinline__ float4 make_pf(const SysDesc& s, double x, double y, double z) {
   if (s.origin_zero) return make_float4(narrow_f64(x), narrow_f64(y), narrow_f64(z), 0.f);
   return make_float4(narrow_f64(x - s.origin[0]), narrow_f64(y - s.origin[1]), narrow_f64(z - s.origin[2]), 0.f);
@@ -226,6 +246,8 @@ __device__ __forceinline__ void make_pf2(const SysDesc& s, double x, double y, d
   hi = make_float4(narrow_f64(rx), narrow_f64(ry), narrow_f64(rz), 0.f);
   lo = make_float4(narrow_f64(rx - widen_f32(hi.x)), narrow_f64(ry - widen_f32(hi.y)), narrow_f64(rz - widen_f32(hi.z)),
                    0.f);
+  hi.w = __uint_as_float(lo_code(lo.x, s.lo_inv_f) | (lo_code(lo.y, s.lo_inv_f) << 10) |
+                         (lo_code(lo.z, s.lo_inv_f) << 20));
 }
 
 __device__ __forceinline__ double widen_f32(float f) {

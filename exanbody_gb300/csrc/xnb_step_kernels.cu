@@ -193,7 +193,6 @@ __global__ void __launch_bounds__(256)
     const double px = S.period[0], py = S.period[1], pz = S.period[2];
     const double rcut2 = S.rcut2;
     const float4 paf = a.pf[i];
-    const float4 pal = (P == kMixed) ? a.pflo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float pre_hi = S.rc2_f + S.pre_margin_f;
     const float pfx = S.period_f[0], pfy = S.period_f[1], pfz = S.period_f[2];
     double fx = 0.0, fy = 0.0, fz = 0.0, pe = 0.0;
@@ -280,10 +279,11 @@ __global__ void __launch_bounds__(256)
       } else {
         float dxf, dyf, dzf;
         if (code == static_cast<uint32_t>(kImageCenter)) {
-          const float4 hb = __ldg(a.pf + j), lb = __ldg(a.pflo + j);
-          dxf = (hb.x - paf.x) + (lb.x - pal.x);
-          dyf = (hb.y - paf.y) + (lb.y - pal.y);
-          dzf = (hb.z - paf.z) + (lb.z - pal.z);
+          const float4 hb = __ldg(a.pf + j);
+          const uint32_t wb = __float_as_uint(hb.w), wa = __float_as_uint(paf.w);
+          dxf = fmaf(small_int_f(lo_field(wb, 0) - lo_field(wa, 0)), S.lo_step_f, hb.x - paf.x);
+          dyf = fmaf(small_int_f(lo_field(wb, 1) - lo_field(wa, 1)), S.lo_step_f, hb.y - paf.y);
+          dzf = fmaf(small_int_f(lo_field(wb, 2) - lo_field(wa, 2)), S.lo_step_f, hb.z - paf.z);
         } else {
           dxf = narrow_f64(__dsub_rn(xb, xa));
           dyf = narrow_f64(__dsub_rn(yb, ya));
