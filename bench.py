@@ -44,7 +44,7 @@ FLOP32_PER_ATOM_MIXED = 387.4
 # DRAM bytes (read + write) per atom of one mixed k_force launch, from an ncu capture of
 # the 256,000-atom case of this workload (FCC 40^3); traffic grows with the atom count at
 # fixed density, so a launch moves this many bytes per atom.
-FORCE_DRAM_BYTES_PER_ATOM = 545.1
+FORCE_DRAM_BYTES_PER_ATOM = 520.0
 
 WORKLOAD = dict(n=100, rho=0.8442, T=1.44, seed=12345, rcut=2.5, skin=0.3, dt=0.005)
 METRIC = "atom-steps/s, 4M-atom LJ MD step (mixed precision; FP64 path and force error reported beside it)"
