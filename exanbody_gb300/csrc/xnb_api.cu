@@ -120,10 +120,12 @@ struct xnb_batch {
     e.n_cells = static_cast<uint32_t>(cells.high_water());
     int hw = 0;
     e.far_coords = 0;
+    e.unpacked = 0;
     for (size_t s = 0; s < sys.size(); ++s)
       if (sys[s].active) {
         hw = static_cast<int>(s) + 1;
         if (sys[s].d.far_coords) e.far_coords = 1;
+        if (!sys[s].d.packed_lo) e.unpacked = 1;
       }
     e.nsys = hw;
     e.sm_count = sm_count;
@@ -325,6 +327,9 @@ SysDesc make_desc(const xnb_lj_params& p) {
     std::frexp(X, &e);  // X = m 2^e, m in [0.5, 1): ulp_32(X) = 2^(e - 24)
     d.lo_step_f = std::ldexp(1.0f, e - 34);
     d.lo_inv_f = std::ldexp(1.0f, 34 - e);
+    // the packed residual's absolute error grows with X: beyond X = 1024 sigma
+    // (lo_step 2^-24) the mixed traversal gathers the FP32 residual mirror instead
+    d.packed_lo = e <= 10 ? 1 : 0;
   }
   // FP32 cell index of the rebin: the mirror pf = fl32(x - origin) and
   // fl32(1/cell_size) put pf * inv within 3.01 u |q| of the quotient q of the
@@ -337,7 +342,7 @@ SysDesc make_desc(const xnb_lj_params& p) {
   d.inv_cell = 1.0 / p.cell_size;
   d.rc2_f = static_cast<float>(d.rcut2);
   {
-    const double delta = 2.0 * static_cast<double>(d.lo_step_f);
+    const double delta = d.packed_lo ? 2.0 * static_cast<double>(d.lo_step_f) : 0.0;
     d.rc_margin_f = static_cast<float>(
         4.0 * (6.0 * u * (d.rcut2 + 1.0) + 2.0 * std::sqrt(3.0) * p.rcut * delta + 3.0 * delta * delta));
   }

@@ -254,11 +254,13 @@ __global__ void __launch_bounds__(kStagedThreads, 2)
           const uint32_t s1 = (e1 >> 11) / 3u * kSlotRow + m + (e1 >> 11) % 3u;
           const uint32_t u0 = sm.slot_base[s0] + (e0 & 2047u), u1 = sm.slot_base[s1] + (e1 & 2047u);
           const uint32_t code0 = sm.slot_code[s0], code1 = sm.slot_code[s1];
-          mixed_pair<PE>(S, code0, sm.x[u0], sm.y[u0], sm.z[u0], sm.hi[u0], c.x, c.y, c.z, c.hi, S.rcut2, q.fx, q.fy,
-                         q.fz, q.psum, q.pe);
+          // packed residuals only: launch_force keeps batches without them off this kernel
+          const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+          mixed_pair<PE, true>(S, code0, sm.x[u0], sm.y[u0], sm.z[u0], sm.hi[u0], z4, c.x, c.y, c.z, c.hi, z4,
+                               S.rcut2, q.fx, q.fy, q.fz, q.psum, q.pe);
           if (h1)
-            mixed_pair<PE>(S, code1, sm.x[u1], sm.y[u1], sm.z[u1], sm.hi[u1], c.x, c.y, c.z, c.hi, S.rcut2, q.fx,
-                           q.fy, q.fz, q.psum, q.pe);
+            mixed_pair<PE, true>(S, code1, sm.x[u1], sm.y[u1], sm.z[u1], sm.hi[u1], z4, c.x, c.y, c.z, c.hi, z4,
+                                 S.rcut2, q.fx, q.fy, q.fz, q.psum, q.pe);
           h0 = h1 && pair::next_mark(mk, b0);
         }
       }

@@ -70,6 +70,7 @@ struct SysDesc {
   float trig_lo_f, trig_hi_f;
   float sub_reach_f;             // nbh_dist / cell_size widened by 1e-5: reach of the sub-cell box test (cells)
   float lo_step_f, lo_inv_f;     // quantum of the residual packed in DevArrays::pf.w (ulp(X)/1024) and its inverse
+  int32_t packed_lo;             // 1: the mixed traversal reads the packed residuals (X < 1024); 0: DevArrays::pflo
   double inv_cell;               // fl(1/cell_size): reciprocal pre-decision of the backup encoding
   double m24eps, eps4, sig2, eps24;  // -24*eps, 4*eps (lennard_jones.cu:54-55), sigma^2, 24*eps
   int32_t dims[3];

@@ -19,6 +19,7 @@ struct Extent {
   int force_block;   // threads per block of the force traversal (multiple of 32, <= 256)
   int force_lanes;   // threads per particle of the FP64 / mixed full-list traversal (1, 2 or 4)
   int far_coords;    // some resident system lies far from the coordinate origin (SysDesc::far_coords)
+  int unpacked;      // some resident system reads the residual mirror, not packed residuals (SysDesc::packed_lo)
   int force_form;    // kForceThread or kForceStaged (mixed full-list traversal)
   uint32_t n_seg;    // cell segments of the staged traversal (DevArrays::seg)
 };

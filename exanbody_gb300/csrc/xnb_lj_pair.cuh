@@ -37,19 +37,29 @@ __device__ __forceinline__ double rcp_nr(double d) {
 // an image entry), the cutoff decided in FP32 outside the proven band and in
 // FP64 inside it, then the FP32 force factor pd and the FP64 accumulation of
 // pd * r_b and pd.
-template <bool PE>
+// PACKED = false (batches holding a system of X >= 1024 sigma, whose packed
+// residuals are too coarse) takes the gathered residual mirrors lb and pal.
+template <bool PE, bool PACKED>
 __device__ __forceinline__ void mixed_pair(const SysDesc& S, uint32_t e, double xb, double yb, double zb, float4 hb,
-                                           double xa, double ya, double za, float4 paf, double rcut2, double& fx,
-                                           double& fy, double& fz, double& psum, double& pe) {
+                                           float4 lb, double xa, double ya, double za, float4 paf, float4 pal,
+                                           double rcut2, double& fx, double& fy, double& fz, double& psum,
+                                           double& pe) {
   const uint32_t code = e & 31u;
   float dxf, dyf, dzf;
   if (code == static_cast<uint32_t>(kImageCenter)) {
-    // within 2u|d| + 2 lo_step of the FP64 displacement (u = 2^-24), without FP64 work
-    const uint32_t wb = __float_as_uint(hb.w), wa = __float_as_uint(paf.w);
-    const float q = S.lo_step_f;
-    dxf = fmaf(small_int_f(lo_field(wb, 0) - lo_field(wa, 0)), q, hb.x - paf.x);
-    dyf = fmaf(small_int_f(lo_field(wb, 1) - lo_field(wa, 1)), q, hb.y - paf.y);
-    dzf = fmaf(small_int_f(lo_field(wb, 2) - lo_field(wa, 2)), q, hb.z - paf.z);
+    if constexpr (PACKED) {
+      // within 2u|d| + 2 lo_step of the FP64 displacement (u = 2^-24), without FP64 work
+      const uint32_t wb = __float_as_uint(hb.w), wa = __float_as_uint(paf.w);
+      const float q = S.lo_step_f;
+      dxf = fmaf(small_int_f(lo_field(wb, 0) - lo_field(wa, 0)), q, hb.x - paf.x);
+      dyf = fmaf(small_int_f(lo_field(wb, 1) - lo_field(wa, 1)), q, hb.y - paf.y);
+      dzf = fmaf(small_int_f(lo_field(wb, 2) - lo_field(wa, 2)), q, hb.z - paf.z);
+    } else {
+      // within 2u|d| of the FP64 displacement
+      dxf = (hb.x - paf.x) + (lb.x - pal.x);
+      dyf = (hb.y - paf.y) + (lb.y - pal.y);
+      dzf = (hb.z - paf.z) + (lb.z - pal.z);
+    }
   } else {
     xb = image_coord(xb, S.period[0], static_cast<int>(code % 3u));
     yb = image_coord(yb, S.period[1], static_cast<int>((code / 3u) % 3u));
@@ -110,7 +120,7 @@ __device__ __forceinline__ void mixed_pair(const SysDesc& S, uint32_t e, double 
 //                    once per particle (sum pd*r_b - r_a*sum pd, all in FP64)
 //                    and the FP32 factor is widened on the integer pipes: a
 //                    pair costs 3 DFMA + 1 DADD on the FP64 pipe.
-template <int P, bool PE, bool KICK>
+template <int P, bool PE, bool KICK, bool PACKED = true>
 struct LJForce {
   const SysDesc* __restrict__ sys;
   DevArrays a;
@@ -159,7 +169,8 @@ struct LJForce {
   }
   __device__ __forceinline__ void entry(Acc& q, const pair::ParticleContext& c, const pair::RawEntry& r) const {
     const SysDesc& S = sys[c.sys];
-    mixed_pair<PE>(S, r.e, r.xb, r.yb, r.zb, r.hb, c.x, c.y, c.z, c.hi, S.rcut2, q.fx, q.fy, q.fz, q.psum, q.pe);
+    mixed_pair<PE, PACKED>(S, r.e, r.xb, r.yb, r.zb, r.hb, r.lb, c.x, c.y, c.z, c.hi, c.lo, S.rcut2, q.fx, q.fy,
+                           q.fz, q.psum, q.pe);
   }
   __device__ __forceinline__ void combine(Acc& q, const Acc& o) const {
     q.fx += o.fx;
@@ -215,13 +226,13 @@ struct LJForce {
 namespace xnb {
 namespace pair {
 // The mixed path takes raw entries (their residuals come packed with the hi
-// mirror, so the residual mirrors are not gathered), two per iteration (both
-// entries' gathers in flight together; list order unchanged); the FP64 paths
-// take the traversal's FP64 pairs within rc.
-template <int P, bool PE, bool KICK>
-struct ComputePairTraits<LJForce<P, PE, KICK>> : DefaultPairTraits {
+// mirror, so the residual mirrors are gathered only without packing), two per
+// iteration (both entries' gathers in flight together; list order unchanged);
+// the FP64 paths take the traversal's FP64 pairs within rc.
+template <int P, bool PE, bool KICK, bool PACKED>
+struct ComputePairTraits<LJForce<P, PE, KICK, PACKED>> : DefaultPairTraits {
   static constexpr bool RawEntries = (P == kMixed);
-  static constexpr bool GatherMirrors = false;
+  static constexpr bool GatherMirrors = (P == kMixed && !PACKED);
   static constexpr int EntriesPerIteration = (P == kMixed) ? 2 : 1;
 };
 }  // namespace pair

@@ -143,8 +143,8 @@ __global__ void __launch_bounds__(256)
 
 // 72 registers: 7 blocks of 128 threads per SM (measured faster than the
 // unconstrained 79 despite a few spilled bytes).
-template <int P, bool PE, bool KICK>
-__global__ void __maxnreg__(72) k_force(uint32_t n_part, BatchSource src, LJForce<P, PE, KICK> f) {
+template <int P, bool PE, bool KICK, bool PACKED = true>
+__global__ void __maxnreg__(72) k_force(uint32_t n_part, BatchSource src, LJForce<P, PE, KICK, PACKED> f) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_part; i += gridDim.x * blockDim.x)
     pair::traverse_particle(src, i, f);
 }
@@ -280,10 +280,17 @@ __global__ void __launch_bounds__(256)
         float dxf, dyf, dzf;
         if (code == static_cast<uint32_t>(kImageCenter)) {
           const float4 hb = __ldg(a.pf + j);
-          const uint32_t wb = __float_as_uint(hb.w), wa = __float_as_uint(paf.w);
-          dxf = fmaf(small_int_f(lo_field(wb, 0) - lo_field(wa, 0)), S.lo_step_f, hb.x - paf.x);
-          dyf = fmaf(small_int_f(lo_field(wb, 1) - lo_field(wa, 1)), S.lo_step_f, hb.y - paf.y);
-          dzf = fmaf(small_int_f(lo_field(wb, 2) - lo_field(wa, 2)), S.lo_step_f, hb.z - paf.z);
+          if (S.packed_lo) {
+            const uint32_t wb = __float_as_uint(hb.w), wa = __float_as_uint(paf.w);
+            dxf = fmaf(small_int_f(lo_field(wb, 0) - lo_field(wa, 0)), S.lo_step_f, hb.x - paf.x);
+            dyf = fmaf(small_int_f(lo_field(wb, 1) - lo_field(wa, 1)), S.lo_step_f, hb.y - paf.y);
+            dzf = fmaf(small_int_f(lo_field(wb, 2) - lo_field(wa, 2)), S.lo_step_f, hb.z - paf.z);
+          } else {
+            const float4 lb = __ldg(a.pflo + j), pal = a.pflo[i];
+            dxf = (hb.x - paf.x) + (lb.x - pal.x);
+            dyf = (hb.y - paf.y) + (lb.y - pal.y);
+            dzf = (hb.z - paf.z) + (lb.z - pal.z);
+          }
         } else {
           dxf = narrow_f64(__dsub_rn(xb, xa));
           dyf = narrow_f64(__dsub_rn(yb, ya));
@@ -420,6 +427,14 @@ void force_dispatch(const Extent& ex, const SysDesc* sys, const SysState* st, co
                     cudaStream_t stream) {
   const int threads = ex.force_block > 0 ? ex.force_block : 128;
   const BatchSource src(sys, st, a, sys_only);
+  if constexpr (P == kMixed) {
+    // a batch holding a box of X >= 1024 sigma: residual mirrors gathered, one thread per particle
+    if (ex.unpacked) {
+      const LJForce<P, PE, KICK, false> fu{sys, a};
+      k_force<P, PE, KICK, false><<<grid_for(ex.n_part, threads), threads, 0, stream>>>(ex.n_part, src, fu);
+      return;
+    }
+  }
   const LJForce<P, PE, KICK> f{sys, a};
   // the bit-exact path keeps one thread per particle (the reference's summation order)
   if constexpr (P != kFp64Exact) {
@@ -488,10 +503,10 @@ __device__ bool grid_barrier(StepCtl* ctl, unsigned int nblocks, unsigned long l
   return __syncthreads_and(ok) != 0;
 }
 
-template <bool EXACT, int P, bool PE>
+template <bool EXACT, int P, bool PE, bool PACKED = true>
 __global__ void __maxnreg__(72)
     k_steps_persistent(uint32_t n_part, int nsys, const SysDesc* __restrict__ sys, SysState* __restrict__ st,
-                       DevArrays a, BatchSource src, LJForce<P, PE, true> f, StepCtl* ctl, int max_steps,
+                       DevArrays a, BatchSource src, LJForce<P, PE, true, PACKED> f, StepCtl* ctl, int max_steps,
                        unsigned int nblocks, unsigned long long wait_ns, bool check) {
   if (check && !grid_barrier(ctl, nblocks + 1u, wait_ns)) return;
   for (int k = 0; k < max_steps; ++k) {
@@ -515,10 +530,10 @@ __global__ void __maxnreg__(72)
   }
 }
 
-template <bool EXACT, int P, bool PE>
+template <bool EXACT, int P, bool PE, bool PACKED = true>
 int persistent_launch(const Extent& ex, const SysDesc* sys, SysState* st, const DevArrays& a, StepCtl* ctl,
                       int max_steps, bool check, cudaStream_t stream) {
-  auto kern = k_steps_persistent<EXACT, P, PE>;
+  auto kern = k_steps_persistent<EXACT, P, PE, PACKED>;
   constexpr int threads = 128;
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0) != cudaSuccess || per_sm < 1)
@@ -539,7 +554,7 @@ int persistent_launch(const Extent& ex, const SysDesc* sys, SysState* st, const 
   // a barrier waits at most 4 s in a run (a phase of the largest batches lasts
   // milliseconds), 20 ms in the timeout check
   const unsigned long long wait_ns = check ? 20000000ull : 4000000000ull;
-  LJForce<P, PE, true> f{sys, a};
+  LJForce<P, PE, true, PACKED> f{sys, a};
   cudaLaunchKernelEx(&cfg, kern, ex.n_part, ex.nsys, sys, st, a, BatchSource(sys, st, a, -1), f, ctl, max_steps,
                      grid, wait_ns, check);
   return 1;
@@ -583,7 +598,7 @@ int launch_force(const Extent& ex, const SysDesc* sys, SysState* st, const DevAr
     k_force_finish<<<g, threads, 0, stream>>>(ex.n_part, sys, st, a, sys_only, second_half);
     return 3;
   }
-  if (precision == kMixed && ex.force_form == kForceStaged && a.nbr16 && a.seg)
+  if (precision == kMixed && ex.force_form == kForceStaged && a.nbr16 && a.seg && !ex.unpacked)
     return launch_force_staged(ex, sys, st, a, with_pe, second_half, sys_only, stream);
 #define XNB_FORCE_CASE(PP)                                                           \
   if (precision == PP) {                                                             \
@@ -623,6 +638,9 @@ int launch_steps_persistent(const Extent& ex, const SysDesc* sys, SysState* st, 
   if (precision == kFp64)
     return with_pe ? persistent_launch<false, kFp64, true>(ex, sys, st, a, ctl, max_steps, check, stream)
                    : persistent_launch<false, kFp64, false>(ex, sys, st, a, ctl, max_steps, check, stream);
+  if (ex.unpacked)
+    return with_pe ? persistent_launch<false, kMixed, true, false>(ex, sys, st, a, ctl, max_steps, check, stream)
+                   : persistent_launch<false, kMixed, false, false>(ex, sys, st, a, ctl, max_steps, check, stream);
   return with_pe ? persistent_launch<false, kMixed, true>(ex, sys, st, a, ctl, max_steps, check, stream)
                  : persistent_launch<false, kMixed, false>(ex, sys, st, a, ctl, max_steps, check, stream);
 }
