@@ -78,32 +78,32 @@ static __device__ __noinline__ bool exact_neighbor_test(const SysDesc& S, const 
 
 // Lane-per-candidate chunk test shared by the warp-per-cell build
 // (xnb_build_kernels.cu) and the sub-cell pruned build (xnb_build_sub.cu):
-// lanes hold 32 staged candidates, kNbrP particles are tested against them, and
+// lanes hold 32 staged candidates, NP particles are tested against them, and
 // a ballot per particle appends its hits in candidate order to sbuf[k * lbuf + ...]
 // (an entry past lbuf - 1 lands on the last word). t0 and low0 are positions in
 // the candidate sequence: the particles' own entries sit at low0 + k.
 constexpr int kNbrP = 4;  // particles tested per staged candidate load (even: FP32x2 pairs)
 
-template <bool AMB, bool SELF>
-__device__ __forceinline__ void nbr_chunk(const SysDesc& S, const DevArrays& a, const float4 b, const float (&px)[kNbrP],
-                                          const float (&py)[kNbrP], const float (&pz)[kNbrP], uint32_t i0,
+template <int NP, bool AMB, bool SELF>
+__device__ __forceinline__ void nbr_chunk(const SysDesc& S, const DevArrays& a, const float4 b, const float (&px)[NP],
+                                          const float (&py)[NP], const float (&pz)[NP], uint32_t i0,
                                           uint32_t self0, uint32_t t0, uint32_t low0, float nb_lo, float nb_hi,
                                           float nb_zero, unsigned lt, uint32_t* sbuf, uint32_t lbuf,
-                                          uint32_t (&cur)[kNbrP], uint32_t (&half)[kNbrP]) {
+                                          uint32_t (&cur)[NP], uint32_t (&half)[NP]) {
   const uint32_t ent = __float_as_uint(b.w);
   const bool amb = AMB && (ent & kAmbiguousBit) != 0;
-  bool hit[kNbrP], may[kNbrP];
+  bool hit[NP], may[NP];
   bool any_may = false;
   // squared FP32 distances two particles at a time on the packed FP32x2 path:
   // per particle the roundings of fmaf(dx, dx, fmaf(dy, dy, dz * dz)) exactly
-  float dd[kNbrP];
+  float dd[NP];
   {
     unsigned long long bx2, by2, bz2;
     asm("mov.b64 %0, {%1, %1};" : "=l"(bx2) : "f"(b.x));
     asm("mov.b64 %0, {%1, %1};" : "=l"(by2) : "f"(b.y));
     asm("mov.b64 %0, {%1, %1};" : "=l"(bz2) : "f"(b.z));
 #pragma unroll
-    for (int k = 0; k < kNbrP; k += 2) {
+    for (int k = 0; k < NP; k += 2) {
       unsigned long long x2, y2, z2, dx, dy, dz, d;
       asm("mov.b64 %0, {%1, %2};" : "=l"(x2) : "f"(px[k]), "f"(px[k + 1]));
       asm("mov.b64 %0, {%1, %2};" : "=l"(y2) : "f"(py[k]), "f"(py[k + 1]));
@@ -118,7 +118,7 @@ __device__ __forceinline__ void nbr_chunk(const SysDesc& S, const DevArrays& a, 
     }
   }
 #pragma unroll
-  for (int k = 0; k < kNbrP; ++k) {
+  for (int k = 0; k < NP; ++k) {
     const float d = dd[k];
     hit[k] = d < nb_lo && d > nb_zero && !amb;
     // the particle's own entry only sits in a SELF chunk (d = 0 there: no hit)
@@ -127,12 +127,12 @@ __device__ __forceinline__ void nbr_chunk(const SysDesc& S, const DevArrays& a, 
   }
   if (__any_sync(0xffffffffu, any_may)) {
 #pragma unroll
-    for (int k = 0; k < kNbrP; ++k)
+    for (int k = 0; k < NP; ++k)
       if (may[k]) hit[k] = exact_neighbor_test(S, a, i0 + k, ent);
   }
   const uint32_t e = AMB ? (ent & ~kAmbiguousBit) : ent;
 #pragma unroll
-  for (int k = 0; k < kNbrP; ++k) {
+  for (int k = 0; k < NP; ++k) {
     const unsigned m = __ballot_sync(0xffffffffu, hit[k]);
     // entries past the slot land in the buffer's last word, which is never written out
     if (hit[k]) sbuf[k * lbuf + min(cur[k] + __popc(m & lt), lbuf - 1u)] = e;

@@ -650,6 +650,8 @@ __global__ void __launch_bounds__(128, 8)
 // warp-uniform branches: a chunk holding a candidate whose ghost filter is
 // undecided in FP32, and an FP32 distance inside the error band around nbh^2
 // (both then take the reference's FP64 decision, as in k_neighbors).
+constexpr int kWarpP = 8;  // particles tested per staged candidate load in the warp-per-cell build
+
 __global__ void __launch_bounds__(128)
     k_neighbors_warp(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap, int lbuf,
                      bool prune, bool half_form) {
@@ -659,8 +661,6 @@ __global__ void __launch_bounds__(128)
   const uint32_t wib = threadIdx.x >> 5;
   const uint32_t nwarp = blockDim.x >> 5;
   float4* srel = stage_w + static_cast<size_t>(wib) * cap;
-  uint32_t* sbuf = reinterpret_cast<uint32_t*>(stage_w + static_cast<size_t>(nwarp) * cap) +
-                   static_cast<size_t>(wib) * kNbrP * lbuf;
   const unsigned lt = lanemask_lt();
   uint32_t acc_s = kInvalid, acc_max = 0;
   unsigned long long acc_sum = 0;
@@ -705,7 +705,7 @@ __global__ void __launch_bounds__(128)
     const uint32_t ncand = __shfl_sync(0xffffffffu, g_off, 26);
     g_off -= g_n;
     const uint32_t slot = S.list_slot;
-    if (ncand > static_cast<uint32_t>(cap) || slot >= static_cast<uint32_t>(lbuf)) {
+    if (ncand > static_cast<uint32_t>(cap)) {
       if (lane == 0) a.nbr_wide[atomicAdd(a.nbr_wide_n, 1u)] = c;
       continue;
     }
@@ -754,13 +754,13 @@ __global__ void __launch_bounds__(128)
     const float nb_lo = S.nbh2_f - S.nbh_margin_f;
     const float nb_zero = S.nbh_margin_f;
     uint32_t* const seg = a.nbr + S.list_base;
-    for (uint32_t p0 = 0; p0 < na; p0 += kNbrP) {
+    for (uint32_t p0 = 0; p0 < na; p0 += kWarpP) {
       // particles past the cell's end sit at -1e18: never within reach of a
       // candidate (real ones, or the +1e18 dummies), so they need no test
-      float px[kNbrP], py[kNbrP], pz[kNbrP];
-      uint32_t cur[kNbrP], half[kNbrP];
+      float px[kWarpP], py[kWarpP], pz[kWarpP];
+      uint32_t cur[kWarpP], half[kWarpP];
 #pragma unroll
-      for (int k = 0; k < kNbrP; ++k) {
+      for (int k = 0; k < kWarpP; ++k) {
         const uint32_t pk = p0 + k;
         float4 q;
         if (na <= 32) {
@@ -780,43 +780,43 @@ __global__ void __launch_bounds__(128)
       const uint32_t i0 = sa + p0;
       const uint32_t self0 = ((i0 - S.part_base) << 5) | static_cast<uint32_t>(kImageCenter);
       const uint32_t low0 = off_self + p0;
+      // hits go straight to the particles' slots (consecutive particles, stride slot)
+      uint32_t* const pslot = seg + static_cast<size_t>(i0 - S.part_base) * slot;
       for (uint32_t t0 = 0; t0 < mpad; t0 += 32) {
         const float4 b = srel[t0 + lane];
         const uint32_t ent = __float_as_uint(b.w);
-        const uint32_t lb = static_cast<uint32_t>(lbuf);
         // the particles' own entries (lower-half ends) sit at stage indices low0 + k
-        const bool self_chunk = t0 < low0 + kNbrP && low0 < t0 + 32u;
+        const bool self_chunk = t0 < low0 + kWarpP && low0 < t0 + 32u;
         // entries in [kAmbiguousBit, kInvalid): ghost filter undecided in FP32
         if (__any_sync(0xffffffffu, ent - kAmbiguousBit < kInvalid - kAmbiguousBit)) {
           if (self_chunk)
-            nbr_chunk<true, true>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, sbuf, lb, cur, half);
+            nbr_chunk<kWarpP, true, true>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, pslot,
+                                          slot, cur, half);
           else
-            nbr_chunk<true, false>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, sbuf, lb, cur, half);
+            nbr_chunk<kWarpP, true, false>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, pslot,
+                                           slot, cur, half);
         } else if (self_chunk) {
-          nbr_chunk<false, true>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, sbuf, lb, cur, half);
+          nbr_chunk<kWarpP, false, true>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, pslot,
+                                         slot, cur, half);
         } else {
-          nbr_chunk<false, false>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, sbuf, lb, cur, half);
+          nbr_chunk<kWarpP, false, false>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, pslot,
+                                          slot, cur, half);
         }
       }
-      __syncwarp();
 #pragma unroll
-      for (int k = 0; k < kNbrP; ++k) {
+      for (int k = 0; k < kWarpP; ++k) {
         const uint32_t pk = p0 + k;
         if (pk < na) {
           const uint32_t i = sa + pk;
-          const uint32_t base = (i - S.part_base) * slot;  // the host keeps npart * slot below 2^32
-          const uint32_t nw = min(cur[k], slot);
-          for (uint32_t q = lane; q < nw; q += 32) seg[base + q] = sbuf[k * lbuf + q];
           if (lane == 0) {
             a.nbr_cnt[i] = cur[k];
             a.nbr_half[i] = half[k];
-            a.nbr_start[i] = base;
+            a.nbr_start[i] = (i - S.part_base) * slot;  // the host keeps npart * slot below 2^32
           }
           acc_max = max(acc_max, cur[k]);
           acc_sum += cur[k];
         }
       }
-      __syncwarp();
     }
   }
   if (lane == 0) flush_list_stats(st, sys, acc_s, acc_max, acc_sum);
@@ -993,7 +993,7 @@ int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const D
   // warp-per-cell buffers: one slot of each of kNbrP particles plus a spill word
   // (lbuf_w > slot); slots above 512 entries leave every cell to k_neighbors
   const int lbuf_w = (lbuf > 0 && lbuf <= 512) ? lbuf + 32 : 32;
-  const size_t smem_w = 4 * (static_cast<size_t>(cap) * sizeof(float4) + static_cast<size_t>(kNbrP) * lbuf_w * 4);
+  const size_t smem_w = 4 * static_cast<size_t>(cap) * sizeof(float4);
   // per-device attributes: set them on the current device every time (host calls, no GPU work)
   cudaFuncSetAttribute(k_neighbors, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
   cudaFuncSetAttribute(k_neighbors_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);

@@ -250,16 +250,16 @@ __global__ void __launch_bounds__(128)
             const bool self_chunk = u0 < low0 + kNbrP && low0 < u0 + 32u;
             if (__any_sync(full, ent - kAmbiguousBit < kInvalid - kAmbiguousBit)) {
               if (self_chunk)
-                nbr_chunk<true, true>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, slot,
+                nbr_chunk<kNbrP, true, true>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, slot,
                                       cur, half);
               else
-                nbr_chunk<true, false>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, slot,
+                nbr_chunk<kNbrP, true, false>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, slot,
                                        cur, half);
             } else if (self_chunk) {
-              nbr_chunk<false, true>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, slot,
+              nbr_chunk<kNbrP, false, true>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, slot,
                                      cur, half);
             } else {
-              nbr_chunk<false, false>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, slot,
+              nbr_chunk<kNbrP, false, false>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, slot,
                                       cur, half);
             }
           }
