@@ -641,19 +641,19 @@ __global__ void __launch_bounds__(128, 8)
 
 // ---------------------------------------------------------------------------
 // Warp-per-cell form of the same build, for every cell whose candidates fit the
-// warp's stage (cap) and whose system's slot fits its list buffers (lbuf > slot);
-// the others are appended to a.nbr_wide for k_neighbors. Each warp stages its
-// cell's candidates itself (no block barrier), then tests kNbrP particles per
-// staged load: lanes hold 32 candidates, a ballot per particle keeps its hits in
-// order, and the hits gather in the particle's shared-memory buffer, written out
-// in full lines once its pass ends. Two rare cases leave the fast test through
+// warp's stage (cap); the others are appended to a.nbr_wide for k_neighbors.
+// Each warp stages its cell's candidates itself (no block barrier), then tests
+// kWarpP particles per staged load: lanes hold 32 candidates, and a ballot per
+// particle appends its hits in order straight to the particle's list slot
+// (an entry past the slot lands on its last word; the count flags the
+// overflow). Two rare cases leave the fast test through
 // warp-uniform branches: a chunk holding a candidate whose ghost filter is
 // undecided in FP32, and an FP32 distance inside the error band around nbh^2
 // (both then take the reference's FP64 decision, as in k_neighbors).
 constexpr int kWarpP = 8;  // particles tested per staged candidate load in the warp-per-cell build
 
 __global__ void __launch_bounds__(128)
-    k_neighbors_warp(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap, int lbuf,
+    k_neighbors_warp(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap,
                      bool prune, bool half_form) {
   if (*a.any_rebuild == 0) return;
   extern __shared__ float4 stage_w[];
@@ -990,9 +990,7 @@ int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const D
                      cudaStream_t stream, int form, bool prune) {
   if (ex.n_cells == 0) return 0;
   const size_t smem = static_cast<size_t>(cap) * sizeof(float4) + static_cast<size_t>(4) * 2 * lbuf * sizeof(uint32_t);
-  // warp-per-cell buffers: one slot of each of kNbrP particles plus a spill word
-  // (lbuf_w > slot); slots above 512 entries leave every cell to k_neighbors
-  const int lbuf_w = (lbuf > 0 && lbuf <= 512) ? lbuf + 32 : 32;
+  // warp-per-cell form: the stage alone (hits go straight to the slots)
   const size_t smem_w = 4 * static_cast<size_t>(cap) * sizeof(float4);
   // per-device attributes: set them on the current device every time (host calls, no GPU work)
   cudaFuncSetAttribute(k_neighbors, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
@@ -1007,7 +1005,7 @@ int launch_neighbors(const Extent& ex, const SysDesc* sys, SysState* st, const D
   const bool half = form == kBuildHalf && a.nmask != nullptr;
   const int nh = half ? launch_neighbors_half_test(ex, sys, st, a, stream) : 0;
   if (form == kBuildRows) launch_neighbors_rows(ex, sys, st, a, stream, prune);
-  else k_neighbors_warp<<<grid_w, 128, smem_w, stream>>>(ex.n_cells, sys, st, a, cap, lbuf_w, prune, half);
+  else k_neighbors_warp<<<grid_w, 128, smem_w, stream>>>(ex.n_cells, sys, st, a, cap, prune, half);
   const int ne = half ? launch_neighbors_half_emit(ex, sys, st, a, stream) : 0;
   // dense cells (sub-grid side >= 2), before the block-per-cell build, which takes the ones it passes on
   const int nsub = prune ? launch_neighbors_sub(ex, sys, st, a, cap, stream) : 0;
