@@ -1353,7 +1353,7 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
   };
   // the half-shell build is not searched: it allocates 27 x 8 bytes per particle
   // and measured slower than the lane-per-candidate build
-  const int caps[3] = {384, 640, 1024}, blocks[2] = {128, 256}, forms[2] = {XNB_BUILD_ROWS, XNB_BUILD_WARP},
+  const int caps[3] = {384, 640, 1024}, blocks[3] = {64, 128, 256}, forms[2] = {XNB_BUILD_ROWS, XNB_BUILD_WARP},
             lanes[3] = {1, 2, 4};
   int best_sc = b->stage_cap, best_fb = b->force_block, best_nw = 0, best_fl = b->force_lanes;
   int best_bf = b->build_form;  // kBuild* and XNB_BUILD_* share their values
@@ -1367,7 +1367,7 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
   // (neighbour-build form, the stage cap of the forms that stage whole
   // neighbourhoods, the force block size, threads per particle of the force
   // traversal and the Newton traversal)
-  const int nvals[5] = {2, 3, 2, 3, 2};
+  const int nvals[5] = {2, 3, 3, 3, 2};
   for (int pass = 0; pass < 5 && rc == 0; ++pass) {
     for (int v = 0; v < nvals[pass] && rc == 0; ++v) {
       int sc = best_sc, fb = best_fb, nw = best_nw, bf = best_bf, fl = best_fl;

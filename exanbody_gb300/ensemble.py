@@ -96,7 +96,7 @@ def autotune(systems, precision=xnb.PREC_MIXED, steps=40, tune_skin=False, strea
     space = {
         "build_form": ["warp", "rows"],
         "stage_cap": [384, 640, 1024],
-        "force_block": [128, 256],
+        "force_block": [64, 128, 256],
         "force_lanes": [1, 2, 4],
         "newton": [False, True],
         "skin": [0.3, 0.4, 0.5] if tune_skin else [0.3],

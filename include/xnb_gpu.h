@@ -281,7 +281,7 @@ int xnb_batch_set_subcell_pruning(xnb_batch* b, int32_t on);
 /* Changes the launch configuration of a live batch (same limits as at creation). */
 int xnb_batch_set_tuning(xnb_batch* b, int32_t stage_cap, int32_t force_block);
 /* Online autotuner: coordinate search over the neighbour-build form
- * {ROWS, WARP}, stage_cap {384, 640, 1024}, force_block {128, 256}, force
+ * {ROWS, WARP}, stage_cap {384, 640, 1024}, force_block {64, 128, 256}, force
  * threads per particle {1, 2, 4} and the Newton traversal (the batch's force
  * form is kept), each configuration timed
  * (CUDA events on `stream`) over trial_steps of xnb_step without host sync
