@@ -661,6 +661,7 @@ __global__ void __launch_bounds__(128)
   const uint32_t wib = threadIdx.x >> 5;
   const uint32_t nwarp = blockDim.x >> 5;
   float4* srel = stage_w + static_cast<size_t>(wib) * cap;
+  __shared__ uint32_t sink[4][kWarpP];  // hits of systems without list slots (blocks of 4 warps)
   const unsigned lt = lanemask_lt();
   uint32_t acc_s = kInvalid, acc_max = 0;
   unsigned long long acc_sum = 0;
@@ -780,8 +781,11 @@ __global__ void __launch_bounds__(128)
       const uint32_t i0 = sa + p0;
       const uint32_t self0 = ((i0 - S.part_base) << 5) | static_cast<uint32_t>(kImageCenter);
       const uint32_t low0 = off_self + p0;
-      // hits go straight to the particles' slots (consecutive particles, stride slot)
-      uint32_t* const pslot = seg + static_cast<size_t>(i0 - S.part_base) * slot;
+      // hits go straight to the particles' slots (consecutive particles, stride
+      // slot); a system without slots yet (the sizing build) only counts, its
+      // hits landing in the warp's sink
+      uint32_t* const pslot = slot ? seg + static_cast<size_t>(i0 - S.part_base) * slot : sink[wib];
+      const uint32_t pstride = slot ? slot : 1u;
       for (uint32_t t0 = 0; t0 < mpad; t0 += 32) {
         const float4 b = srel[t0 + lane];
         const uint32_t ent = __float_as_uint(b.w);
@@ -791,16 +795,16 @@ __global__ void __launch_bounds__(128)
         if (__any_sync(0xffffffffu, ent - kAmbiguousBit < kInvalid - kAmbiguousBit)) {
           if (self_chunk)
             nbr_chunk<kWarpP, true, true>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, pslot,
-                                          slot, cur, half);
+                                          pstride, cur, half);
           else
             nbr_chunk<kWarpP, true, false>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, pslot,
-                                           slot, cur, half);
+                                           pstride, cur, half);
         } else if (self_chunk) {
           nbr_chunk<kWarpP, false, true>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, pslot,
-                                         slot, cur, half);
+                                         pstride, cur, half);
         } else {
           nbr_chunk<kWarpP, false, false>(S, a, b, px, py, pz, i0, self0, t0, low0, nb_lo, nb_hi, nb_zero, lt, pslot,
-                                          slot, cur, half);
+                                          pstride, cur, half);
         }
       }
 #pragma unroll

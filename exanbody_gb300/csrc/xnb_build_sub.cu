@@ -78,6 +78,7 @@ __global__ void __launch_bounds__(128)
                        static_cast<size_t>(wib) * cap;
   const unsigned full = 0xffffffffu;
   const unsigned lt = lanemask_lt();
+  __shared__ uint32_t sink[4][kNbrP];  // hits of systems without list slots (blocks of 4 warps)
   uint32_t acc_s = kInvalid, acc_max = 0;
   unsigned long long acc_sum = 0;
   const uint32_t n_sub = min(*a.nbr_sub_n, n_cells);
@@ -242,7 +243,9 @@ __global__ void __launch_bounds__(128)
           const uint32_t i0 = sa + p0;
           const uint32_t self0 = ((i0 - S.part_base) << 5) | static_cast<uint32_t>(kImageCenter);
           const uint32_t low0 = self_pos + (p0 - a0);
-          uint32_t* const pslot = seg + static_cast<size_t>(i0 - S.part_base) * slot;
+          // a system without slots yet (the sizing build) only counts: its hits land in the sink
+          uint32_t* const pslot = slot ? seg + static_cast<size_t>(i0 - S.part_base) * slot : sink[wib];
+          const uint32_t pstride = slot ? slot : 1u;
           for (uint32_t t0 = 0; t0 < mpad; t0 += 32) {
             const float4 b = srel[t0 + lane];
             const uint32_t ent = __float_as_uint(b.w);
@@ -250,16 +253,16 @@ __global__ void __launch_bounds__(128)
             const bool self_chunk = u0 < low0 + kNbrP && low0 < u0 + 32u;
             if (__any_sync(full, ent - kAmbiguousBit < kInvalid - kAmbiguousBit)) {
               if (self_chunk)
-                nbr_chunk<kNbrP, true, true>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, slot,
+                nbr_chunk<kNbrP, true, true>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, pstride,
                                       cur, half);
               else
-                nbr_chunk<kNbrP, true, false>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, slot,
+                nbr_chunk<kNbrP, true, false>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, pstride,
                                        cur, half);
             } else if (self_chunk) {
-              nbr_chunk<kNbrP, false, true>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, slot,
+              nbr_chunk<kNbrP, false, true>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, pstride,
                                      cur, half);
             } else {
-              nbr_chunk<kNbrP, false, false>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, slot,
+              nbr_chunk<kNbrP, false, false>(S, a, b, px, py, pz, i0, self0, u0, low0, nb_lo, nb_hi, nb_zero, lt, pslot, pstride,
                                       cur, half);
             }
           }

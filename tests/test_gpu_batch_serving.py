@@ -15,7 +15,7 @@ def test_autotuner_trials_and_choice():
     best, rate, log = ensemble.autotune(systems, xnb.PREC_MIXED, steps=20)
     assert rate > 0 and len(log) >= 4
     assert rate == max(t["rate"] for t in log if all(t[k] == best[k] for k in best))
-    assert best["stage_cap"] in (384, 640, 1024) and best["force_block"] in (128, 256)
+    assert best["stage_cap"] in (384, 640, 1024) and best["force_block"] in (64, 128, 256)
     assert best["build_form"] in ("warp", "rows") and best["force_lanes"] in (1, 2, 4)
 
 

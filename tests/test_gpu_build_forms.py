@@ -59,3 +59,29 @@ def test_build_form_lists_equal_the_oracle(form, n, rho, T, seed, steps):
     assert e <= 1e-12, e
     b.check_errors()
     b.close()
+
+
+@pytest.mark.parametrize("form,factor", [(xnb.BUILD_WARP, 1.0), (xnb.BUILD_ROWS, 1.0), (xnb.BUILD_HALF, 1.0),
+                                         (xnb.BUILD_WARP, 2.0)])
+def test_sizing_build_of_a_new_system_leaves_resident_lists_alone(form, factor):
+    """A system added to a batch is first built without list slots (the build
+    that sizes them): its hits must go nowhere. The resident system's lists,
+    which may start at the same offset of the list pool, stay as they were
+    (warp, rows and half-shell forms; sub-cell pruned cells with factor 2)."""
+    wa = workloads.lj_fcc_system(10, 0.8442, 1.44, 31, cell_factor=factor)
+    wb = workloads.lj_fcc_system(8, 0.9, 1.2, 32, cell_factor=factor)
+    b = new_batch([wa["n_atoms"], wb["n_atoms"]], [ncells(wa["geom"]), ncells(wb["geom"])], max_systems=2)
+    b.set_build_form(form)
+    sa = b.add_system(xnb.lj_params(wa["geom"]), wa["r"], wa["v"], wa["id"])
+    b.init_particles(sa, xnb.PREC_MIXED)
+    before = b.pairs(sa)
+    sb = b.add_system(xnb.lj_params(wb["geom"]), wb["r"], wb["v"], wb["id"])
+    b.init_particles(sb, xnb.PREC_MIXED)
+    after = b.pairs(sa)
+    for x, y in zip(before, after):
+        assert np.array_equal(x, y)
+    o = oracle_from(wb)
+    o.init()
+    compare_pairs_sliced(b, sb, o, b.download(sb))
+    b.check_errors()
+    b.close()
