@@ -654,8 +654,13 @@ int xnb_system_add(xnb_batch* b, const xnb_lj_params* p, int64_t n, const double
   SysState zero{};
   XCK(cudaMemcpyAsync(b->d_st + slot, &zero, sizeof(SysState), cudaMemcpyHostToDevice, st));
   sh.active = true;
+  b->h_st[slot] = zero;  // the host mirror may still hold a previous occupant's state
   rc = upload_desc(b, slot, st);
   if (rc) return rc;
+  // list slots from the uniform-fluid estimate, so that the first build usually
+  // fits in one pass (a larger count regrows them as before); when the pool has
+  // no room now, the first build sizes them
+  if (size_lists(b, slot, 0, st) != XNB_OK) g_err.clear();
   // the caller's arrays and the host staging are pageable: finish the copies before returning
   XCK(cudaStreamSynchronize(st));
   *sys_out = slot;
