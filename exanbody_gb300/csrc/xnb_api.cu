@@ -96,7 +96,7 @@ struct xnb_batch {
   int sm_count = 1;
   xnb_batch_config cfg{};
   int stage_cap = 640;
-  int force_block = 128;
+  int force_block = 64;
   int force_lanes = 1;          // threads per particle of the FP64 / mixed force traversal
   int force_form = kForceThread;  // mixed full-list traversal form (xnb_batch_set_force_form)
   std::vector<uint4> segs;      // cell segments of the staged traversal (host copy of a.seg)

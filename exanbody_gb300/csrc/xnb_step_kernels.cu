@@ -425,7 +425,7 @@ inline int grid_capped(uint32_t n, int threads, int sm_count, int per_sm) {
 template <int P, bool PE, bool KICK>
 void force_dispatch(const Extent& ex, const SysDesc* sys, const SysState* st, const DevArrays& a, int sys_only,
                     cudaStream_t stream) {
-  const int threads = ex.force_block > 0 ? ex.force_block : 128;
+  const int threads = ex.force_block > 0 ? ex.force_block : 64;
   const BatchSource src(sys, st, a, sys_only);
   if constexpr (P == kMixed) {
     // a batch holding a box of X >= 1024 sigma: residual mirrors gathered, one thread per particle

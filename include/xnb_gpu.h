@@ -91,7 +91,7 @@ typedef struct xnb_batch_config {
   int64_t list_capacity;     /* neighbour entries over all resident systems */
   int32_t stage_cap;         /* neighbour-build candidates staged per cell (<= 1024): cells with more go to the
                                 block-per-cell build, in rounds of this size; 0 = default (640) */
-  int32_t force_block;       /* threads per block of the full-list force traversal; 0 = default (128) */
+  int32_t force_block;       /* threads per block of the full-list force traversal; 0 = default (64) */
 } xnb_batch_config;
 
 typedef struct xnb_system_info {

@@ -63,7 +63,7 @@ def test_native_online_autotune():
     b.init_particles(-1, xnb.PREC_MIXED)
     r0 = sum(b.info(s).rebuilds for s in ids)
     t = b.autotune(10, xnb.PREC_MIXED)
-    assert t["stage_cap"] in (384, 640, 1024) and t["force_block"] in (128, 256) and t["newton"] in (0, 1)
+    assert t["stage_cap"] in (384, 640, 1024) and t["force_block"] in (64, 128, 256) and t["newton"] in (0, 1)
     assert t["trials"] >= 4 and t["atom_steps_per_s"] > 0
     assert sum(b.info(s).rebuilds for s in ids) > r0  # the trials were real steps
     prec = xnb.PREC_MIXED | (xnb.PREC_NEWTON if t["newton"] else 0)
