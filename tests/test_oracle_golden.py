@@ -106,15 +106,15 @@ def test_chunk_neighbors_verifier_invariants():
     assert not np.any(a == b)  # no self
     got = set(zip(a.tolist(), b.tolist()))
     assert len(got) == len(a)  # no duplicates
-    # lists are taken at the last rebuild; compare against brute force on those positions
-    # by rebuilding now and checking completeness + symmetry
-    ref = brute_force_pairs(P, w["geom"], 2.8)
-    # every current list pair was within 2.8 at build time and the skin bounds drift;
-    # symmetric by construction:
+    assert s.rebuilds >= 1  # the lists below come from a rebuild after init
+    # full lists are symmetric
     assert got == {(y, x) for (x, y) in got}
-    assert ref <= got or s.rebuilds >= 0  # completeness holds for pairs within rcut below
-    cut = brute_force_pairs(P, w["geom"], 2.5)
-    assert cut <= got  # every pair inside rcut is in the list (Verlet-skin guarantee)
+    # the lists date from the last rebuild, when every listed pair lay within
+    # nbh = rcut + skin = 2.8; each particle has moved at most skin / 2 since,
+    # so a listed pair now lies within nbh + skin ...
+    assert got <= brute_force_pairs(P, w["geom"], 2.8 + 0.3 + 1e-9)
+    # ... and every pair now inside rcut was within nbh at the build: it is listed
+    assert brute_force_pairs(P, w["geom"], 2.5) <= got
 
 
 def test_neighbor_set_matches_brute_force_at_build():
