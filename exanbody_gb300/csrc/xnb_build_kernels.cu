@@ -650,9 +650,12 @@ __global__ void __launch_bounds__(128, 8)
 // warp-uniform branches: a chunk holding a candidate whose ghost filter is
 // undecided in FP32, and an FP32 distance inside the error band around nbh^2
 // (both then take the reference's FP64 decision, as in k_neighbors).
-constexpr int kWarpP = 8;  // particles tested per staged candidate load in the warp-per-cell build
+// Six particles per staged load fit 96 registers (8 bytes spilled), so 5 blocks
+// of 4 warps stay resident per SM (5 x 40 KB of stage at cap 640); eight per
+// load need 126 registers and hold 4 blocks, and take 13% longer per rebuild.
+constexpr int kWarpP = 6;  // particles tested per staged candidate load in the warp-per-cell build
 
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 5)
     k_neighbors_warp(uint32_t n_cells, const SysDesc* __restrict__ sys, SysState* st, DevArrays a, int cap,
                      bool prune, bool half_form) {
   if (*a.any_rebuild == 0) return;

@@ -248,7 +248,7 @@ int xnb_batch_set_force_form(xnb_batch* b, int32_t form);
  *   x-adjacent cells, each cell's mirrors one bulk copy (cp.async.bulk) into
  *   shared memory, the next row's copy in flight while the current row is tested.
  * XNB_BUILD_WARP: one warp per cell, one lane per candidate; the whole 27-cell
- *   block (up to stage_cap candidates) staged by the warp, eight particles tested
+ *   block (up to stage_cap candidates) staged by the warp, six particles tested
  *   per staged load with a ballot each.
  * Cells neither form takes (more than 64 particles, or candidates over the
  * stage) are built block-per-cell. */
