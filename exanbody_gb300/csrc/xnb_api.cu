@@ -1374,14 +1374,18 @@ int xnb_autotune(xnb_batch* b, int32_t trial_steps, int32_t precision, void* str
   // traversal and the Newton traversal)
   const int nvals[5] = {2, 3, 3, 3, 2};
   for (int pass = 0; pass < 5 && rc == 0; ++pass) {
+    // the pass's knob at its value when the pass starts was timed already (the
+    // other knobs stay as they are through the pass): it is not timed again
+    // after another value of the knob took the lead
+    const int timed = pass == 0 ? best_bf : pass == 1 ? best_sc : pass == 2 ? best_fb : pass == 3 ? best_fl : best_nw;
     for (int v = 0; v < nvals[pass] && rc == 0; ++v) {
-      int sc = best_sc, fb = best_fb, nw = best_nw, bf = best_bf, fl = best_fl;
-      if (pass == 0) bf = forms[v];
-      else if (pass == 1) sc = caps[v];
-      else if (pass == 2) fb = blocks[v];
-      else if (pass == 3) fl = lanes[v];
-      else nw = v;
-      if (sc == best_sc && fb == best_fb && nw == best_nw && bf == best_bf && fl == best_fl) continue;
+      int sc = best_sc, fb = best_fb, nw = best_nw, bf = best_bf, fl = best_fl, val = 0;
+      if (pass == 0) bf = val = forms[v];
+      else if (pass == 1) sc = val = caps[v];
+      else if (pass == 2) fb = val = blocks[v];
+      else if (pass == 3) fl = val = lanes[v];
+      else nw = val = v;
+      if (val == timed) continue;
       double r = 0.0;
       rc = rate_of(sc, fb, nw, bf, fl, best_ff, &r);
       if (rc == 0 && r > best) {

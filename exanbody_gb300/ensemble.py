@@ -105,8 +105,9 @@ def autotune(systems, precision=xnb.PREC_MIXED, steps=40, tune_skin=False, strea
     best_rate = trial(systems, best, steps, precision, stream)
     log = [dict(best, rate=best_rate)]
     for key in ("build_form", "stage_cap", "force_block", "force_lanes", "newton", "skin"):
+        measured = best[key]  # this knob's value in the configuration already timed
         for v in space[key]:
-            if v == best[key]:
+            if v == measured:
                 continue
             cand = dict(best, **{key: v})
             rate = trial(systems, cand, steps, precision, stream)
