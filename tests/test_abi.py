@@ -32,6 +32,23 @@ def test_binding_covers_header():
     assert set(declared("xnb_gpu.h")) == set(xnb.EXPORTED)
 
 
+def test_binding_constants_equal_header_defines():
+    """Every XNB_* value the header defines has the same value in the binding
+    (xnb.NAME for XNB_NAME); the include guard and XNB_OK (0, checked by _ck)
+    are the only defines without a twin."""
+    text = open(os.path.join(ROOT, "include", "xnb_gpu.h")).read()
+    defines = re.findall(r"^#define\s+XNB_([A-Z0-9_]+)\s+\(?\s*(-?(?:0x[0-9a-fA-F]+|\d+))u?\s*\)?", text, flags=re.M)
+    assert len(defines) >= 20
+    checked = 0
+    for name, value in defines:
+        if name == "OK":
+            continue
+        assert hasattr(xnb, name), "XNB_%s has no binding constant" % name
+        assert getattr(xnb, name) == int(value, 0), name
+        checked += 1
+    assert checked == len(defines) - 1
+
+
 def test_dump_header_symbols_exported_and_bound():
     lib = ctypes.CDLL(build.build())
     names = declared("xnb_dump.h")
